@@ -1,0 +1,184 @@
+// k_kk.cu -- Kramers-Kronig transform as a GEMM against a fixed kernel.
+//
+// Reference: genReChi0/genImChi0 (Chi_RPA/Optabs.f90:1112-1318) and genChi0
+// (W/Sloss.f90:954-1059).  For every output frequency io = 1..no-1 and every
+// (G,G') the reference sums fact(io,jo) * S0(..) over jo with end-point
+// corrections.  Those weights depend only on (io, jo, no, domega), so they
+// are tabulated once into a kernel matrix K (rows io, columns = rows of S0)
+// by kk_matrix() below, which restates the reference's branch structure
+// verbatim -- including the difference between the two drivers: Optabs uses
+// independent `if`s (end-point overrides apply) while Sloss uses an
+// `if (jo /= io) ... else if` chain (overrides only reach jo == io).
+// chi0 = K S0 - i pi S0(io-1) is then one GEMM per q with the pi term in the
+// epilogue.
+
+#include "rpa_internal.cuh"
+
+namespace rpa {
+
+// Kernel matrix K[(no-1) x nw] for the given variant (row-major).
+void kk_matrix(int variant, int no, double domega, std::vector<double>& K, int* nw_out) {
+  if (variant == RPA_KK_SLOSS_REAL) {
+    const int nw = no;
+    K.assign((size_t)(no - 1) * nw, 0.0);
+    for (int io = 1; io <= no - 1; ++io) {
+      double oi = (io - 1) * domega;
+      double* row = K.data() + (size_t)(io - 1) * nw;
+      if (io == 1) {
+        for (int jo = 2; jo <= no; ++jo) {
+          double oj = (jo - 1) * domega;
+          double fact = domega / oj;
+          if (jo == 2) fact = 3.0 / 2.0;
+          else if (jo == no) fact = 0.5 * domega / oj;
+          row[jo - 1] += -2.0 * fact;
+        }
+      } else {
+        for (int jo = 1; jo <= no; ++jo) {
+          double oj = (jo - 1) * domega;
+          double fm = (jo != io) ? domega / (oi - oj) : 0.0;
+          double fp = domega / (oi + oj);
+          if (jo == 1 || jo == no) fp = 0.5 * domega / (oi + oj);
+          row[jo - 1] += fm - fp;
+        }
+      }
+    }
+    *nw_out = nw;
+  } else {
+    const int nw = 2 * no + 1;
+    K.assign((size_t)(no - 1) * nw, 0.0);
+    for (int io = 1; io <= no - 1; ++io) {
+      double oi = (io - 1) * domega;
+      double* row = K.data() + (size_t)(io - 1) * nw;
+      // column of S0(j) is j + no
+      if (io == 1) {
+        for (int jo = 2; jo <= no; ++jo) {
+          double oj = (jo - 1) * domega;
+          double fact = domega / oj;
+          if (jo == 2) fact = 3.0 / 2.0;
+          else if (jo == no) fact = 0.5 * domega / oj;
+          row[(-jo + 1) + no] += fact;
+          row[(jo - 1) + no] -= fact;
+        }
+        continue;
+      }
+      double fact = 0.0;
+      for (int jo = 1; jo <= no; ++jo) {
+        double oj = (jo - 1) * domega;
+        if (io == 2) {
+          if (jo != io) fact = domega / (oi - oj);
+          if (jo == 1) fact = 1.0;
+          else if (jo == 2) fact = 0.0;
+          else if (jo == 3) fact = -3.0 / 2.0;
+          else if (jo == no) fact = 0.5 * domega / (oi - oj);
+        } else if (io == no - 1) {
+          if (jo != io) fact = domega / (oi - oj);
+          if (jo == 1) fact = 0.5 * domega / (oi - oj);
+          else if (jo == no - 2) fact = 3.0 / 2.0;
+          else if (jo == no - 1) fact = 0.0;
+          else if (jo == no) fact = -1.0;
+        } else {
+          if (jo != io) fact = domega / (oi - oj);
+          if (jo == 1) fact = 0.5 * domega / (oi - oj);
+          else if (jo == io - 1) fact = 3.0 / 2.0;
+          else if (jo == io) fact = 0.0;
+          else if (jo == io + 1) fact = -3.0 / 2.0;
+          else if (jo == no) fact = 0.5 * domega / (oi - oj);
+        }
+        row[(jo - 1) + no] += fact;
+        double fp = domega / (oi + oj);
+        if (jo == 1 || jo == no) fp = 0.5 * domega / (oi + oj);
+        row[(-jo + 1) + no] += fp;
+        fact = fp;  // Fortran carries the last assigned value of `fact`
+      }
+    }
+    *nw_out = nw;
+  }
+}
+
+// out[io0][p] = sum_r K[io0][r] S[r][col] with the -i pi S(row(io0)) epilogue.
+// S is viewed as [nw][ncols] doubles (ncols = np for real S, 2 np for complex).
+template <bool CPLX>
+__global__ void __launch_bounds__(256) k_kk_fp64(const double* __restrict__ K, const double* __restrict__ S,
+                                                 double2* __restrict__ out, int nrow, int nw, int np,
+                                                 int pi_row0) {
+  constexpr int BM = 32, BN = 64, BK = 16;
+  __shared__ double Ks[BK][BM + 1];
+  __shared__ double Ss[BK][BN];
+  const int ncols = CPLX ? 2 * np : np;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+  for (int k0 = 0; k0 < nw; k0 += BK) {
+    for (int e = threadIdx.x; e < BM * BK; e += 256) {
+      int mm = e / BK, kk = e % BK;
+      int r = m0 + mm, k = k0 + kk;
+      Ks[kk][mm] = (r < nrow && k < nw) ? K[(size_t)r * nw + k] : 0.0;
+    }
+    for (int e = threadIdx.x; e < BK * BN; e += 256) {
+      int kk = e / BN, nn = e % BN;
+      int k = k0 + kk, col = n0 + nn;
+      Ss[kk][nn] = (k < nw && col < ncols) ? S[(size_t)k * ncols + col] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double a0 = Ks[kk][ty * 2], a1 = Ks[kk][ty * 2 + 1];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        double b = Ss[kk][tx * 4 + j];
+        acc[0][j] = fma(a0, b, acc[0][j]);
+        acc[1][j] = fma(a1, b, acc[1][j]);
+      }
+    }
+    __syncthreads();
+  }
+  const double pi = 3.141592653589793238462643383279502884;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    int r = m0 + ty * 2 + i;
+    if (r >= nrow) continue;
+    const double* srow = S + (size_t)(pi_row0 + r) * ncols;
+    if (CPLX) {
+#pragma unroll
+      for (int j = 0; j < 4; j += 2) {
+        int col = n0 + tx * 4 + j;
+        if (col >= ncols) continue;
+        int p = col >> 1;
+        double sr = srow[col], si = srow[col + 1];
+        out[(size_t)r * np + p] = make_double2(acc[i][j] + pi * si, acc[i][j + 1] - pi * sr);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        int col = n0 + tx * 4 + j;
+        if (col >= ncols) continue;
+        out[(size_t)r * np + col] = make_double2(acc[i][j], -pi * srow[col]);
+      }
+    }
+  }
+}
+
+int kk_run(rpa_ctx* c, int variant, int no, double domega) {
+  std::vector<double> K;
+  int nw = 0;
+  kk_matrix(variant, no, domega, K, &nw);
+  const int nrow = no - 1, np = c->nlf * c->nlf;
+  RPA_TRY(ensure(c, c->d_kk, sizeof(double) * K.size()));
+  RPA_CUDA(c, cudaMemcpyAsync(c->d_kk.p, K.data(), sizeof(double) * K.size(), cudaMemcpyHostToDevice, c->stream));
+  RPA_TRY(ensure(c, c->d_chi0, sizeof(double2) * (size_t)nrow * np));
+  const bool cplx = variant == RPA_KK_OPTABS_COMPLEX;
+  const int ncols = cplx ? 2 * np : np;
+  dim3 grid((ncols + 63) / 64, (nrow + 31) / 32);
+  // S row holding S0(io-1): Sloss row io-1 (io0), Optabs row (io-1)+no
+  const int pi_row0 = cplx ? no : 0;
+  if (cplx)
+    k_kk_fp64<true><<<grid, 256, 0, c->stream>>>(c->d_kk.as<double>(), c->d_S.as<double>(),
+                                                 c->d_chi0.as<double2>(), nrow, nw, np, pi_row0);
+  else
+    k_kk_fp64<false><<<grid, 256, 0, c->stream>>>(c->d_kk.as<double>(), c->d_S.as<double>(),
+                                                  c->d_chi0.as<double2>(), nrow, nw, np, pi_row0);
+  RPA_CUDA(c, cudaGetLastError());
+  return RPA_OK;
+}
+
+}  // namespace rpa

@@ -1,0 +1,720 @@
+// rpa_abi.cu -- the C ABI (include/rpa_gpu.h) and the host orchestration.
+//
+// The host side keeps the reference's drivers' contract: arrays arrive in
+// their Fortran layouts with 1-based indices, results leave in the same
+// layouts.  Everything between (occupations, transition lists, index maps,
+// vertices, S0, KK, Dyson) runs on the device of the context.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+
+#include "rpa_internal.cuh"
+
+namespace rpa {
+
+// stage implementations (k_*.cu)
+int count_pairs(rpa_ctx* c, const Chi0Plan& Pl, int k0, int nk, std::vector<int>& counts, int* maxp);
+int emit_pairs(rpa_ctx* c, const Chi0Plan& Pl, int k0, int nk, const std::vector<long long>& offsets,
+               long long n_trans, int* wmax_out, int* n_inter_out, double* winsum_out);
+int sort_trans(rpa_ctx* c, int n_trans, int nw);
+int vertices_fp64(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, long long n_trans);
+int accumulate_fp64(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax);
+int qeff_fp64(rpa_ctx* c, const Chi0Plan& P, int n_inter, int n_trans);
+int kk_run(rpa_ctx* c, int variant, int no, double domega);
+int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singular, int* n_zero);
+void kk_matrix(int variant, int no, double domega, std::vector<double>& K, int* nw_out);
+int gk_sort_host(const double* k, int npwx, int ngm, const double* g, double ecut, int* ngk, int* igk, double* gk);
+
+static thread_local std::string g_create_err;
+
+int fail(rpa_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  else g_create_err = buf;
+  return code;
+}
+
+int cuda_fail(rpa_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, e == cudaErrorMemoryAllocation ? RPA_ENOMEM : RPA_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int ensure(rpa_ctx* c, DevBuf& b, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (b.bytes >= bytes) return RPA_OK;
+  if (b.p) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+  }
+  cudaError_t e = cudaMalloc(&b.p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    b.p = nullptr;
+    return fail(c, RPA_ENOMEM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+  }
+  b.bytes = bytes;
+  return RPA_OK;
+}
+
+void release(DevBuf& b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_basis_transpose(const double2* __restrict__ src, double2* __restrict__ dst, int nkc, int nbnd,
+                                  int npwx) {
+  // src [k][b][i] (Fortran C(npwx,nbnd,nks)) -> dst [k][i][b]
+  size_t n = (size_t)nkc * nbnd * npwx;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    int b = (int)(e % nbnd);
+    size_t r = e / nbnd;
+    int i = (int)(r % npwx);
+    int k = (int)(r / npwx);
+    dst[e] = src[((size_t)k * nbnd + b) * npwx + i];
+  }
+}
+
+__global__ void k_build_inv(const int* __restrict__ gidx, const int* __restrict__ npw, int* __restrict__ inv,
+                            int nks, int npwx, int ng, int* bad) {
+  size_t n = (size_t)nks * npwx;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    int k = (int)(e / npwx), i = (int)(e % npwx);
+    if (i >= npw[k]) continue;
+    int g = gidx[e];
+    if (g < 0 || g >= ng) {
+      atomicExch(bad, 1);
+      continue;
+    }
+    if (atomicCAS(&inv[(size_t)k * ng + g], -1, i) != -1) atomicExch(bad, 2);
+  }
+}
+
+static void fill_identity_sym(rpa_ctx* c) {
+  c->nsym = 1;
+  c->h_R.assign(48 * 9, 0.0);
+  for (int i = 0; i < 3; ++i) c->h_R[0 + 48 * (i + 3 * i)] = 1.0;
+  c->h_RI = c->h_R;
+}
+
+static int upload_symmetry(rpa_ctx* c) {
+  // crystal matrices Rc = KC^-1 R KC (row-major [isym][i][j])
+  double K[9], Ki[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) K[3 * i + j] = c->KC[i + 3 * j];
+  double det = K[0] * (K[4] * K[8] - K[5] * K[7]) - K[1] * (K[3] * K[8] - K[5] * K[6]) + K[2] * (K[3] * K[7] - K[4] * K[6]);
+  if (std::fabs(det) < 1e-14) return fail(c, RPA_EINVAL, "reciprocal axes KC are singular");
+  Ki[0] = (K[4] * K[8] - K[5] * K[7]) / det;
+  Ki[1] = (K[2] * K[7] - K[1] * K[8]) / det;
+  Ki[2] = (K[1] * K[5] - K[2] * K[4]) / det;
+  Ki[3] = (K[5] * K[6] - K[3] * K[8]) / det;
+  Ki[4] = (K[0] * K[8] - K[2] * K[6]) / det;
+  Ki[5] = (K[2] * K[3] - K[0] * K[5]) / det;
+  Ki[6] = (K[3] * K[7] - K[4] * K[6]) / det;
+  Ki[7] = (K[1] * K[6] - K[0] * K[7]) / det;
+  Ki[8] = (K[0] * K[4] - K[1] * K[3]) / det;
+  c->h_Rc.assign(48 * 9, 0);
+  c->h_RIc.assign(48 * 9, 0);
+  std::vector<double> Rcart(48 * 9, 0.0);
+  for (int s = 0; s < c->nsym; ++s) {
+    for (int which = 0; which < 2; ++which) {
+      const std::vector<double>& Rf = which ? c->h_RI : c->h_R;
+      double R[9], T[9], X[9];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) R[3 * i + j] = Rf[s + 48 * (i + 3 * j)];
+      if (!which)
+        for (int e = 0; e < 9; ++e) Rcart[9 * s + e] = R[e];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double a = 0;
+          for (int k = 0; k < 3; ++k) a += R[3 * i + k] * K[3 * k + j];
+          T[3 * i + j] = a;
+        }
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double a = 0;
+          for (int k = 0; k < 3; ++k) a += Ki[3 * i + k] * T[3 * k + j];
+          X[3 * i + j] = a;
+        }
+      for (int e = 0; e < 9; ++e) {
+        double r = std::nearbyint(X[e]);
+        if (std::fabs(X[e] - r) > 1e-6)
+          return fail(c, RPA_EINVAL, "symmetry %d is not an integer matrix in crystal coordinates", s + 1);
+        (which ? c->h_RIc : c->h_Rc)[9 * s + e] = (int)r;
+      }
+    }
+  }
+  RPA_TRY(ensure(c, c->d_Rc, sizeof(int) * 48 * 9));
+  RPA_TRY(ensure(c, c->d_RIc, sizeof(int) * 48 * 9));
+  RPA_TRY(ensure(c, c->d_Rcart, sizeof(double) * 48 * 9));
+  RPA_CUDA(c, cudaMemcpy(c->d_Rc.p, c->h_Rc.data(), sizeof(int) * 48 * 9, cudaMemcpyHostToDevice));
+  RPA_CUDA(c, cudaMemcpy(c->d_RIc.p, c->h_RIc.data(), sizeof(int) * 48 * 9, cudaMemcpyHostToDevice));
+  RPA_CUDA(c, cudaMemcpy(c->d_Rcart.p, Rcart.data(), sizeof(double) * 48 * 9, cudaMemcpyHostToDevice));
+  return RPA_OK;
+}
+
+// genV, W/Sloss.f90:1173-1208 (q and Glf in 2pi/a0 units, converted with Gcar).
+static void genV_host(const rpa_ctx* c, double Gcar, double c0, double eps, std::vector<double>& V) {
+  const int n = c->nlf;
+  const double pi = 4.0 * std::atan(1.0);
+  V.assign((size_t)n * n, 0.0);
+  double qx = Gcar * c->q[0], qy = Gcar * c->q[1];
+  for (int iG = 0; iG < n; ++iG) {
+    const double* gi = &c->h_G[3 * (size_t)c->h_ilf[iG]];
+    double gvx = Gcar * gi[0], gvy = Gcar * gi[1], gvz = Gcar * gi[2];
+    double Gabs = std::sqrt((qx + gvx) * (qx + gvx) + (qy + gvy) * (qy + gvy));
+    if (Gabs == 0.0) Gabs = eps;
+    for (int jG = 0; jG < n; ++jG) {
+      const double* gj = &c->h_G[3 * (size_t)c->h_ilf[jG]];
+      double gjz = Gcar * gj[2];
+      double v = 0.0;
+      if (gj[0] == gi[0] && gj[1] == gi[1]) {
+        v = 4.0 * pi * (1.0 - std::exp(-Gabs * c0)) / (Gabs * c0);
+        v = v * (Gabs * Gabs - gvz * gjz);
+        v = v / (Gabs * Gabs + gvz * gvz);
+        v = v / (Gabs * Gabs + gjz * gjz);
+        v = -(double)c->h_parG[iG] * (double)c->h_parG[jG] * v;
+        if (gj[2] == gi[2]) v = 4.0 * pi / (Gabs * Gabs + gvz * gvz) + v;
+      }
+      V[iG + (size_t)n * jG] = v;
+    }
+  }
+}
+
+struct EvTimer {
+  rpa_ctx* c;
+  int a, b;
+  double* out;
+};
+
+static double elapsed(rpa_ctx* c, int a, int b) {
+  float ms = 0.f;
+  cudaEventSynchronize(c->ev[b]);
+  cudaEventElapsedTime(&ms, c->ev[a], c->ev[b]);
+  return ms;
+}
+
+}  // namespace rpa
+
+using namespace rpa;
+
+extern "C" {
+
+int rpa_create(rpa_ctx** out, const rpa_opts* opts) {
+  if (!out) return fail(nullptr, RPA_EINVAL, "rpa_create: out is NULL");
+  *out = nullptr;
+  int dev = opts ? opts->device : 0;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return fail(nullptr, RPA_ECUDA, "rpa_create: no CUDA device (%s)", cudaGetErrorString(e));
+  if (dev < 0 || dev >= ndev) return fail(nullptr, RPA_EINVAL, "rpa_create: device %d out of range", dev);
+  if (opts && opts->precision != RPA_PREC_FP64 && opts->precision != RPA_PREC_MIXED)
+    return fail(nullptr, RPA_EINVAL, "rpa_create: unknown precision %d", opts->precision);
+  e = cudaSetDevice(dev);
+  if (e != cudaSuccess) return fail(nullptr, RPA_ECUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+  rpa_ctx* c = new rpa_ctx();
+  c->device = dev;
+  c->precision = opts ? opts->precision : RPA_PREC_FP64;
+  c->verbose = opts ? opts->verbose : 0;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(nullptr, RPA_ECUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  for (auto& ev : c->ev) cudaEventCreate(&ev);
+  fill_identity_sym(c);
+  *out = c;
+  return RPA_OK;
+}
+
+int rpa_destroy(rpa_ctx* c) {
+  if (!c) return RPA_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  DevBuf* bufs[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
+                    &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_E, &c->d_kmap, &c->d_ktot, &c->d_lf_miller,
+                    &c->d_Glf, &c->d_occ, &c->d_counts, &c->d_offsets, &c->d_trans, &c->d_keys, &c->d_keys_alt,
+                    &c->d_vals, &c->d_vals_alt, &c->d_sorted, &c->d_M, &c->d_M2, &c->d_cub, &c->d_wmax,
+                    &c->d_ntrans, &c->d_S, &c->d_Q, &c->d_chi0, &c->d_kk, &c->d_V, &c->d_eps, &c->d_WT,
+                    &c->d_flags, &c->d_tmp};
+  for (DevBuf* b : bufs) release(*b);
+  for (auto& ev : c->ev)
+    if (ev) cudaEventDestroy(ev);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return RPA_OK;
+}
+
+const char* rpa_last_error(const rpa_ctx* c) { return c ? c->err.c_str() : g_create_err.c_str(); }
+
+int rpa_set_gvectors(rpa_ctx* c, int ng, const int* miller, const double* G, const double* KC) {
+  if (!c || ng <= 0 || !miller || !G || !KC) return fail(c, RPA_EINVAL, "rpa_set_gvectors: bad arguments");
+  cudaSetDevice(c->device);
+  if (miller[0] != 0 || miller[1] != 0 || miller[2] != 0)
+    return fail(c, RPA_EINVAL, "G(1) is not (0,0,0)");
+  c->ng = ng;
+  c->h_miller.assign(miller, miller + 3 * (size_t)ng);
+  c->h_G.assign(G, G + 3 * (size_t)ng);
+  std::memcpy(c->KC, KC, sizeof(double) * 9);
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  for (int g = 0; g < ng; ++g)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::min(lo[d], miller[3 * g + d]);
+      hi[d] = std::max(hi[d], miller[3 * g + d]);
+    }
+  size_t vol = 1;
+  for (int d = 0; d < 3; ++d) {
+    c->box_lo[d] = lo[d];
+    c->box_dim[d] = hi[d] - lo[d] + 1;
+    vol *= (size_t)c->box_dim[d];
+  }
+  if (vol > ((size_t)1 << 31)) return fail(c, RPA_EINVAL, "Miller index range too large");
+  std::vector<int> box(vol, -1);
+  for (int g = 0; g < ng; ++g) {
+    size_t idx = ((size_t)(miller[3 * g] - lo[0]) * c->box_dim[1] + (miller[3 * g + 1] - lo[1])) * c->box_dim[2] +
+                 (miller[3 * g + 2] - lo[2]);
+    if (box[idx] >= 0) return fail(c, RPA_EINVAL, "G vector %d repeats G vector %d", g + 1, box[idx] + 1);
+    box[idx] = g;
+  }
+  RPA_TRY(ensure(c, c->d_miller, sizeof(int) * 3 * (size_t)ng));
+  RPA_TRY(ensure(c, c->d_G, sizeof(double) * 3 * (size_t)ng));
+  RPA_TRY(ensure(c, c->d_box, sizeof(int) * vol));
+  RPA_CUDA(c, cudaMemcpy(c->d_miller.p, miller, sizeof(int) * 3 * (size_t)ng, cudaMemcpyHostToDevice));
+  RPA_CUDA(c, cudaMemcpy(c->d_G.p, G, sizeof(double) * 3 * (size_t)ng, cudaMemcpyHostToDevice));
+  RPA_CUDA(c, cudaMemcpy(c->d_box.p, box.data(), sizeof(int) * vol, cudaMemcpyHostToDevice));
+  return upload_symmetry(c);
+}
+
+int rpa_set_symmetry(rpa_ctx* c, int nsym, const double* R, const double* RI) {
+  if (!c || nsym < 1 || nsym > 48 || !R || !RI) return fail(c, RPA_EINVAL, "rpa_set_symmetry: bad arguments");
+  if (c->ng == 0) return fail(c, RPA_ESTATE, "rpa_set_symmetry: call rpa_set_gvectors first");
+  cudaSetDevice(c->device);
+  c->nsym = nsym;
+  c->h_R.assign(R, R + 48 * 9);
+  c->h_RI.assign(RI, RI + 48 * 9);
+  return upload_symmetry(c);
+}
+
+int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, const int* igk, const double* coeff,
+                   const double* E) {
+  if (!c || nks <= 0 || nbnd <= 0 || npwx <= 0 || !npw || !coeff || !E)
+    return fail(c, RPA_EINVAL, "rpa_load_basis: bad arguments");
+  if (c->ng == 0) return fail(c, RPA_ESTATE, "rpa_load_basis: call rpa_set_gvectors first");
+  if (nbnd > 4096) return fail(c, RPA_EINVAL, "rpa_load_basis: nbnd too large");
+  cudaSetDevice(c->device);
+  for (int k = 0; k < nks; ++k)
+    if (npw[k] < 1 || npw[k] > npwx) return fail(c, RPA_EINVAL, "npw(%d) = %d outside 1..npwx", k + 1, npw[k]);
+  c->nks = nks;
+  c->nbnd = nbnd;
+  c->npwx = npwx;
+  c->legacy = igk == nullptr;
+  c->h_npw.assign(npw, npw + nks);
+  if (c->legacy) {
+    for (int k = 0; k < nks; ++k)
+      if (npw[k] > c->ng) return fail(c, RPA_EINVAL, "npw(%d) exceeds NG in legacy mode", k + 1);
+  }
+  c->h_E.resize((size_t)nks * nbnd);
+  for (int k = 0; k < nks; ++k)
+    for (int b = 0; b < nbnd; ++b) c->h_E[(size_t)k * nbnd + b] = E[k + (size_t)nks * b];
+  cudaEventRecord(c->ev[6], c->stream);
+  RPA_TRY(ensure(c, c->d_npw, sizeof(int) * nks));
+  RPA_TRY(ensure(c, c->d_E, sizeof(double) * (size_t)nks * nbnd));
+  RPA_TRY(ensure(c, c->d_gidx, sizeof(int) * (size_t)nks * npwx));
+  RPA_CUDA(c, cudaMemcpyAsync(c->d_npw.p, npw, sizeof(int) * nks, cudaMemcpyHostToDevice, c->stream));
+  RPA_CUDA(c, cudaMemcpyAsync(c->d_E.p, c->h_E.data(), sizeof(double) * (size_t)nks * nbnd, cudaMemcpyHostToDevice,
+                              c->stream));
+  std::vector<int> gidx((size_t)nks * npwx);
+  for (int k = 0; k < nks; ++k)
+    for (int i = 0; i < npwx; ++i) gidx[(size_t)k * npwx + i] = igk ? igk[(size_t)k * npwx + i] - 1 : i;
+  RPA_CUDA(c, cudaMemcpyAsync(c->d_gidx.p, gidx.data(), sizeof(int) * gidx.size(), cudaMemcpyHostToDevice, c->stream));
+  if (!c->legacy) {
+    RPA_TRY(ensure(c, c->d_inv, sizeof(int) * (size_t)nks * c->ng));
+    RPA_TRY(ensure(c, c->d_flags, sizeof(int) * 4));
+    RPA_CUDA(c, cudaMemsetAsync(c->d_inv.p, 0xff, sizeof(int) * (size_t)nks * c->ng, c->stream));
+    RPA_CUDA(c, cudaMemsetAsync(c->d_flags.p, 0, sizeof(int) * 4, c->stream));
+    k_build_inv<<<1024, 256, 0, c->stream>>>(c->d_gidx.as<int>(), c->d_npw.as<int>(), c->d_inv.as<int>(), nks, npwx,
+                                             c->ng, c->d_flags.as<int>());
+    RPA_CUDA(c, cudaGetLastError());
+    int bad = 0;
+    RPA_CUDA(c, cudaMemcpyAsync(&bad, c->d_flags.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (bad == 1) return fail(c, RPA_EINVAL, "igk entry outside 1..NG");
+    if (bad == 2) return fail(c, RPA_EINVAL, "igk repeats a G vector within one k-point");
+  }
+  // coefficients: stage raw Fortran blocks and transpose to [k][i][b]
+  const size_t per_k = (size_t)nbnd * npwx;
+  RPA_TRY(ensure(c, c->d_coeff, sizeof(double2) * per_k * nks));
+  int kc = (int)std::max<size_t>(1, std::min<size_t>(nks, ((size_t)512 << 20) / (sizeof(double2) * per_k)));
+  RPA_TRY(ensure(c, c->d_tmp, sizeof(double2) * per_k * kc));
+  for (int k0 = 0; k0 < nks; k0 += kc) {
+    int nk = std::min(kc, nks - k0);
+    RPA_CUDA(c, cudaMemcpyAsync(c->d_tmp.p, coeff + 2 * per_k * k0, sizeof(double2) * per_k * nk,
+                                cudaMemcpyHostToDevice, c->stream));
+    k_basis_transpose<<<2048, 256, 0, c->stream>>>(c->d_tmp.as<double2>(), c->d_coeff.as<double2>() + per_k * k0, nk,
+                                                   nbnd, npwx);
+    RPA_CUDA(c, cudaGetLastError());
+  }
+  cudaEventRecord(c->ev[7], c->stream);
+  RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->stage_ms[5] = elapsed(c, 6, 7);
+  c->have_S = c->have_chi0 = false;
+  return RPA_OK;
+}
+
+int rpa_kmap(rpa_ctx* c, int ntot, const double* ktot, const int* K1, const int* R1, const int* K2, const int* R2,
+             const int* iG0) {
+  if (!c || ntot <= 0 || !ktot || !K1 || !R1 || !K2 || !R2 || !iG0)
+    return fail(c, RPA_EINVAL, "rpa_kmap: bad arguments");
+  if (c->nks == 0) return fail(c, RPA_ESTATE, "rpa_kmap: call rpa_load_basis first");
+  cudaSetDevice(c->device);
+  std::vector<int> km(5 * (size_t)ntot);
+  for (int k = 0; k < ntot; ++k) {
+    int v[5] = {K1[k] - 1, R1[k] - 1, K2[k] - 1, R2[k] - 1, iG0[k] - 1};
+    if (v[0] < 0 || v[0] >= c->nks || v[2] < 0 || v[2] >= c->nks)
+      return fail(c, RPA_EINVAL, "K1/K2 of k-point %d outside 1..nks", k + 1);
+    if (v[1] < 0 || v[1] >= c->nsym || v[3] < 0 || v[3] >= c->nsym)
+      return fail(c, RPA_EINVAL, "R1/R2 of k-point %d outside 1..Nsym", k + 1);
+    if (v[4] < 0 || v[4] >= c->ng) return fail(c, RPA_EINVAL, "iG0 of k-point %d outside 1..NG", k + 1);
+    for (int j = 0; j < 5; ++j) km[5 * (size_t)k + j] = v[j];
+  }
+  c->ntot = ntot;
+  c->h_kmap.swap(km);
+  c->h_ktot.assign(ktot, ktot + 3 * (size_t)ntot);
+  RPA_TRY(ensure(c, c->d_kmap, sizeof(int) * 5 * (size_t)ntot));
+  RPA_TRY(ensure(c, c->d_ktot, sizeof(double) * 3 * (size_t)ntot));
+  RPA_CUDA(c, cudaMemcpy(c->d_kmap.p, c->h_kmap.data(), sizeof(int) * 5 * (size_t)ntot, cudaMemcpyHostToDevice));
+  RPA_CUDA(c, cudaMemcpy(c->d_ktot.p, ktot, sizeof(double) * 3 * (size_t)ntot, cudaMemcpyHostToDevice));
+  c->have_S = c->have_chi0 = false;
+  return RPA_OK;
+}
+
+int rpa_set_q(rpa_ctx* c, const double* q, int nlf, const int* ilf, const int* parG) {
+  if (!c || !q || nlf <= 0 || !ilf) return fail(c, RPA_EINVAL, "rpa_set_q: bad arguments");
+  if (nlf > 1000) return fail(c, RPA_EINVAL, "Nlf = %d exceeds the gjel limit NMAX = 1000", nlf);
+  if (c->ng == 0) return fail(c, RPA_ESTATE, "rpa_set_q: call rpa_set_gvectors first");
+  cudaSetDevice(c->device);
+  std::vector<int> lm(3 * (size_t)nlf), il(nlf), pg(nlf, 1);
+  std::vector<double> gl(3 * (size_t)nlf);
+  for (int i = 0; i < nlf; ++i) {
+    int g = ilf[i] - 1;
+    if (g < 0 || g >= c->ng) return fail(c, RPA_EINVAL, "ilf(%d) outside 1..NG", i + 1);
+    il[i] = g;
+    for (int d = 0; d < 3; ++d) {
+      lm[3 * i + d] = c->h_miller[3 * (size_t)g + d];
+      gl[3 * i + d] = c->h_G[3 * (size_t)g + d];
+    }
+    if (parG) {
+      if (parG[i] != 1 && parG[i] != -1) return fail(c, RPA_EINVAL, "parG(%d) must be +1 or -1", i + 1);
+      pg[i] = parG[i];
+    }
+  }
+  c->h_ilf.swap(il);
+  c->h_parG.swap(pg);
+  for (int d = 0; d < 3; ++d) c->q[d] = q[d];
+  c->nlf = nlf;
+  RPA_TRY(ensure(c, c->d_lf_miller, sizeof(int) * 3 * (size_t)nlf));
+  RPA_TRY(ensure(c, c->d_Glf, sizeof(double) * 3 * (size_t)nlf));
+  RPA_CUDA(c, cudaMemcpy(c->d_lf_miller.p, lm.data(), sizeof(int) * lm.size(), cudaMemcpyHostToDevice));
+  RPA_CUDA(c, cudaMemcpy(c->d_Glf.p, gl.data(), sizeof(double) * gl.size(), cudaMemcpyHostToDevice));
+  c->have_q = true;
+  c->have_S = c->have_chi0 = false;
+  return RPA_OK;
+}
+
+int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_out) {
+  if (!c || !a) return fail(c, RPA_EINVAL, "rpa_chi0: bad arguments");
+  if (c->nks == 0 || c->ntot == 0 || !c->have_q)
+    return fail(c, RPA_ESTATE, "rpa_chi0: basis, k map and q must be set first");
+  if (a->mode != RPA_MODE_CHARGE && a->mode != RPA_MODE_CURRENT)
+    return fail(c, RPA_EINVAL, "rpa_chi0: unknown mode %d", a->mode);
+  if (a->pol < RPA_POL_XX || a->pol > RPA_POL_ZY) return fail(c, RPA_EINVAL, "rpa_chi0: unknown pol %d", a->pol);
+  if (a->no < 3) return fail(c, RPA_EINVAL, "rpa_chi0: no must be >= 3");
+  if (!(a->domega > 0) || !(a->eta > 0) || !(a->Vcell > 0)) return fail(c, RPA_EINVAL, "rpa_chi0: domega, eta, Vcell must be > 0");
+  if (a->mode == RPA_MODE_CHARGE && (a->nocc < 1 || a->nocc >= c->nbnd))
+    return fail(c, RPA_EINVAL, "rpa_chi0: nocc must be in 1..nbnd-1");
+  if (a->mode == RPA_MODE_CURRENT && !(a->T > 0)) return fail(c, RPA_EINVAL, "rpa_chi0: T must be > 0");
+  if (c->precision != RPA_PREC_FP64)
+    return fail(c, RPA_EINVAL, "rpa_chi0: this context precision has no accumulation path");
+  cudaSetDevice(c->device);
+
+  Chi0Plan P;
+  P.mode = a->mode;
+  P.pol = a->pol;
+  P.no = a->no;
+  P.nw = a->mode == RPA_MODE_CHARGE ? a->no : 2 * a->no + 1;
+  P.wbase = a->mode == RPA_MODE_CHARGE ? 0 : -a->no;
+  P.nocc = a->nocc;
+  P.domega = a->domega;
+  P.eta = a->eta;
+  P.cut = a->mode == RPA_MODE_CHARGE ? 1.0e-3 : a->lor_cut;
+  P.df_cut = a->df_cut;
+  P.T = a->T;
+  P.Efermi = a->Efermi;
+  P.Gcar = a->Gcar;
+  P.ntot_norm = a->ntot_norm > 0 ? a->ntot_norm : c->ntot;
+  const double pi = 4.0 * std::atan(1.0);
+  P.norm_s = pi * P.ntot_norm * a->Vcell;
+  P.norm_q = P.ntot_norm * a->Vcell;
+  P.nsum_legacy = 0;
+  if (c->legacy) {
+    if (a->ngd < 1) return fail(c, RPA_EINVAL, "rpa_chi0: NGd must be >= 1 without an igk map");
+    for (int k = 0; k < c->ntot; ++k) {
+      int K1 = c->h_kmap[5 * k], K2 = c->h_kmap[5 * k + 2];
+      if (a->ngd > c->h_npw[K1]) return fail(c, RPA_EINVAL, "NGd is bigger than NG1=%d", c->h_npw[K1]);
+      if (a->ngd > c->h_npw[K2]) return fail(c, RPA_EINVAL, "NGd is bigger than NG2=%d", c->h_npw[K2]);
+    }
+    P.nsum_legacy = a->ngd;
+  }
+
+  // occupations (genOccupation, Optabs.f90:935-951) and Qeff prefactors on the host
+  {
+    std::vector<double> occ(2 * (size_t)c->nks * c->nbnd, 0.0);
+    if (a->mode == RPA_MODE_CURRENT) {
+      for (size_t i = 0; i < (size_t)c->nks * c->nbnd; ++i) {
+        double x = (c->h_E[i] - a->Efermi) / a->T, expo, f;
+        if (x < -20) {
+          expo = 0.0;
+          f = 1.0;
+        } else if (x > 20) {
+          expo = x;
+          f = 0.0;
+        } else {
+          expo = std::exp(x);
+          f = 1.0 / (expo + 1.0);
+        }
+        double fact = expo / ((expo + 1.0) * (expo + 1.0));
+        fact = -fact / a->T;
+        occ[2 * i] = f;
+        occ[2 * i + 1] = 2.0 * fact / P.norm_q;
+      }
+    }
+    RPA_TRY(ensure(c, c->d_occ, sizeof(double) * occ.size()));
+    RPA_CUDA(c, cudaMemcpyAsync(c->d_occ.p, occ.data(), sizeof(double) * occ.size(), cudaMemcpyHostToDevice, c->stream));
+  }
+  const int np = c->nlf * c->nlf;
+  const bool cplx = a->mode == RPA_MODE_CURRENT;
+  const size_t s_bytes = (size_t)P.nw * np * (cplx ? 16 : 8);
+  RPA_TRY(ensure(c, c->d_S, s_bytes));
+  RPA_TRY(ensure(c, c->d_Q, sizeof(double2) * np));
+  RPA_CUDA(c, cudaMemsetAsync(c->d_S.p, 0, s_bytes, c->stream));
+  RPA_CUDA(c, cudaMemsetAsync(c->d_Q.p, 0, sizeof(double2) * np, c->stream));
+
+  double t_pairs = 0, t_vert = 0, t_acc = 0;
+  double st_trans = 0, st_win = 0, st_mac = 0, st_launch = 0;
+  std::vector<int> counts;
+  int maxp = 0;
+  cudaEventRecord(c->ev[0], c->stream);
+  RPA_TRY(count_pairs(c, P, 0, c->ntot, counts, &maxp));
+  // k chunks bounded by the vertex buffer budget
+  const bool two = cplx && (a->pol == RPA_POL_YZ || a->pol == RPA_POL_ZY);
+  const size_t per_trans = (size_t)c->nlf * sizeof(double2) * (two ? 2 : 1) + sizeof(Trans) + 16;
+  const size_t budget = (size_t)6 << 30;
+  size_t max_trans = std::max<size_t>(budget / per_trans, (size_t)maxp + 1);
+  max_trans = std::min<size_t>(max_trans, (size_t)1 << 30);
+  int k0 = 0;
+  while (k0 < c->ntot) {
+    long long tot = 0;
+    int k1 = k0;
+    while (k1 < c->ntot && (size_t)(tot + counts[k1]) <= max_trans) tot += counts[k1++];
+    if (k1 == k0) return fail(c, RPA_EINVAL, "rpa_chi0: one k-point exceeds the transition budget");
+    int nk = k1 - k0;
+    std::vector<long long> off(nk + 1, 0);
+    for (int i = 0; i < nk; ++i) off[i + 1] = off[i] + counts[k0 + i];
+    int wmax = 0, n_inter = 0;
+    double winsum = 0;
+    cudaEventRecord(c->ev[1], c->stream);
+    RPA_TRY(emit_pairs(c, P, k0, nk, off, tot, &wmax, &n_inter, &winsum));
+    RPA_TRY(sort_trans(c, (int)tot, P.nw));
+    cudaEventRecord(c->ev[2], c->stream);
+    RPA_TRY(vertices_fp64(c, P, k0, nk, maxp, tot));
+    cudaEventRecord(c->ev[3], c->stream);
+    RPA_TRY(accumulate_fp64(c, P, n_inter, wmax));
+    if (cplx) RPA_TRY(qeff_fp64(c, P, n_inter, (int)tot));
+    cudaEventRecord(c->ev[4], c->stream);
+    RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+    t_pairs += elapsed(c, 1, 2);
+    t_vert += elapsed(c, 2, 3);
+    t_acc += elapsed(c, 3, 4);
+    st_trans += (double)n_inter;
+    st_win += winsum;
+    st_launch += 1;
+    for (int i = 0; i < nk; ++i) {
+      int K1 = c->h_kmap[5 * (size_t)(k0 + i)];
+      st_mac += (double)counts[k0 + i] * c->nlf * (c->legacy ? P.nsum_legacy : c->h_npw[K1]);
+    }
+    k0 = k1;
+  }
+  cudaEventRecord(c->ev[5], c->stream);
+  RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->stage_ms[0] = t_pairs;
+  c->stage_ms[1] = t_vert;
+  c->stage_ms[2] = t_acc;
+  c->stats[0] = st_trans;
+  c->stats[1] = st_win;
+  c->stats[2] = st_mac;
+  c->stats[3] = st_launch;
+  c->last_mode = a->mode;
+  c->last_no = a->no;
+  c->last_nw = P.nw;
+  c->last_domega = a->domega;
+  c->last_Gcar = a->Gcar;
+  c->have_S = true;
+  c->have_chi0 = false;
+  // results to the host, in the Fortran layouts
+  double t_io = 0;
+  if (S0_out || Qeff_out) {
+    cudaEventRecord(c->ev[6], c->stream);
+    if (S0_out) {
+      RPA_TRY(ensure(c, c->d_tmp, s_bytes));
+      launch_transpose_wp_to_fortran(c->d_S.as<double>(), c->d_tmp.as<double>(), P.nw, np, cplx ? 2 : 1, c->stream);
+      RPA_CUDA(c, cudaGetLastError());
+      RPA_CUDA(c, cudaMemcpyAsync(S0_out, c->d_tmp.p, s_bytes, cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (Qeff_out && cplx)
+      RPA_CUDA(c, cudaMemcpyAsync(Qeff_out, c->d_Q.p, sizeof(double2) * np, cudaMemcpyDeviceToHost, c->stream));
+    cudaEventRecord(c->ev[7], c->stream);
+    RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+    t_io = elapsed(c, 6, 7);
+  }
+  c->stage_ms[5] = t_io;
+  return RPA_OK;
+}
+
+int rpa_kk(rpa_ctx* c, int variant, double* chi0_out) {
+  if (!c) return fail(c, RPA_EINVAL, "rpa_kk: ctx is NULL");
+  if (!c->have_S) return fail(c, RPA_ESTATE, "rpa_kk: no S0 on the device (call rpa_chi0 first)");
+  if (variant != RPA_KK_OPTABS_COMPLEX && variant != RPA_KK_SLOSS_REAL)
+    return fail(c, RPA_EINVAL, "rpa_kk: unknown variant %d", variant);
+  if ((variant == RPA_KK_OPTABS_COMPLEX) != (c->last_mode == RPA_MODE_CURRENT))
+    return fail(c, RPA_EINVAL, "rpa_kk: variant does not match the S0 on the device");
+  cudaSetDevice(c->device);
+  cudaEventRecord(c->ev[0], c->stream);
+  RPA_TRY(kk_run(c, variant, c->last_no, c->last_domega));
+  cudaEventRecord(c->ev[1], c->stream);
+  RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->stage_ms[3] = elapsed(c, 0, 1);
+  c->have_chi0 = true;
+  if (chi0_out) {
+    const int nwo = c->last_no - 1, np = c->nlf * c->nlf;
+    RPA_TRY(ensure(c, c->d_tmp, sizeof(double2) * (size_t)nwo * np));
+    cudaEventRecord(c->ev[6], c->stream);
+    launch_transpose_wp_to_fortran(c->d_chi0.as<double>(), c->d_tmp.as<double>(), nwo, np, 2, c->stream);
+    RPA_CUDA(c, cudaGetLastError());
+    RPA_CUDA(c, cudaMemcpyAsync(chi0_out, c->d_tmp.p, sizeof(double2) * (size_t)nwo * np, cudaMemcpyDeviceToHost,
+                                c->stream));
+    cudaEventRecord(c->ev[7], c->stream);
+    RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->stage_ms[5] = elapsed(c, 6, 7);
+  }
+  return RPA_OK;
+}
+
+int rpa_dyson(rpa_ctx* c, double c0, double eps, double* WT_out, double* epsinv_out, double* head_out) {
+  if (!c) return fail(c, RPA_EINVAL, "rpa_dyson: ctx is NULL");
+  if (!c->have_chi0) return fail(c, RPA_ESTATE, "rpa_dyson: no chi0 on the device (call rpa_kk first)");
+  if (!(c0 > 0)) return fail(c, RPA_EINVAL, "rpa_dyson: c0 must be > 0");
+  cudaSetDevice(c->device);
+  std::vector<double> V;
+  genV_host(c, c->last_Gcar, c0, eps, V);
+  int nsing = 0, nzero = 0;
+  cudaEventRecord(c->ev[0], c->stream);
+  RPA_TRY(dyson_fp64(c, V.data(), epsinv_out != nullptr, &nsing, &nzero));
+  cudaEventRecord(c->ev[1], c->stream);
+  RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->stage_ms[4] = elapsed(c, 0, 1);
+  const int nwo = c->last_no - 1, np = c->nlf * c->nlf;
+  const int grid_used = (int)((c->d_tmp.bytes / sizeof(double2) - (nwo + 1)) / (3 * (size_t)np));
+  (void)grid_used;
+  cudaEventRecord(c->ev[6], c->stream);
+  if (head_out) {
+    // heads live right after the per-block scratch of the Dyson kernel
+    int dev_sms = 0;
+    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device);
+    int grid = nwo < 2 * dev_sms ? nwo : 2 * dev_sms;
+    const double2* head = c->d_tmp.as<double2>() + (size_t)grid * 3 * np;
+    RPA_CUDA(c, cudaMemcpyAsync(head_out, head, sizeof(double2) * nwo, cudaMemcpyDeviceToHost, c->stream));
+  }
+  RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (WT_out || epsinv_out) {
+    // d_tmp is reused for the transposes; heads were copied above
+    RPA_TRY(ensure(c, c->d_tmp, sizeof(double2) * (size_t)nwo * np));
+    if (WT_out) {
+      launch_transpose_wp_to_fortran(c->d_WT.as<double>(), c->d_tmp.as<double>(), nwo, np, 2, c->stream);
+      RPA_CUDA(c, cudaGetLastError());
+      RPA_CUDA(c, cudaMemcpyAsync(WT_out, c->d_tmp.p, sizeof(double2) * (size_t)nwo * np, cudaMemcpyDeviceToHost,
+                                  c->stream));
+      RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    if (epsinv_out) {
+      launch_transpose_wp_to_fortran(c->d_eps.as<double>(), c->d_tmp.as<double>(), nwo, np, 2, c->stream);
+      RPA_CUDA(c, cudaGetLastError());
+      RPA_CUDA(c, cudaMemcpyAsync(epsinv_out, c->d_tmp.p, sizeof(double2) * (size_t)nwo * np,
+                                  cudaMemcpyDeviceToHost, c->stream));
+    }
+  }
+  cudaEventRecord(c->ev[7], c->stream);
+  RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->stage_ms[5] = elapsed(c, 6, 7);
+  if (nsing) return fail(c, RPA_ESINGULAR, "singular matrix in gjel at %d frequencies", nsing);
+  if (nzero && c->verbose) fprintf(stderr, "rpa_dyson: singular matrix in gjel (zero pivot) at %d frequencies\n", nzero);
+  return RPA_OK;
+}
+
+int rpa_gfast(rpa_ctx* c, int ik, int ngd, int* out) {
+  if (!c || !out) return fail(c, RPA_EINVAL, "rpa_gfast: bad arguments");
+  if (c->ntot == 0 || !c->have_q) return fail(c, RPA_ESTATE, "rpa_gfast: k map and q must be set first");
+  if (ik < 1 || ik > c->ntot) return fail(c, RPA_EINVAL, "rpa_gfast: ik outside 1..Ntot");
+  if (c->legacy && ngd < 1) return fail(c, RPA_EINVAL, "rpa_gfast: NGd must be >= 1 without an igk map");
+  cudaSetDevice(c->device);
+  return build_gfast(c, ik - 1, ngd, out);
+}
+
+int rpa_init_igk(int nks, const double* xk, int npwx, int ngm, const double* g, double gcutw, int* igk_k, int* ngk) {
+  if (nks <= 0 || !xk || npwx <= 0 || ngm <= 0 || !g || !igk_k || !ngk) return RPA_EINVAL;
+  std::vector<double> gk(npwx);
+  for (int ik = 0; ik < nks; ++ik) {
+    int rc = gk_sort_host(xk + 3 * (size_t)ik, npwx, ngm, g, gcutw, &ngk[ik], igk_k + (size_t)npwx * ik, gk.data());
+    if (rc != 0) return RPA_EINVAL;
+  }
+  return RPA_OK;
+}
+
+int rpa_kk_matrix(int variant, int no, double domega, double* K) {
+  if (!K || no < 3 || !(domega > 0)) return RPA_EINVAL;
+  if (variant != RPA_KK_OPTABS_COMPLEX && variant != RPA_KK_SLOSS_REAL) return RPA_EINVAL;
+  std::vector<double> k;
+  int nw = 0;
+  kk_matrix(variant, no, domega, k, &nw);
+  std::memcpy(K, k.data(), sizeof(double) * k.size());
+  return RPA_OK;
+}
+
+int rpa_stage_times(const rpa_ctx* c, double* ms6) {
+  if (!c || !ms6) return RPA_EINVAL;
+  for (int i = 0; i < 6; ++i) ms6[i] = c->stage_ms[i];
+  return RPA_OK;
+}
+
+int rpa_chi0_stats(const rpa_ctx* c, double* out4) {
+  if (!c || !out4) return RPA_EINVAL;
+  for (int i = 0; i < 4; ++i) out4[i] = c->stats[i];
+  return RPA_OK;
+}
+
+int rpa_synchronize(rpa_ctx* c) {
+  if (!c) return RPA_EINVAL;
+  cudaSetDevice(c->device);
+  RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+  return RPA_OK;
+}
+
+}  // extern "C"

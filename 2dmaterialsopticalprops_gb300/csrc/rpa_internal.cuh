@@ -1,0 +1,128 @@
+// rpa_internal.cuh -- shared state and helpers of the GB300 RPA library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/rpa_gpu.h"
+
+namespace rpa {
+
+// ---------------------------------------------------------------------------
+// Device buffer that only grows.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  template <class T>
+  T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// One transition (n, m) of one FBZ k-point that contributes to S0 or Qeff.
+// e1 = E(K1,n), e2 = E(K2,m) are kept apart so that dE = (o + e1) - e2 is
+// formed in the reference's operation order (Sloss.f90:410, Optabs.f90:391).
+struct Trans {
+  int k;      // FBZ index within the current k-chunk
+  int nm;     // n | (m << 16), 0-based bands
+  int lo;     // first frequency row of the Lorentzian window (row index)
+  int hi;     // last frequency row (inclusive)
+  double e1;
+  double e2;
+  double c;   // prefactor: S0 += c * L(io) * M conj(M2) (inter) or Qeff += c M conj(M2) (intra)
+};
+
+static constexpr int KEY_INTRA = 0x7fffffff;
+
+}  // namespace rpa
+
+struct rpa_ctx {
+  int device = 0;
+  int precision = RPA_PREC_FP64;
+  int verbose = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  // G list
+  int ng = 0;
+  std::vector<int> h_miller;  // 3*ng
+  std::vector<double> h_G;    // 3*ng
+  double KC[9] = {0};
+  int box_lo[3] = {0, 0, 0}, box_dim[3] = {0, 0, 0};
+  rpa::DevBuf d_miller, d_G, d_box;
+
+  // symmetry (crystal-coordinate integer matrices, row-major [isym][3][3])
+  int nsym = 0;
+  std::vector<double> h_R, h_RI;  // Fortran R(48,3,3)
+  std::vector<int> h_Rc, h_RIc;   // 48*9
+  rpa::DevBuf d_Rc, d_RIc, d_Rcart;
+
+  // basis
+  int nks = 0, nbnd = 0, npwx = 0;
+  bool legacy = false;
+  std::vector<int> h_npw;
+  std::vector<double> h_E;        // [k][b]
+  rpa::DevBuf d_npw, d_gidx, d_inv, d_coeff, d_coeff32, d_E;
+
+  // k map
+  int ntot = 0;
+  std::vector<int> h_kmap;        // 5*ntot: K1,R1,K2,R2,iG0 (0-based)
+  std::vector<double> h_ktot;
+  rpa::DevBuf d_kmap, d_ktot;
+
+  // q
+  bool have_q = false;
+  double q[3] = {0, 0, 0};
+  int nlf = 0;
+  std::vector<int> h_ilf, h_parG;
+  rpa::DevBuf d_lf_miller, d_Glf;
+
+  // per-call scratch
+  rpa::DevBuf d_occ, d_counts, d_offsets, d_trans, d_keys, d_keys_alt, d_vals, d_vals_alt, d_sorted,
+      d_M, d_M2, d_cub, d_wmax, d_ntrans;
+  // results
+  int last_mode = -1, last_no = 0, last_nw = 0;
+  double last_domega = 0.0, last_Gcar = 0.0;
+  bool have_S = false, have_chi0 = false;
+  rpa::DevBuf d_S, d_Q, d_chi0, d_kk, d_V, d_eps, d_WT, d_flags, d_tmp;
+  double stage_ms[6] = {0, 0, 0, 0, 0, 0};
+  double stats[4] = {0, 0, 0, 0};
+  cudaEvent_t ev[8] = {};
+};
+
+namespace rpa {
+
+int fail(rpa_ctx* c, int code, const char* fmt, ...);
+int cuda_fail(rpa_ctx* c, cudaError_t e, const char* what);
+int ensure(rpa_ctx* c, DevBuf& b, size_t bytes);
+void release(DevBuf& b);
+
+#define RPA_CUDA(ctx, call)                                   \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return rpa::cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+#define RPA_TRY(x)            \
+  do {                        \
+    int rc_ = (x);            \
+    if (rc_ != RPA_OK) return rc_; \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Stage entry points (implemented in the k_*.cu files).
+struct Chi0Plan {
+  int mode, pol, no, nw, wbase;  // nw = rows of S0 (no or 2no+1); row r <-> io = r + wbase
+  int nocc, nsum_legacy;
+  double domega, eta, cut, df_cut, T, Efermi, norm_s, norm_q, Gcar;
+  int ntot_norm;
+};
+
+int build_gfast(rpa_ctx* c, int ik, int nsum_legacy, int* out);
+
+// device layout transposes between [w][p] (library) and (w fastest) Fortran
+void launch_transpose_wp_to_fortran(const double* src, double* dst, int nw, int np, int ncomp,
+                                    cudaStream_t s);
+
+}  // namespace rpa

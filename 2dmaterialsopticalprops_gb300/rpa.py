@@ -1,0 +1,261 @@
+"""ctypes binding of librpa_gb300.so (the C ABI of include/rpa_gpu.h).
+
+This is the Python mirror of what the Fortran drivers bind through
+ISO_C_BINDING: every call passes the drivers' own Fortran-layout arrays.
+The library must be built (``build.build()``); there is no fallback path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librpa_gb300.so")
+
+RPA_OK, RPA_EINVAL, RPA_ENOMEM, RPA_ESINGULAR, RPA_ETIMEOUT, RPA_ECUDA, RPA_ESTATE, RPA_ENOTFOUND = (
+    0, -1, -2, -3, -4, -5, -6, -7)
+PREC_FP64, PREC_MIXED = 0, 1
+MODE_CHARGE, MODE_CURRENT = 0, 1
+POL = {"xx": 0, "yy": 1, "zz": 2, "yz": 3, "zy": 4}
+KK_OPTABS_COMPLEX, KK_SLOSS_REAL = 1, 2
+
+EXPORTS = ["rpa_create", "rpa_destroy", "rpa_last_error", "rpa_set_gvectors", "rpa_set_symmetry",
+           "rpa_load_basis", "rpa_kmap", "rpa_set_q", "rpa_chi0", "rpa_kk", "rpa_dyson", "rpa_gfast",
+           "rpa_init_igk", "rpa_kk_matrix", "rpa_stage_times", "rpa_chi0_stats", "rpa_synchronize"]
+
+
+class RpaOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("verbose", C.c_int), ("reserved", C.c_int * 5)]
+
+
+class RpaChi0Args(C.Structure):
+    _fields_ = [("mode", C.c_int), ("pol", C.c_int), ("ngd", C.c_int), ("nocc", C.c_int), ("no", C.c_int),
+                ("ntot_norm", C.c_int), ("domega", C.c_double), ("eta", C.c_double), ("lor_cut", C.c_double),
+                ("df_cut", C.c_double), ("T", C.c_double), ("Efermi", C.c_double), ("Vcell", C.c_double),
+                ("Gcar", C.c_double)]
+
+
+class RpaError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"rpa error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with 2dmaterialsopticalprops_gb300/build.py")
+    L = C.CDLL(path)
+    vp, ip, dp = C.c_void_p, C.c_int, C.c_double
+    L.rpa_create.argtypes = [C.POINTER(vp), C.POINTER(RpaOpts)]
+    L.rpa_destroy.argtypes = [vp]
+    L.rpa_last_error.argtypes = [vp]
+    L.rpa_last_error.restype = C.c_char_p
+    L.rpa_set_gvectors.argtypes = [vp, ip, vp, vp, vp]
+    L.rpa_set_symmetry.argtypes = [vp, ip, vp, vp]
+    L.rpa_load_basis.argtypes = [vp, ip, ip, ip, vp, vp, vp, vp]
+    L.rpa_kmap.argtypes = [vp, ip, vp, vp, vp, vp, vp, vp]
+    L.rpa_set_q.argtypes = [vp, vp, ip, vp, vp]
+    L.rpa_chi0.argtypes = [vp, C.POINTER(RpaChi0Args), vp, vp]
+    L.rpa_kk.argtypes = [vp, ip, vp]
+    L.rpa_dyson.argtypes = [vp, dp, dp, vp, vp, vp]
+    L.rpa_gfast.argtypes = [vp, ip, ip, vp]
+    L.rpa_init_igk.argtypes = [ip, vp, ip, ip, vp, dp, vp, vp]
+    L.rpa_kk_matrix.argtypes = [ip, ip, dp, vp]
+    L.rpa_stage_times.argtypes = [vp, vp]
+    L.rpa_chi0_stats.argtypes = [vp, vp]
+    L.rpa_synchronize.argtypes = [vp]
+    for name in EXPORTS:
+        if name != "rpa_last_error":
+            getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def init_igk(xk: np.ndarray, g: np.ndarray, gcutw: float, npwx: int):
+    """init_igk (Modules/qe_gksort.f90:11-42) through the library's host code.
+
+    xk (nks,3), g (ngm,3) in 2pi/alat units.  Returns (igk (nks,npwx), ngk (nks,))."""
+    L = load_library()
+    xk = np.ascontiguousarray(xk, dtype=np.float64)
+    g = np.ascontiguousarray(g, dtype=np.float64)
+    nks = xk.shape[0]
+    igk = np.zeros((nks, npwx), dtype=np.int32)
+    ngk = np.zeros(nks, dtype=np.int32)
+    rc = L.rpa_init_igk(nks, _p(xk), npwx, g.shape[0], _p(g), float(gcutw), _p(igk), _p(ngk))
+    if rc != RPA_OK:
+        raise RpaError(rc, "init_igk: npwx too small or G list too short")
+    return igk, ngk
+
+
+def kk_matrix(variant: int, no: int, domega: float) -> np.ndarray:
+    """The KK kernel matrix rpa_kk applies (host code, no device needed)."""
+    L = load_library()
+    nw = no if variant == KK_SLOSS_REAL else 2 * no + 1
+    K = np.zeros((no - 1, nw), dtype=np.float64)
+    rc = L.rpa_kk_matrix(variant, no, float(domega), _p(K))
+    if rc != RPA_OK:
+        raise RpaError(rc, "rpa_kk_matrix: bad arguments")
+    return K
+
+
+class Context:
+    """One rpa_ctx: resident basis + per-q state, Fortran-layout I/O."""
+
+    def __init__(self, device: int = 0, precision: int = PREC_FP64, verbose: int = 0):
+        self.L = load_library()
+        self.h = C.c_void_p()
+        opts = RpaOpts(device=device, precision=precision, verbose=verbose)
+        rc = self.L.rpa_create(C.byref(self.h), C.byref(opts))
+        if rc != RPA_OK:
+            raise RpaError(rc, self.L.rpa_last_error(None).decode())
+        self.precision = precision
+        self.nlf = 0
+        self.no = 0
+        self.mode = None
+
+    def _chk(self, rc: int):
+        if rc != RPA_OK:
+            raise RpaError(rc, self.L.rpa_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.L.rpa_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- setup ---------------------------------------------------------------
+    def set_gvectors(self, miller, G, KC):
+        mil = np.ascontiguousarray(miller, dtype=np.int32)
+        G = np.ascontiguousarray(G, dtype=np.float64)
+        KC = np.asfortranarray(KC, dtype=np.float64)
+        self._chk(self.L.rpa_set_gvectors(self.h, mil.shape[0], _p(mil), _p(G), _p(KC)))
+
+    def set_symmetry(self, nsym, R, RI):
+        R = np.asfortranarray(R, dtype=np.float64)
+        RI = np.asfortranarray(RI, dtype=np.float64)
+        self._chk(self.L.rpa_set_symmetry(self.h, nsym, _p(R), _p(RI)))
+
+    def load_basis(self, npw, igk, coeff, E):
+        """npw (nks,), igk (nks,npwx) 1-based or None, coeff (nks,nbnd,npwx) complex, E (nbnd,nks) Ha."""
+        npw = np.ascontiguousarray(npw, dtype=np.int32)
+        coeff = np.ascontiguousarray(coeff, dtype=np.complex128)
+        nks, nbnd, npwx = coeff.shape
+        igk_a = None if igk is None else np.ascontiguousarray(igk, dtype=np.int32)
+        E = np.ascontiguousarray(E, dtype=np.float64)
+        self._chk(self.L.rpa_load_basis(self.h, nks, nbnd, npwx, _p(npw), _p(igk_a), _p(coeff), _p(E)))
+
+    def kmap(self, ktot, K1, R1, K2, R2, iG0):
+        ktot = np.ascontiguousarray(ktot, dtype=np.float64)
+        arrs = [np.ascontiguousarray(x, dtype=np.int32) for x in (K1, R1, K2, R2, iG0)]
+        self._chk(self.L.rpa_kmap(self.h, ktot.shape[0], _p(ktot), *[_p(a) for a in arrs]))
+
+    def set_q(self, q, ilf, parG=None):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        ilf = np.ascontiguousarray(ilf, dtype=np.int32)
+        par = None if parG is None else np.ascontiguousarray(parG, dtype=np.int32)
+        self._chk(self.L.rpa_set_q(self.h, _p(q), ilf.size, _p(ilf), _p(par)))
+        self.nlf = ilf.size
+
+    def load_system(self, s):
+        """All setup calls for a synth.System (what a driver does before its q loop)."""
+        self.set_gvectors(s.miller, s.G, s.KC)
+        self.load_basis(s.npw, s.igk, s.coeff, s.E)
+        self.kmap(s.ktot, s.K1, s.R1, s.K2, s.R2, s.iG0)
+        self.set_q(s.q, s.ilf, s.parG)
+        self.sys = s
+
+    # -- the hot path ----------------------------------------------------------
+    def chi0(self, mode: int, *, no: int, domega: float, eta: float, Vcell: float, Gcar: float, pol: str = "xx",
+             ngd: int = 0, nocc: int = 0, lor_cut: float = 1e-3, df_cut: float = 1e-4, T: float = 0.0,
+             Efermi: float = 0.0, ntot_norm: int = 0, want: bool = True):
+        args = RpaChi0Args(mode=mode, pol=POL[pol], ngd=ngd, nocc=nocc, no=no, ntot_norm=ntot_norm, domega=domega,
+                           eta=eta, lor_cut=lor_cut, df_cut=df_cut, T=T, Efermi=Efermi, Vcell=Vcell, Gcar=Gcar)
+        nlf = self.nlf
+        S0 = Q = None
+        if want:
+            if mode == MODE_CURRENT:
+                S0 = np.zeros((nlf, nlf, 2 * no + 1), dtype=np.complex128)
+                Q = np.zeros((nlf, nlf), dtype=np.complex128)
+            else:
+                S0 = np.zeros((nlf, nlf, no), dtype=np.float64)
+        self._chk(self.L.rpa_chi0(self.h, C.byref(args), _p(S0), _p(Q)))
+        self.no = no
+        self.mode = mode
+        return S0, Q
+
+    def kk(self, variant: int, want: bool = True):
+        out = np.zeros((self.nlf, self.nlf, self.no - 1), dtype=np.complex128) if want else None
+        self._chk(self.L.rpa_kk(self.h, variant, _p(out)))
+        return out
+
+    def dyson(self, c0: float, eps: float, want_wt: bool = True, want_epsinv: bool = False, want_head: bool = True):
+        n, nw = self.nlf, self.no - 1
+        WT = np.zeros((n, n, nw), dtype=np.complex128) if want_wt else None
+        Ei = np.zeros((n, n, nw), dtype=np.complex128) if want_epsinv else None
+        head = np.zeros(nw, dtype=np.complex128) if want_head else None
+        rc = self.L.rpa_dyson(self.h, c0, eps, _p(WT), _p(Ei), _p(head))
+        self._chk(rc)
+        return WT, Ei, head
+
+    def gfast(self, ik1: int, ngd: int = 0) -> np.ndarray:
+        s = self.sys
+        K1 = int(s.K1[ik1 - 1])
+        nsum = int(s.npw[K1 - 1]) if s.igk is not None else ngd
+        out = np.zeros(self.nlf * nsum, dtype=np.int32)
+        self._chk(self.L.rpa_gfast(self.h, ik1, ngd, _p(out)))
+        return out.reshape(self.nlf, nsum)
+
+    def stage_times(self):
+        out = np.zeros(6)
+        self._chk(self.L.rpa_stage_times(self.h, _p(out)))
+        return dict(zip(["pairs", "vertices", "accumulate", "kk", "dyson", "copies"], out.tolist()))
+
+    def chi0_stats(self):
+        out = np.zeros(4)
+        self._chk(self.L.rpa_chi0_stats(self.h, _p(out)))
+        return dict(zip(["transitions", "sum_nwin", "vertex_macs", "chunks"], out.tolist()))
+
+    def synchronize(self):
+        self._chk(self.L.rpa_synchronize(self.h))
+
+
+def sloss_args(s) -> dict:
+    """rpa_chi0 arguments of the Sloss driver for a synth.System."""
+    return dict(no=s.no, domega=s.domega, eta=s.eta, Vcell=s.Vcell, Gcar=s.Gcar, nocc=s.nocc,
+                ngd=0 if s.igk is not None else s.ngd)
+
+
+def optabs_args(s, pol: str = "xx") -> dict:
+    """rpa_chi0 arguments of the Optabs driver for a synth.System."""
+    c = s.cfg
+    return dict(no=s.no, domega=s.domega, eta=s.eta, Vcell=s.Vcell, Gcar=s.Gcar, pol=pol, lor_cut=c.lor_cut,
+                df_cut=c.df_cut, T=s.T, Efermi=s.Efermi, ngd=0 if s.igk is not None else s.ngd)
+
+
+def relerr(a: np.ndarray, b: np.ndarray) -> tuple[float, float]:
+    """(max |a-b| / max |b|, ||a-b||_2 / ||b||_2)."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    nb = float(np.max(np.abs(b))) if b.size else 0.0
+    if nb == 0.0:
+        return float(np.max(np.abs(a - b))) if a.size else 0.0, 0.0
+    return float(np.max(np.abs(a - b)) / nb), float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))

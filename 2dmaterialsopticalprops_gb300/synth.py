@@ -1,0 +1,363 @@
+"""Seeded synthetic Bloch bases in the layout the RPA drivers hand to the library.
+
+The reference reads Quantum ESPRESSO outputs (gvectors.xml / charge-density.dat
+for the G list, one coefficient record per band and k-point, a bands.x energy
+file, the reciprocal axes and symmetry block of scf.out).  No QE run exists
+here, so this module builds the same arrays from a seeded random model:
+
+* a 2D hexagonal cell (lattice constant ``a_ang``, cell height ``c_ang``),
+  reciprocal axes KC in 2pi/a0 units (columns b1, b2, b3 as `loadKC` returns
+  them, Chi_RPA/Optabs.f90:652-680);
+* the G list: Miller triples inside a density sphere, sorted by |G|^2 with
+  G(1) = 0 as `loadG` requires (Optabs.f90:1061-1110);
+* per IBZ k-point, the k+G basis ordered by QE's gk_sort (Modules/qe_gksort.f90)
+  or, in legacy mode, the first ``npw`` entries of the G list for every k;
+* band energies from a nearest-neighbour tight-binding dispersion (hopping
+  ``t_eV``) stacked into ``nbnd`` bands around E_F = 0, plus N(0, 0.1 eV)
+  offsets;
+* coefficients drawn N(0,1) and orthonormalised per k-point (QR);
+* the identity point group (Nsym = 1), so the FBZ equals the IBZ grid, and
+  the K = R1*K1, K+Q = G0 + R2*K2 bookkeeping computed by integer arithmetic
+  on the Monkhorst-Pack grid (commensurate q), or, for q off the grid, a
+  second seeded basis at the shifted points k+q, as a QE nscf run would give.
+
+Arrays are kept in NumPy C order with the Fortran index order reversed, so
+that ``arr.ctypes.data`` is the Fortran column-major array the drivers pass
+(e.g. ``coeff`` has shape (nks, nbnd, npwx) == Fortran C(npwx, nbnd, nks)).
+"""
+from __future__ import annotations
+
+import concurrent.futures as _cf
+import math
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HARTREE_EV = 2.0 * 13.6056923  # Optabs.f90:50
+BOHR_ANG = 0.5291772  # Optabs.f90:52
+
+
+@dataclass
+class SynthConfig:
+    nk: int = 24                 # nk x nk Monkhorst-Pack grid (Gamma centred)
+    nbnd: int = 8
+    nocc: int = 4
+    npw: int = 300               # target coefficients per band
+    nlf: int = 19                # local fields (lf='z', odd)
+    no: int = 201                # frequencies
+    omax_ev: float = 30.0
+    eta_ev: float = 0.05
+    T_ev: float = 0.025852       # 300 K
+    a_ang: float = 2.46
+    c_ang: float = 20.0
+    t_ev: float = 2.7
+    band_gap_step_ev: float = 1.0
+    q_frac: float = 0.01         # |q| in 2pi/a0 units along Gamma-M (b1 direction)
+    q_steps: int | None = None   # commensurate q = q_steps * b1/nk (overrides q_frac)
+    igk: bool = True             # per-k gk_sort basis (False: legacy G-list order)
+    ngd: int | None = None       # legacy NGd (defaults to min npw)
+    seed: int = 1234
+    lor_cut: float = 1.0e-3
+    df_cut: float = 1.0e-4
+    eps: float = 1.0e-4
+    threads: int = 0
+
+
+@dataclass
+class System:
+    cfg: SynthConfig
+    a0: float
+    c0: float
+    Vcell: float
+    Gcar: float
+    KC: np.ndarray            # (3,3): KC[:, j] = b_j (2pi/a0 units)
+    miller: np.ndarray        # (NG,3) int32
+    G: np.ndarray             # (NG,3) float64 == Fortran G(3,NG)
+    nks: int
+    nbnd: int
+    nocc: int
+    npwx: int
+    npw: np.ndarray           # (nks,) int32
+    igk: np.ndarray | None    # (nks,npwx) int32, 1-based == Fortran igk_k(npwx,nks)
+    ngd: int
+    coeff: np.ndarray         # (nks,nbnd,npwx) complex128 == Fortran C(npwx,nbnd,nks)
+    E: np.ndarray             # (nbnd,nks) float64 Hartree == Fortran E(nks,nbnd)
+    R: np.ndarray             # (48,3,3) [isym,i,j]
+    RI: np.ndarray
+    ntot: int
+    ktot: np.ndarray          # (ntot,3) == Fortran ktot(3,ntot)
+    K1: np.ndarray
+    R1: np.ndarray
+    K2: np.ndarray
+    R2: np.ndarray
+    iG0: np.ndarray
+    nlf: int
+    ilf: np.ndarray           # (nlf,) 1-based G indices of the local fields
+    Glf: np.ndarray           # (nlf,3)
+    parG: np.ndarray          # (nlf,) +-1, parity of the z Miller index
+    q: np.ndarray             # (3,) 2pi/a0 units
+    no: int
+    domega: float             # Hartree
+    eta: float                # Hartree
+    T: float                  # Hartree
+    Efermi: float             # Hartree
+    extra: dict = field(default_factory=dict)
+
+    # Fortran-order views for C callers ---------------------------------
+    def R_f(self) -> np.ndarray:
+        return np.asfortranarray(self.R)
+
+    def RI_f(self) -> np.ndarray:
+        return np.asfortranarray(self.RI)
+
+
+# ---------------------------------------------------------------------------
+def hex_cell(a_ang: float, c_ang: float):
+    """Bohr lattice constants, cell volume and reciprocal axes (2pi/a0 units)."""
+    a0 = a_ang / BOHR_ANG
+    c0 = c_ang / BOHR_ANG
+    s3 = math.sqrt(3.0)
+    # direct axes in units of a0: a1=(1,0,0), a2=(-1/2,sqrt3/2,0), a3=(0,0,c/a)
+    b1 = [1.0, 1.0 / s3, 0.0]
+    b2 = [0.0, 2.0 / s3, 0.0]
+    b3 = [0.0, 0.0, a0 / c0]
+    KC = np.array([b1, b2, b3]).T.copy()
+    Vcell = a0 * a0 * (s3 / 2.0) * c0
+    return a0, c0, Vcell, KC
+
+
+def g_list(KC: np.ndarray, gcut2: float):
+    """All Miller triples with |G|^2 <= gcut2 ((2pi/a0)^2), sorted by |G|^2.
+
+    Ties are ordered by the Miller triple so the order is deterministic.
+    """
+    b = KC.T  # rows b1,b2,b3
+    # bound each Miller index by |G|/|b_i projected| (generous box)
+    binv = np.linalg.inv(KC)
+    hmax = [int(math.ceil(math.sqrt(gcut2) * np.linalg.norm(binv[i, :]))) + 1 for i in range(3)]
+    h = np.arange(-hmax[0], hmax[0] + 1)
+    k = np.arange(-hmax[1], hmax[1] + 1)
+    l = np.arange(-hmax[2], hmax[2] + 1)
+    H, K, L = np.meshgrid(h, k, l, indexing="ij")
+    mil = np.stack([H.ravel(), K.ravel(), L.ravel()], axis=1)
+    G = mil @ b
+    g2 = np.einsum("ij,ij->i", G, G)
+    keep = g2 <= gcut2
+    mil, G, g2 = mil[keep], G[keep], g2[keep]
+    order = np.lexsort((mil[:, 2], mil[:, 1], mil[:, 0], np.round(g2, 10)))
+    mil = mil[order].astype(np.int32)
+    return mil, (mil.astype(np.float64) @ b)
+
+
+def gk_sort(k: np.ndarray, G: np.ndarray, ecut: float, npwx: int | None = None):
+    """QE gk_sort (Modules/qe_gksort.f90:44-94): igk (1-based) of |k+G|^2 <= ecut.
+
+    Sorted by |k+G|^2 with values closer than 1e-8 treated as equal and then
+    ordered by G index, which is what hpsort_eps yields whenever no chain of
+    near-equal values spans more than 1e-8 (checked here).
+    """
+    eps8 = 1.0e-8
+    kg = G + k[None, :]
+    q = np.einsum("ij,ij->i", kg, kg)
+    q[q <= eps8] = 0.0
+    g2 = np.einsum("ij,ij->i", G, G)
+    q2x = (math.sqrt(float(k @ k)) + math.sqrt(ecut)) ** 2
+    inside = np.nonzero(q <= ecut)[0]
+    beyond = np.nonzero((q > ecut) & (g2 > q2x + eps8))[0]
+    if beyond.size == 0:
+        raise ValueError("G list too short for gk_sort (no early exit)")
+    stop = beyond[0]
+    idx = inside[inside < stop]
+    if npwx is not None and idx.size > npwx:
+        raise ValueError("npwx too small")
+    qq = q[idx]
+    o = np.argsort(qq, kind="stable")
+    qs, ids = qq[o], idx[o]
+    # regroup runs of eps-equal values and order them by G index
+    out = np.empty_like(ids)
+    i = 0
+    n = qs.size
+    while i < n:
+        j = i + 1
+        while j < n and abs(qs[j] - qs[j - 1]) < eps8:
+            j += 1
+        if j - i > 1:
+            if qs[j - 1] - qs[i] >= eps8:
+                raise ValueError("ambiguous eps chain in gk_sort")
+            out[i:j] = np.sort(ids[i:j])
+        else:
+            out[i] = ids[i]
+        i = j
+    return (out + 1).astype(np.int32)
+
+
+def tb_energies(kcart: np.ndarray, nbnd: int, nocc: int, t_ev: float, step_ev: float,
+                rng: np.random.Generator) -> np.ndarray:
+    """Nearest-neighbour graphene-like |f(k)| stacked into nbnd bands (eV)."""
+    a1 = np.array([1.0, 0.0, 0.0])
+    a2 = np.array([-0.5, math.sqrt(3.0) / 2.0, 0.0])
+    ph1 = 2.0 * math.pi * (kcart @ a1)
+    ph2 = 2.0 * math.pi * (kcart @ a2)
+    f = np.abs(1.0 + np.exp(1j * ph1) + np.exp(1j * ph2))
+    E = np.empty((kcart.shape[0], nbnd))
+    for n in range(nbnd):
+        if n < nocc:
+            E[:, n] = -t_ev * f - (nocc - 1 - n) * step_ev
+        else:
+            E[:, n] = t_ev * f + (n - nocc) * step_ev
+    E += rng.normal(0.0, 0.1, size=E.shape)
+    return E
+
+
+def _coeff_block(seed_seq: np.random.SeedSequence, nb: int, npw_list, npwx: int):
+    rng = np.random.default_rng(seed_seq)
+    out = np.zeros((len(npw_list), nb, npwx), dtype=np.complex128)
+    for i, npw in enumerate(npw_list):
+        z = rng.standard_normal((npw, nb)) + 1j * rng.standard_normal((npw, nb))
+        qm, _ = np.linalg.qr(z)
+        out[i, :, :npw] = qm.T
+    return out
+
+
+def make_coefficients(npw: np.ndarray, nbnd: int, npwx: int, seed: int, tag: int, threads: int = 0):
+    """Orthonormal N(0,1) coefficient blocks, seeded per chunk of k-points."""
+    nks = npw.size
+    chunk = 64
+    starts = list(range(0, nks, chunk))
+    ss = np.random.SeedSequence([seed, tag]).spawn(len(starts))
+    out = np.zeros((nks, nbnd, npwx), dtype=np.complex128)
+    nth = threads or min(16, os.cpu_count() or 1)
+    with _cf.ThreadPoolExecutor(max_workers=nth) as ex:
+        futs = {ex.submit(_coeff_block, ss[i], nbnd, npw[s:s + chunk], npwx): s for i, s in enumerate(starts)}
+        for fu in _cf.as_completed(futs):
+            s = futs[fu]
+            blk = fu.result()
+            out[s:s + blk.shape[0]] = blk
+    return out
+
+
+def _count_sphere(G: np.ndarray, radius2: float) -> int:
+    return int(np.count_nonzero(np.einsum("ij,ij->i", G, G) <= radius2))
+
+
+def build(cfg: SynthConfig) -> System:
+    a0, c0, Vcell, KC = hex_cell(cfg.a_ang, cfg.c_ang)
+    Gcar = 2.0 * math.pi / a0
+    b = KC.T
+    # wavefunction cutoff giving ~npw plane waves; density sphere of radius 2x
+    vol_rec = abs(np.linalg.det(KC))
+    r = (3.0 * cfg.npw * vol_rec / (4.0 * math.pi)) ** (1.0 / 3.0)
+    kmax = 0.75 * np.linalg.norm(b[0])
+    _, Gtrial = g_list(KC, (2.0 * r + 2.0 * kmax) ** 2)
+    # refine r so the Gamma sphere holds ~npw vectors
+    g2s = np.sort(np.einsum("ij,ij->i", Gtrial, Gtrial))
+    target = min(cfg.npw, g2s.size) - 1
+    ecutw = float(0.5 * (g2s[target] + g2s[min(target + 1, g2s.size - 1)]))
+    gcut_rho = (math.sqrt(ecutw) * 2.0 + 2.0 * kmax) ** 2
+    miller, G = g_list(KC, gcut_rho)
+    NG = G.shape[0]
+
+    # Monkhorst-Pack grid, Gamma centred: k = i/nk b1 + j/nk b2
+    nk = cfg.nk
+    ii, jj = np.meshgrid(np.arange(nk), np.arange(nk), indexing="ij")
+    ii, jj = ii.ravel(), jj.ravel()
+    kgrid = (ii[:, None] * b[0] + jj[:, None] * b[1]) / nk
+    nks_grid = nk * nk
+
+    rng = np.random.default_rng(np.random.SeedSequence([cfg.seed, 7]))
+    E_grid = tb_energies(kgrid, cfg.nbnd, cfg.nocc, cfg.t_ev, cfg.band_gap_step_ev, rng)
+
+    # q and the K+Q bookkeeping
+    ntot = nks_grid
+    ktot = kgrid.copy()
+    K1 = np.arange(1, ntot + 1, dtype=np.int32)
+    R1 = np.ones(ntot, dtype=np.int32)
+    R2 = np.ones(ntot, dtype=np.int32)
+    mil_index = {tuple(m): i + 1 for i, m in enumerate(miller.tolist())}
+    if cfg.q_steps is not None:
+        s = int(cfg.q_steps)
+        q = s * b[0] / nk
+        i2 = (ii + s) % nk
+        g0 = (ii + s) // nk
+        K2 = (i2 * nk + jj + 1).astype(np.int32)
+        iG0 = np.array([mil_index[(int(g), 0, 0)] for g in g0], dtype=np.int32)
+        kpts = kgrid
+        E_all = E_grid
+        nks = nks_grid
+    else:
+        q = cfg.q_frac * b[0] / np.linalg.norm(b[0])
+        kq = kgrid + q[None, :]
+        rng2 = np.random.default_rng(np.random.SeedSequence([cfg.seed, 8]))
+        E_kq = tb_energies(kq, cfg.nbnd, cfg.nocc, cfg.t_ev, cfg.band_gap_step_ev, rng2)
+        kpts = np.concatenate([kgrid, kq], axis=0)
+        E_all = np.concatenate([E_grid, E_kq], axis=0)
+        nks = 2 * nks_grid
+        K2 = (np.arange(ntot) + nks_grid + 1).astype(np.int32)
+        iG0 = np.ones(ntot, dtype=np.int32)
+
+    # per-k basis
+    if cfg.igk:
+        igks = [gk_sort(kpts[i], G, ecutw) for i in range(nks)]
+        npw = np.array([x.size for x in igks], dtype=np.int32)
+        npwx = int(npw.max())
+        igk = np.zeros((nks, npwx), dtype=np.int32)
+        for i, x in enumerate(igks):
+            igk[i, :x.size] = x
+        ngd = int(npw.min())
+    else:
+        nleg = _count_sphere(G, ecutw)
+        npw = np.full(nks, nleg, dtype=np.int32)
+        npwx = nleg
+        igk = None
+        ngd = int(cfg.ngd or nleg)
+    coeff = make_coefficients(npw, cfg.nbnd, npwx, cfg.seed, 11, cfg.threads)
+
+    # local fields, lf='z' (genGlfandParity, Sloss.f90:824-881): G_par = 0, by G order
+    zsel = np.nonzero((miller[:, 0] == 0) & (miller[:, 1] == 0))[0]
+    if zsel.size < cfg.nlf:
+        raise ValueError("not enough G_z vectors for nlf")
+    ilf = (zsel[:cfg.nlf] + 1).astype(np.int32)
+    Glf = G[ilf - 1].copy()
+    Glf[:, 0:2] = 0.0
+    parG = np.where(miller[ilf - 1, 2] % 2 == 0, 1, -1).astype(np.int32)
+
+    R = np.zeros((48, 3, 3))
+    R[0] = np.eye(3)
+    RI = R.copy()
+
+    omax = cfg.omax_ev / HARTREE_EV
+    domega = omax / (cfg.no - 1)
+    sysd = System(cfg=cfg, a0=a0, c0=c0, Vcell=Vcell, Gcar=Gcar, KC=KC, miller=miller, G=G,
+                  nks=nks, nbnd=cfg.nbnd, nocc=cfg.nocc, npwx=npwx, npw=npw, igk=igk, ngd=ngd,
+                  coeff=coeff, E=np.ascontiguousarray((E_all / HARTREE_EV).T), R=R, RI=RI,
+                  ntot=ntot, ktot=ktot, K1=K1, R1=R1, K2=K2, R2=R2, iG0=iG0, nlf=cfg.nlf,
+                  ilf=ilf, Glf=Glf, parG=parG, q=q, no=cfg.no, domega=domega,
+                  eta=cfg.eta_ev / HARTREE_EV, T=cfg.T_ev / HARTREE_EV, Efermi=0.0)
+    sysd.extra["ecutw"] = ecutw
+    sysd.extra["kpts"] = kpts
+    return sysd
+
+
+# Named workloads -------------------------------------------------------------
+def config_small(**kw) -> SynthConfig:
+    """A few-second oracle case with the C1 shapes scaled down."""
+    base = dict(nk=6, nbnd=8, nocc=4, npw=60, nlf=7, no=41, omax_ev=30.0, eta_ev=0.3, q_steps=1)
+    base.update(kw)
+    return SynthConfig(**base)
+
+
+def config_c1(**kw) -> SynthConfig:
+    """24x24 grid, 8 bands (4 occupied), 300 coefficients, NGloc=19, nw=201,
+    q = 0.01 2pi/a along Gamma-M, eta = 50 meV."""
+    base = dict(nk=24, nbnd=8, nocc=4, npw=300, nlf=19, no=201, omax_ev=30.0, eta_ev=0.05, q_frac=0.01)
+    base.update(kw)
+    return SynthConfig(**base)
+
+
+def config_c2(**kw) -> SynthConfig:
+    """120x120 grid, 30 bands (8 occupied), 1500 coefficients, NGloc=91,
+    nw=1001 on 0-30 eV, eta = 25 meV, q one grid step along Gamma-M."""
+    base = dict(nk=120, nbnd=30, nocc=8, npw=1500, nlf=91, no=1001, omax_ev=30.0, eta_ev=0.025, q_steps=1)
+    base.update(kw)
+    return SynthConfig(**base)

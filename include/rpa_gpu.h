@@ -1,0 +1,182 @@
+/* rpa_gpu.h -- C ABI of the GB300 RPA response library.
+ *
+ * Drop-in for the OpenMP k-loop, the Kramers-Kronig stage and the Dyson
+ * stage of the 2DMaterialsOpticalProps drivers:
+ *   Chi_RPA/Optabs.f90:291-471  (current vertices, complex S0 and Qeff)
+ *   Chi_RPA/Optabs.f90:575-614  (KK of complex S0 -> chi0 / Pi)
+ *   W/Sloss.f90:309-438         (charge vertices, real S0)
+ *   W/Sloss.f90:452-481         (KK, V, eps = 1 - chi0 V, gjel, chi, W)
+ * The drivers keep their namelists, the setup (PointR, genFBZ, findKinIBZ,
+ * findKQinBZ, genGlf) and every file they write; they hand the arrays they
+ * already hold to these calls through an ISO_C_BINDING interface.
+ *
+ * Conventions
+ *  - Every array is Fortran column-major, exactly as the drivers declare it;
+ *    every index handed in (K1, R1, K2, R2, iG0, igk, ilf) is 1-based.
+ *  - Complex arrays are interleaved (re, im) doubles (Fortran complex(dp)).
+ *  - Host buffers are owned by the caller and only touched during the call.
+ *    Device state (coefficients, energies, index maps, S0, chi0, W) is owned
+ *    by the context and released by rpa_destroy.
+ *  - Every call returns RPA_OK (0) or a negative error code and never exits
+ *    the process; rpa_last_error() gives the message.  One context per host
+ *    thread; calls on a context are serialised by the caller.
+ */
+#ifndef RPA_GPU_H
+#define RPA_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RPA_OK 0
+#define RPA_EINVAL (-1)     /* bad argument or size (e.g. NGd > igwx, Nlf > capacity) */
+#define RPA_ENOMEM (-2)     /* device allocation failed */
+#define RPA_ESINGULAR (-3)  /* gjel met a repeated pivot ("singular matrix in gjel" + stop) */
+#define RPA_ETIMEOUT (-4)   /* a bounded device wait gave up */
+#define RPA_ECUDA (-5)      /* CUDA runtime error */
+#define RPA_ESTATE (-6)     /* call made before the state it needs was set */
+#define RPA_ENOTFOUND (-7)  /* an index map could not be resolved */
+
+enum { RPA_PREC_FP64 = 0, RPA_PREC_MIXED = 1 };
+enum { RPA_MODE_CHARGE = 0, RPA_MODE_CURRENT = 1 };
+enum { RPA_POL_XX = 0, RPA_POL_YY = 1, RPA_POL_ZZ = 2, RPA_POL_YZ = 3, RPA_POL_ZY = 4 };
+enum { RPA_KK_OPTABS_COMPLEX = 1, RPA_KK_SLOSS_REAL = 2 };
+
+typedef struct rpa_ctx rpa_ctx;
+
+typedef struct rpa_opts {
+  int device;     /* CUDA device ordinal */
+  int precision;  /* RPA_PREC_FP64 (plain drop-in) or RPA_PREC_MIXED */
+  int verbose;    /* 0: silent */
+  int reserved[5];
+} rpa_opts;
+
+/* Arguments of one chi0 accumulation (the namelist values the drivers use).
+ * Energies are in Hartree, as the drivers hold them after their eV->Ha
+ * conversion (Optabs.f90:173-181, Sloss.f90:195-199). */
+typedef struct rpa_chi0_args {
+  int mode;       /* RPA_MODE_CHARGE: Sloss (n <= nocc < m, real S0, io = 1..no)
+                     RPA_MODE_CURRENT: Optabs (df cut, complex S0, io = -no..no, Qeff) */
+  int pol;        /* RPA_POL_* (current vertices, genStrujniVrhovi) */
+  int ngd;        /* NGd: coefficients summed per band when the basis has no igk
+                     map (legacy drivers); ignored with an igk map (npw(K1) is used) */
+  int nocc;       /* Sloss Nocc */
+  int no;         /* number of frequencies */
+  int ntot_norm;  /* Ntot in the 1/(pi Ntot Vcell) normalisation; 0 -> ntot of rpa_kmap */
+  double domega;  /* Hartree */
+  double eta;     /* Sloss eta / Optabs eta_inter, Hartree */
+  double lor_cut; /* Optabs Lor_cut (Sloss hard-codes 1e-3) */
+  double df_cut;  /* Optabs df_cut */
+  double T;       /* Optabs temperature, Hartree */
+  double Efermi;  /* Optabs Fermi energy, Hartree */
+  double Vcell;   /* bohr^3 */
+  double Gcar;    /* 2 pi / a0 */
+} rpa_chi0_args;
+
+/* Replaces: the process-wide setup of a driver run.  Creates a context on
+ * opts->device with its own stream. */
+int rpa_create(rpa_ctx** out, const rpa_opts* opts);
+
+/* Releases every device buffer of the context. */
+int rpa_destroy(rpa_ctx* ctx);
+
+/* Message of the last failing call on ctx (or of rpa_create when ctx is NULL). */
+const char* rpa_last_error(const rpa_ctx* ctx);
+
+/* Replaces: loadKC + loadG (Optabs.f90:652-680, 1061-1110; Sloss.f90:1309-1348).
+ *   miller : Gi(3,NG), the crystal (Miller) coordinates read from gvectors.xml
+ *   G      : G(3,NG), Cartesian in 2pi/a0 units, as loadG computes it
+ *   KC     : KC(3,3), reciprocal axes (columns b1, b2, b3) in 2pi/a0 units
+ * G(:,1) must be 0 (loadG stops otherwise). */
+int rpa_set_gvectors(rpa_ctx* ctx, int ng, const int* miller, const double* G, const double* KC);
+
+/* Replaces: PointR (Chi_RPA/PointR.f90:11-144) output R(48,3,3), RI(48,3,3)
+ * in Cartesian coordinates.  Each operation must map the G lattice onto
+ * itself (integer matrix in crystal coordinates). */
+int rpa_set_symmetry(rpa_ctx* ctx, int nsym, const double* R, const double* RI);
+
+/* Replaces: the per-band coefficient reads inside the k-loop
+ * (iotk_scan_dat, Optabs.f90:332-374, Sloss.f90:355-393) and loadkIandE.
+ *   npw   : npw(nks) = igwx of each IBZ k-point
+ *   igk   : igk_k(npwx,nks) (1-based into G, init_igk of Modules/qe_gksort.f90),
+ *           or NULL for the legacy drivers, where coefficient i belongs to G(:,i)
+ *   coeff : C(npwx,nbnd,nks) complex(dp)
+ *   E     : E(nks,nbnd) Hartree (any scissor already applied)
+ * The basis stays resident on the device until the next call or rpa_destroy. */
+int rpa_load_basis(rpa_ctx* ctx, int nks, int nbnd, int npwx, const int* npw, const int* igk,
+                   const double* coeff, const double* E);
+
+/* Replaces: findKinIBZ / findKQinBZ results of the k-loop
+ * (Optabs.f90:306,320; Sloss.f90:327,339): for every FBZ point ik,
+ * ktot(3,ik) = R1*K1 and ktot + q = G(iG0) + R2*K2. */
+int rpa_kmap(rpa_ctx* ctx, int ntot, const double* ktot, const int* K1, const int* R1,
+             const int* K2, const int* R2, const int* iG0);
+
+/* Replaces: findMinQ + genGlf/genGlfandParity results (Optabs.f90:272,248;
+ * Sloss.f90:295,258).
+ *   q    : q(3), 2pi/a0 units (before the Gcar conversion)
+ *   ilf  : ilf(nlf), 1-based G index of each local field (Glf(:,i) = G(:,ilf(i)))
+ *   parG : parG(nlf) = +-1 parity used by genV (may be NULL for Optabs) */
+int rpa_set_q(rpa_ctx* ctx, const double* q, int nlf, const int* ilf, const int* parG);
+
+/* Replaces: the OpenMP k-loop with its vertices and the S0 accumulation,
+ * Optabs.f90:291-471 (mode CURRENT) or Sloss.f90:309-438 (mode CHARGE).
+ * S0_out: CURRENT -> complex S0(-no:no,nlf,nlf); CHARGE -> real S0(no,nlf,nlf).
+ * Qeff_out: complex Qeff(nlf,nlf) (CURRENT only).  Either may be NULL, in which
+ * case the result only stays on the device for rpa_kk. */
+int rpa_chi0(rpa_ctx* ctx, const rpa_chi0_args* args, double* S0_out, double* Qeff_out);
+
+/* Replaces: genReChi0/genImChi0 (Optabs.f90:1112-1318, variant
+ * RPA_KK_OPTABS_COMPLEX) or genChi0 (Sloss.f90:954-1059, RPA_KK_SLOSS_REAL)
+ * for io = 1..no-1 over the S0 left on the device by rpa_chi0.
+ * chi0_out: complex chi0(no-1,nlf,nlf) (may be NULL). */
+int rpa_kk(rpa_ctx* ctx, int variant, double* chi0_out);
+
+/* Replaces: the Dyson loop of Sloss.f90:452-481 for io = 1..no-1:
+ * genV, eps = I - chi0 V, gjel (W/gjel.f), chi = eps^-1 chi0, WT = V + V chi V.
+ *   c0, eps    : the &parameters c0 (bohr) and eps of the driver
+ *   WT_out     : complex WT(no-1,nlf,nlf) (may be NULL)
+ *   epsinv_out : complex eps^-1(no-1,nlf,nlf) (may be NULL)
+ *   head_out   : complex eps^-1_{11}(no-1), the loss function is -Im (may be NULL)
+ * Returns RPA_ESINGULAR where gjel would stop. */
+int rpa_dyson(rpa_ctx* ctx, double c0, double eps, double* WT_out, double* epsinv_out,
+              double* head_out);
+
+/* Replaces: init_igk (Modules/qe_gksort.f90:11-42): igk_k(npwx,nks) and ngk(nks)
+ * of the k+G spheres |k+G|^2 <= gcutw, sorted as hpsort_eps does.
+ * Host-side; needs no device.  Returns RPA_EINVAL when npwx is too small or
+ * the G list ends inside a sphere. */
+int rpa_init_igk(int nks, const double* xk, int npwx, int ngm, const double* g, double gcutw,
+                 int* igk_k, int* ngk);
+
+/* Diagnostic for the index-map parity checks: the Gfast map of FBZ point ik
+ * (1-based) in the reference's convention (Sloss.f90:905-944): for local
+ * field iG and coefficient iG1 of K1, the 1-based K2 basis position of
+ * G'' = RI_R2 (R_R1 G1 + Glf + G_iG0), or NG2+1 when K2 has no such
+ * coefficient.  out is Gfast((iG-1)*nsum + iG1), nsum = NGd (no igk map) or
+ * npw(K1). */
+int rpa_gfast(rpa_ctx* ctx, int ik, int ngd, int* out);
+
+/* Host-side diagnostic: the KK kernel matrix K((no-1), nw) that rpa_kk applies
+ * (row-major, rows io = 1..no-1; columns are the S0 rows: jo = 1..no for
+ * RPA_KK_SLOSS_REAL, j = -no..no for RPA_KK_OPTABS_COMPLEX).  Needs no device. */
+int rpa_kk_matrix(int variant, int no, double domega, double* K);
+
+/* Timing of the stages of the last rpa_chi0/rpa_kk/rpa_dyson calls (ms, CUDA
+ * events on the context stream): [0] pairs+sort, [1] vertices,
+ * [2] accumulation, [3] KK, [4] Dyson, [5] host<->device copies. */
+int rpa_stage_times(const rpa_ctx* ctx, double* ms6);
+
+/* Statistics of the last rpa_chi0: [0] transitions with a non-empty window,
+ * [1] sum over transitions of window lengths (N_win), [2] vertex complex MACs,
+ * [3] accumulation launches. */
+int rpa_chi0_stats(const rpa_ctx* ctx, double* out4);
+
+/* Blocks until the context stream is idle. */
+int rpa_synchronize(rpa_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RPA_GPU_H */

@@ -152,6 +152,7 @@ int accumulate_fp64(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax) {
   else
     k_accum_fp64<BO, TT, false><<<grid, 128, 0, c->stream>>>(A, c->d_S.as<double>());
   RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
   return RPA_OK;
 }
 
@@ -184,6 +185,7 @@ int qeff_fp64(rpa_ctx* c, const Chi0Plan& P, int n_inter, int n_trans) {
                                                   two ? c->d_M2.as<double2>() : c->d_M.as<double2>(), c->nlf,
                                                   c->d_Q.as<double2>());
   RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
   return RPA_OK;
 }
 

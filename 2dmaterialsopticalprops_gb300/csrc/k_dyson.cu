@@ -239,6 +239,7 @@ int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singul
   RPA_CUDA(c, cudaFuncSetAttribute(k_dyson_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_dyson_fp64<<<grid, 256, smem, c->stream>>>(D);
   RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
   int fl[4];
   RPA_CUDA(c, cudaMemcpyAsync(fl, c->d_flags.p, sizeof(int) * 4, cudaMemcpyDeviceToHost, c->stream));
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -178,6 +178,7 @@ int kk_run(rpa_ctx* c, int variant, int no, double domega) {
     k_kk_fp64<false><<<grid, 256, 0, c->stream>>>(c->d_kk.as<double>(), c->d_S.as<double>(),
                                                   c->d_chi0.as<double2>(), nrow, nw, np, pi_row0);
   RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
   return RPA_OK;
 }
 

@@ -205,6 +205,7 @@ int count_pairs(rpa_ctx* c, const Chi0Plan& Pl, int k0, int nk, std::vector<int>
   k_pairs_count<<<nk, 256, 0, c->stream>>>(P, k0, npairs_of(c, Pl), c->d_counts.as<int>(),
                                            c->d_wmax.as<int>() + 1);
   RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
   counts.resize(nk);
   RPA_CUDA(c, cudaMemcpyAsync(counts.data(), c->d_counts.p, sizeof(int) * nk, cudaMemcpyDeviceToHost,
                               c->stream));
@@ -230,6 +231,7 @@ int emit_pairs(rpa_ctx* c, const Chi0Plan& Pl, int k0, int nk, const std::vector
                                           Pl.nw, c->d_wmax.as<int>(),
                                           reinterpret_cast<unsigned long long*>(c->d_wmax.as<int>() + 4));
   RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
   int w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   RPA_CUDA(c, cudaMemcpyAsync(w, c->d_wmax.p, 32, cudaMemcpyDeviceToHost, c->stream));
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -261,6 +263,7 @@ int sort_trans(rpa_ctx* c, int n_trans, int nw) {
   k_gather_sorted<<<(n_trans + 255) / 256, 256, 0, c->stream>>>(c->d_trans.as<Trans>(), c->d_vals_alt.as<int>(),
                                                                 c->d_sorted.as<Trans>(), n_trans);
   RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
   return RPA_OK;
 }
 

@@ -283,6 +283,7 @@ int vertices_fp64(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, l
     kern<<<grid, 256, smem, c->stream>>>(C, coeff, tr, off, k0, GC, c->nbnd, ca, cb, M, M2);
   }
   RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
   return RPA_OK;
 }
 
@@ -307,6 +308,7 @@ int build_gfast(rpa_ctx* c, int ik, int nsum_legacy, int* host_out) {
   RPA_TRY(ensure(c, c->d_tmp, sizeof(int) * (n + 1)));
   k_gfast<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(C, ik, nsum, c->d_tmp.as<int>());
   RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
   RPA_CUDA(c, cudaMemcpyAsync(host_out, c->d_tmp.p, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
   return RPA_OK;

@@ -21,10 +21,16 @@ int emit_pairs(rpa_ctx* c, const Chi0Plan& Pl, int k0, int nk, const std::vector
 int sort_trans(rpa_ctx* c, int n_trans, int nw);
 int vertices_fp64(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, long long n_trans);
 int accumulate_fp64(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax);
+int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const float2* Mf, const float2* Mf2,
+                  float amaxM, float amaxM2, double cmax);
+int pack_sorted_fp32(rpa_ctx* c, int n_inter, float2* Mf, float2* Mf2, bool two, float* amaxM, float* amaxM2,
+                     double* cmax);
+int df_to_f64(rpa_ctx* c, size_t n);
 int qeff_fp64(rpa_ctx* c, const Chi0Plan& P, int n_inter, int n_trans);
 int kk_run(rpa_ctx* c, int variant, int no, double domega);
 int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singular, int* n_zero);
 void kk_matrix(int variant, int no, double domega, std::vector<double>& K, int* nw_out);
+int selftest_umma(int which, double* result);
 int gk_sort_host(const double* k, int npwx, int ngm, const double* g, double ecut, int* ngk, int* igk, double* gk);
 
 static thread_local std::string g_create_err;
@@ -225,6 +231,7 @@ int rpa_create(rpa_ctx** out, const rpa_opts* opts) {
   c->device = dev;
   c->precision = opts ? opts->precision : RPA_PREC_FP64;
   c->verbose = opts ? opts->verbose : 0;
+  c->split_f16 = opts ? opts->split == 0 : true;
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete c;
@@ -243,8 +250,8 @@ int rpa_destroy(rpa_ctx* c) {
   DevBuf* bufs[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
                     &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_E, &c->d_kmap, &c->d_ktot, &c->d_lf_miller,
                     &c->d_Glf, &c->d_occ, &c->d_counts, &c->d_offsets, &c->d_trans, &c->d_keys, &c->d_keys_alt,
-                    &c->d_vals, &c->d_vals_alt, &c->d_sorted, &c->d_M, &c->d_M2, &c->d_cub, &c->d_wmax,
-                    &c->d_ntrans, &c->d_S, &c->d_Q, &c->d_chi0, &c->d_kk, &c->d_V, &c->d_eps, &c->d_WT,
+                    &c->d_vals, &c->d_vals_alt, &c->d_sorted, &c->d_M, &c->d_M2, &c->d_Mf, &c->d_Mf2, &c->d_cub, &c->d_wmax,
+                    &c->d_ntrans, &c->d_S, &c->d_Sdf, &c->d_Q, &c->d_chi0, &c->d_kk, &c->d_V, &c->d_eps, &c->d_WT,
                     &c->d_flags, &c->d_tmp};
   for (DevBuf* b : bufs) release(*b);
   for (auto& ev : c->ev)
@@ -344,6 +351,7 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
     k_build_inv<<<1024, 256, 0, c->stream>>>(c->d_gidx.as<int>(), c->d_npw.as<int>(), c->d_inv.as<int>(), nks, npwx,
                                              c->ng, c->d_flags.as<int>());
     RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
     int bad = 0;
     RPA_CUDA(c, cudaMemcpyAsync(&bad, c->d_flags.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     RPA_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -362,6 +370,7 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
     k_basis_transpose<<<2048, 256, 0, c->stream>>>(c->d_tmp.as<double2>(), c->d_coeff.as<double2>() + per_k * k0, nk,
                                                    nbnd, npwx);
     RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
   }
   cudaEventRecord(c->ev[7], c->stream);
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -442,8 +451,6 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
   if (a->mode == RPA_MODE_CHARGE && (a->nocc < 1 || a->nocc >= c->nbnd))
     return fail(c, RPA_EINVAL, "rpa_chi0: nocc must be in 1..nbnd-1");
   if (a->mode == RPA_MODE_CURRENT && !(a->T > 0)) return fail(c, RPA_EINVAL, "rpa_chi0: T must be > 0");
-  if (c->precision != RPA_PREC_FP64)
-    return fail(c, RPA_EINVAL, "rpa_chi0: this context precision has no accumulation path");
   cudaSetDevice(c->device);
 
   Chi0Plan P;
@@ -506,8 +513,14 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
   RPA_TRY(ensure(c, c->d_S, s_bytes));
   RPA_TRY(ensure(c, c->d_Q, sizeof(double2) * np));
   RPA_CUDA(c, cudaMemsetAsync(c->d_S.p, 0, s_bytes, c->stream));
+  if (c->precision == RPA_PREC_MIXED) {
+    RPA_TRY(ensure(c, c->d_Sdf, s_bytes));  // one (hi, lo) float pair per double of S0
+    RPA_CUDA(c, cudaMemsetAsync(c->d_Sdf.p, 0, s_bytes, c->stream));
+  }
   RPA_CUDA(c, cudaMemsetAsync(c->d_Q.p, 0, sizeof(double2) * np, c->stream));
 
+  RPA_TRY(ensure(c, c->d_flags, sizeof(int) * 4));
+  RPA_CUDA(c, cudaMemsetAsync(c->d_flags.p, 0, sizeof(int) * 4, c->stream));
   double t_pairs = 0, t_vert = 0, t_acc = 0;
   double st_trans = 0, st_win = 0, st_mac = 0, st_launch = 0;
   std::vector<int> counts;
@@ -537,7 +550,18 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
     cudaEventRecord(c->ev[2], c->stream);
     RPA_TRY(vertices_fp64(c, P, k0, nk, maxp, tot));
     cudaEventRecord(c->ev[3], c->stream);
-    RPA_TRY(accumulate_fp64(c, P, n_inter, wmax));
+    if (c->precision == RPA_PREC_MIXED) {
+      RPA_TRY(ensure(c, c->d_Mf, sizeof(float2) * ((size_t)n_inter + 1) * c->nlf));
+      if (two) RPA_TRY(ensure(c, c->d_Mf2, sizeof(float2) * ((size_t)n_inter + 1) * c->nlf));
+      float2* Mf = c->d_Mf.as<float2>();
+      float2* Mf2 = two ? c->d_Mf2.as<float2>() : Mf;
+      float amM = 0.f, amM2 = 0.f;
+      double cmax = 0.0;
+      RPA_TRY(pack_sorted_fp32(c, n_inter, Mf, Mf2, two, &amM, &amM2, &cmax));
+      RPA_TRY(accumulate_tc(c, P, n_inter, wmax, Mf, Mf2, amM, amM2, cmax));
+    } else {
+      RPA_TRY(accumulate_fp64(c, P, n_inter, wmax));
+    }
     if (cplx) RPA_TRY(qeff_fp64(c, P, n_inter, (int)tot));
     cudaEventRecord(c->ev[4], c->stream);
     RPA_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -553,8 +577,14 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
     }
     k0 = k1;
   }
+  if (c->precision == RPA_PREC_MIXED) RPA_TRY(df_to_f64(c, s_bytes / sizeof(double)));
   cudaEventRecord(c->ev[5], c->stream);
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+  {
+    int fl[4] = {0, 0, 0, 0};
+    RPA_CUDA(c, cudaMemcpy(fl, c->d_flags.p, sizeof(int) * 4, cudaMemcpyDeviceToHost));
+    if (fl[2]) return fail(c, RPA_ETIMEOUT, "rpa_chi0: a tensor-core completion wait timed out");
+  }
   c->stage_ms[0] = t_pairs;
   c->stage_ms[1] = t_vert;
   c->stage_ms[2] = t_acc;
@@ -577,6 +607,7 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
       RPA_TRY(ensure(c, c->d_tmp, s_bytes));
       launch_transpose_wp_to_fortran(c->d_S.as<double>(), c->d_tmp.as<double>(), P.nw, np, cplx ? 2 : 1, c->stream);
       RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
       RPA_CUDA(c, cudaMemcpyAsync(S0_out, c->d_tmp.p, s_bytes, cudaMemcpyDeviceToHost, c->stream));
     }
     if (Qeff_out && cplx)
@@ -609,6 +640,7 @@ int rpa_kk(rpa_ctx* c, int variant, double* chi0_out) {
     cudaEventRecord(c->ev[6], c->stream);
     launch_transpose_wp_to_fortran(c->d_chi0.as<double>(), c->d_tmp.as<double>(), nwo, np, 2, c->stream);
     RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
     RPA_CUDA(c, cudaMemcpyAsync(chi0_out, c->d_tmp.p, sizeof(double2) * (size_t)nwo * np, cudaMemcpyDeviceToHost,
                                 c->stream));
     cudaEventRecord(c->ev[7], c->stream);
@@ -650,6 +682,7 @@ int rpa_dyson(rpa_ctx* c, double c0, double eps, double* WT_out, double* epsinv_
     if (WT_out) {
       launch_transpose_wp_to_fortran(c->d_WT.as<double>(), c->d_tmp.as<double>(), nwo, np, 2, c->stream);
       RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
       RPA_CUDA(c, cudaMemcpyAsync(WT_out, c->d_tmp.p, sizeof(double2) * (size_t)nwo * np, cudaMemcpyDeviceToHost,
                                   c->stream));
       RPA_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -657,6 +690,7 @@ int rpa_dyson(rpa_ctx* c, double c0, double eps, double* WT_out, double* epsinv_
     if (epsinv_out) {
       launch_transpose_wp_to_fortran(c->d_eps.as<double>(), c->d_tmp.as<double>(), nwo, np, 2, c->stream);
       RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
       RPA_CUDA(c, cudaMemcpyAsync(epsinv_out, c->d_tmp.p, sizeof(double2) * (size_t)nwo * np,
                                   cudaMemcpyDeviceToHost, c->stream));
     }
@@ -707,6 +741,23 @@ int rpa_stage_times(const rpa_ctx* c, double* ms6) {
 int rpa_chi0_stats(const rpa_ctx* c, double* out4) {
   if (!c || !out4) return RPA_EINVAL;
   for (int i = 0; i < 4; ++i) out4[i] = c->stats[i];
+  return RPA_OK;
+}
+
+int rpa_selftest(int which, double* result) {
+  if (!result || which < 0 || which > 2) return RPA_EINVAL;
+  return selftest_umma(which, result);
+}
+
+int rpa_launch_count(const rpa_ctx* c, long long* count) {
+  if (!c || !count) return RPA_EINVAL;
+  *count = c->launches;
+  return RPA_OK;
+}
+
+int rpa_get_stream(const rpa_ctx* c, void** stream) {
+  if (!c || !stream) return RPA_EINVAL;
+  *stream = (void*)c->stream;
   return RPA_OK;
 }
 

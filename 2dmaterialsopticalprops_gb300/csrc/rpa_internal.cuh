@@ -41,6 +41,7 @@ struct rpa_ctx {
   int device = 0;
   int precision = RPA_PREC_FP64;
   int verbose = 0;
+  bool split_f16 = true;  // mixed path: fp16 (scaled) or bf16 hi/lo operands
   cudaStream_t stream = nullptr;
   std::string err;
 
@@ -80,13 +81,14 @@ struct rpa_ctx {
 
   // per-call scratch
   rpa::DevBuf d_occ, d_counts, d_offsets, d_trans, d_keys, d_keys_alt, d_vals, d_vals_alt, d_sorted,
-      d_M, d_M2, d_cub, d_wmax, d_ntrans;
+      d_M, d_M2, d_Mf, d_Mf2, d_cub, d_wmax, d_ntrans;
   // results
   int last_mode = -1, last_no = 0, last_nw = 0;
   double last_domega = 0.0, last_Gcar = 0.0;
   bool have_S = false, have_chi0 = false;
-  rpa::DevBuf d_S, d_Q, d_chi0, d_kk, d_V, d_eps, d_WT, d_flags, d_tmp;
+  rpa::DevBuf d_S, d_Sdf, d_Q, d_chi0, d_kk, d_V, d_eps, d_WT, d_flags, d_tmp;
   double stage_ms[6] = {0, 0, 0, 0, 0, 0};
+  long long launches = 0;  // kernels launched by this context
   double stats[4] = {0, 0, 0, 0};
   cudaEvent_t ev[8] = {};
 };

@@ -24,11 +24,12 @@ KK_OPTABS_COMPLEX, KK_SLOSS_REAL = 1, 2
 
 EXPORTS = ["rpa_create", "rpa_destroy", "rpa_last_error", "rpa_set_gvectors", "rpa_set_symmetry",
            "rpa_load_basis", "rpa_kmap", "rpa_set_q", "rpa_chi0", "rpa_kk", "rpa_dyson", "rpa_gfast",
-           "rpa_init_igk", "rpa_kk_matrix", "rpa_stage_times", "rpa_chi0_stats", "rpa_synchronize"]
+           "rpa_init_igk", "rpa_kk_matrix", "rpa_stage_times", "rpa_chi0_stats", "rpa_selftest", "rpa_launch_count", "rpa_get_stream", "rpa_synchronize"]
 
 
 class RpaOpts(C.Structure):
-    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("verbose", C.c_int), ("reserved", C.c_int * 5)]
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("verbose", C.c_int), ("split", C.c_int),
+                ("reserved", C.c_int * 4)]
 
 
 class RpaChi0Args(C.Structure):
@@ -73,6 +74,9 @@ def load_library(path: str = LIB_PATH):
     L.rpa_kk_matrix.argtypes = [ip, ip, dp, vp]
     L.rpa_stage_times.argtypes = [vp, vp]
     L.rpa_chi0_stats.argtypes = [vp, vp]
+    L.rpa_selftest.argtypes = [ip, C.POINTER(C.c_double)]
+    L.rpa_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
+    L.rpa_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.rpa_synchronize.argtypes = [vp]
     for name in EXPORTS:
         if name != "rpa_last_error":
@@ -112,13 +116,23 @@ def kk_matrix(variant: int, no: int, domega: float) -> np.ndarray:
     return K
 
 
+def selftest(which: int) -> float:
+    """Runs the on-device tcgen05 GEMM self-test; returns its max relative error."""
+    L = load_library()
+    r = C.c_double()
+    rc = L.rpa_selftest(which, C.byref(r))
+    if rc != RPA_OK:
+        raise RpaError(rc, "rpa_selftest failed")
+    return r.value
+
+
 class Context:
     """One rpa_ctx: resident basis + per-q state, Fortran-layout I/O."""
 
-    def __init__(self, device: int = 0, precision: int = PREC_FP64, verbose: int = 0):
+    def __init__(self, device: int = 0, precision: int = PREC_FP64, verbose: int = 0, split: int = 0):
         self.L = load_library()
         self.h = C.c_void_p()
-        opts = RpaOpts(device=device, precision=precision, verbose=verbose)
+        opts = RpaOpts(device=device, precision=precision, verbose=verbose, split=split)
         rc = self.L.rpa_create(C.byref(self.h), C.byref(opts))
         if rc != RPA_OK:
             raise RpaError(rc, self.L.rpa_last_error(None).decode())
@@ -233,6 +247,16 @@ class Context:
         out = np.zeros(4)
         self._chk(self.L.rpa_chi0_stats(self.h, _p(out)))
         return dict(zip(["transitions", "sum_nwin", "vertex_macs", "chunks"], out.tolist()))
+
+    def launch_count(self) -> int:
+        n = C.c_longlong()
+        self._chk(self.L.rpa_launch_count(self.h, C.byref(n)))
+        return int(n.value)
+
+    def stream_handle(self) -> int:
+        h = C.c_void_p()
+        self._chk(self.L.rpa_get_stream(self.h, C.byref(h)))
+        return h.value or 0
 
     def synchronize(self):
         self._chk(self.L.rpa_synchronize(self.h))

@@ -44,7 +44,8 @@ class SynthConfig:
     nbnd: int = 8
     nocc: int = 4
     npw: int = 300               # target coefficients per band
-    nlf: int = 19                # local fields (lf='z', odd)
+    nlf: int = 19                # local fields
+    lf: str = "z"                # 'z': G_par = 0 vectors (genGlf lf='z'); 'xyz': first nlf G vectors
     no: int = 201                # frequencies
     omax_ev: float = 30.0
     eta_ev: float = 0.05
@@ -174,21 +175,17 @@ def gk_sort(k: np.ndarray, G: np.ndarray, ecut: float, npwx: int | None = None):
     qq = q[idx]
     o = np.argsort(qq, kind="stable")
     qs, ids = qq[o], idx[o]
-    # regroup runs of eps-equal values and order them by G index
-    out = np.empty_like(ids)
-    i = 0
-    n = qs.size
-    while i < n:
-        j = i + 1
-        while j < n and abs(qs[j] - qs[j - 1]) < eps8:
-            j += 1
-        if j - i > 1:
-            if qs[j - 1] - qs[i] >= eps8:
-                raise ValueError("ambiguous eps chain in gk_sort")
-            out[i:j] = np.sort(ids[i:j])
-        else:
-            out[i] = ids[i]
-        i = j
+    if qs.size == 0:
+        return np.zeros(0, dtype=np.int32)
+    # runs of eps-equal values are ordered by G index
+    brk = np.empty(qs.size, dtype=bool)
+    brk[0] = True
+    brk[1:] = np.diff(qs) >= eps8
+    starts = np.nonzero(brk)[0]
+    if np.any(np.maximum.reduceat(qs, starts) - qs[starts] >= eps8):
+        raise ValueError("ambiguous eps chain in gk_sort")
+    grp = np.cumsum(brk)
+    out = ids[np.lexsort((ids, grp))]
     return (out + 1).astype(np.int32)
 
 
@@ -211,25 +208,40 @@ def tb_energies(kcart: np.ndarray, nbnd: int, nocc: int, t_ev: float, step_ev: f
 
 
 def _coeff_block(seed_seq: np.random.SeedSequence, nb: int, npw_list, npwx: int):
+    """N(0,1) complex blocks orthonormalised by Cholesky-QR (Q = Z L^-H, Z^H Z = L L^H)."""
     rng = np.random.default_rng(seed_seq)
-    out = np.zeros((len(npw_list), nb, npwx), dtype=np.complex128)
-    for i, npw in enumerate(npw_list):
-        z = rng.standard_normal((npw, nb)) + 1j * rng.standard_normal((npw, nb))
-        qm, _ = np.linalg.qr(z)
-        out[i, :, :npw] = qm.T
-    return out
+    npw_list = np.asarray(npw_list)
+    nc = npw_list.size
+    z = rng.standard_normal((nc, npwx, nb, 2)).view(np.complex128)[..., 0]
+    z[np.arange(npwx)[None, :] >= npw_list[:, None]] = 0.0
+    gram = np.conj(np.transpose(z, (0, 2, 1))) @ z
+    L = np.linalg.cholesky(gram)
+    # Q^H = L^-1 Z^H
+    qh = np.linalg.solve(L, np.conj(np.transpose(z, (0, 2, 1))))
+    return np.conj(qh)
 
 
-def make_coefficients(npw: np.ndarray, nbnd: int, npwx: int, seed: int, tag: int, threads: int = 0):
-    """Orthonormal N(0,1) coefficient blocks, seeded per chunk of k-points."""
+def make_coefficients(npw: np.ndarray, nbnd: int, npwx: int, seed: int, tag: int, threads: int = 0,
+                      only=None, out: np.ndarray | None = None):
+    """Orthonormal N(0,1) coefficient blocks, seeded per chunk of 64 k-points.
+
+    ``only``: IBZ indices (0-based) whose blocks are needed; the chunks holding
+    them are generated (with the same values as a full build) and the rest
+    stay zero.  ``out``: preallocated (nks, nbnd, npwx) complex array (e.g.
+    page-locked host memory)."""
     nks = npw.size
     chunk = 64
     starts = list(range(0, nks, chunk))
     ss = np.random.SeedSequence([seed, tag]).spawn(len(starts))
-    out = np.zeros((nks, nbnd, npwx), dtype=np.complex128)
+    if out is None:
+        out = np.zeros((nks, nbnd, npwx), dtype=np.complex128)
+    else:
+        out[...] = 0.0
+    want = None if only is None else set(int(k) // chunk for k in only)
     nth = threads or min(16, os.cpu_count() or 1)
     with _cf.ThreadPoolExecutor(max_workers=nth) as ex:
-        futs = {ex.submit(_coeff_block, ss[i], nbnd, npw[s:s + chunk], npwx): s for i, s in enumerate(starts)}
+        futs = {ex.submit(_coeff_block, ss[i], nbnd, npw[s:s + chunk], npwx): s for i, s in enumerate(starts)
+                if want is None or i in want}
         for fu in _cf.as_completed(futs):
             s = futs[fu]
             blk = fu.result()
@@ -241,7 +253,10 @@ def _count_sphere(G: np.ndarray, radius2: float) -> int:
     return int(np.count_nonzero(np.einsum("ij,ij->i", G, G) <= radius2))
 
 
-def build(cfg: SynthConfig) -> System:
+def build(cfg: SynthConfig, coeff_only=None, coeff_out: np.ndarray | None = None) -> System:
+    """Builds the seeded system.  ``coeff_only``: FBZ k indices (0-based) whose
+    K1/K2 coefficient blocks are needed (others left zero, for sampled CPU
+    runs); ``coeff_out``: preallocated coefficient array to fill."""
     a0, c0, Vcell, KC = hex_cell(cfg.a_ang, cfg.c_ang)
     Gcar = 2.0 * math.pi / a0
     b = KC.T
@@ -311,15 +326,24 @@ def build(cfg: SynthConfig) -> System:
         npwx = nleg
         igk = None
         ngd = int(cfg.ngd or nleg)
-    coeff = make_coefficients(npw, cfg.nbnd, npwx, cfg.seed, 11, cfg.threads)
+    only = None
+    if coeff_only is not None:
+        ko = np.asarray(coeff_only, dtype=np.int64)
+        only = np.unique(np.concatenate([K1[ko] - 1, K2[ko] - 1]))
+    if coeff_out is not None and coeff_out.shape != (nks, cfg.nbnd, npwx):
+        raise ValueError(f"coeff_out must have shape {(nks, cfg.nbnd, npwx)}")
+    coeff = make_coefficients(npw, cfg.nbnd, npwx, cfg.seed, 11, cfg.threads, only=only, out=coeff_out)
 
-    # local fields, lf='z' (genGlfandParity, Sloss.f90:824-881): G_par = 0, by G order
-    zsel = np.nonzero((miller[:, 0] == 0) & (miller[:, 1] == 0))[0]
+    # local fields (genGlfandParity, Sloss.f90:824-881), in G-list order:
+    # lf='z' keeps G_par = 0 vectors, lf='xyz' the first nlf vectors of the list
+    if cfg.lf == "z":
+        zsel = np.nonzero((miller[:, 0] == 0) & (miller[:, 1] == 0))[0]
+    else:
+        zsel = np.arange(miller.shape[0])
     if zsel.size < cfg.nlf:
-        raise ValueError("not enough G_z vectors for nlf")
+        raise ValueError("not enough G vectors for nlf")
     ilf = (zsel[:cfg.nlf] + 1).astype(np.int32)
     Glf = G[ilf - 1].copy()
-    Glf[:, 0:2] = 0.0
     parG = np.where(miller[ilf - 1, 2] % 2 == 0, 1, -1).astype(np.int32)
 
     R = np.zeros((48, 3, 3))

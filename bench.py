@@ -1,0 +1,369 @@
+#!/usr/bin/env python
+"""One q-point of the production-size RPA workload per step.
+
+Workload (default ``--config c2``): 120x120 k-grid (14400 FBZ points, Nsym=1),
+30 bands (8 occupied), ~1500 plane-wave coefficients per band (igk-ordered
+k+G spheres), NGloc = 91 local fields, nw = 1001 frequencies on 0-30 eV,
+eta = 25 meV, q one grid step along Gamma-M.  A step computes, for that q:
+the current-current correlation S0 and chi0 for pol xx and pol zz (Optabs:
+vertices, S0 over -no..no, Qeff, KK) and the loss chain (Sloss: vertices,
+S0, KK, eps = 1 - chi0 V, gjel, chi, W).  Metric: q-point spectra per second.
+
+value : inputs resident in HBM (basis loaded once), outputs left on the device.
+e2e   : the same step through the C ABI with host buffers: the basis is copied
+        from page-locked host memory every step and S0 (xx, zz), Qeff, chi0
+        (xx, zz, loss), W and eps^-1_00 are read back.
+--impl reference : the CPU restatement of the reference (oracle/, OpenMP on
+        all host cores) on a bounded k / frequency sample, extrapolated.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = "2dmaterialsopticalprops_gb300"
+
+
+def pkg(name):
+    return importlib.import_module(f"{PKG}.{name}")
+
+
+def config_of(name: str, q_steps: int):
+    synth = pkg("synth")
+    if name == "c2":
+        return synth.config_c2(q_steps=q_steps)
+    if name == "c1":
+        return synth.config_c1()
+    if name == "small":
+        return synth.config_small(q_steps=q_steps)
+    raise SystemExit(f"unknown config {name}")
+
+
+def workload_desc(s, name):
+    c = s.cfg
+    return {"workload": f"{name}: {c.nk}x{c.nk} k-grid, {c.nbnd} bands ({c.nocc} occ), ~{c.npw} coefficients, "
+                        f"NGloc={s.nlf}, nw={s.no}, eta={c.eta_ev * 1000:.0f} meV; per q: Optabs xx+zz (S0, Qeff, "
+                        f"KK) + Sloss (S0, KK, Dyson, W)",
+            "ntot": int(s.ntot), "nbnd": int(s.nbnd), "npw_max": int(s.npwx), "ng": int(s.G.shape[0]),
+            "nlf": int(s.nlf), "nw": int(s.no), "q_per_step": 1, "basis_gb": round(s.coeff.nbytes / 1e9, 2)}
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), float(f[3]), f[5:9]))
+            except ValueError:
+                pass
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        load = [r for r in rows if r[2] > 200.0] or rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in load for i, v in enumerate(r[3]) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median([r[0] for r in load])), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(r[2] for r in rows)}
+
+
+# ---------------------------------------------------------------------------
+def run_step(ctx, s, rpa, host=None):
+    """One q-point: Optabs xx, Optabs zz, Sloss + Dyson.  host: dict of output buffers."""
+    want = host is not None
+    out = {}
+    for pol in ("xx", "zz"):
+        S0, Q = ctx.chi0(rpa.MODE_CURRENT, want=want, **rpa.optabs_args(s, pol))
+        chi = ctx.kk(rpa.KK_OPTABS_COMPLEX, want=want)
+        out[pol] = (S0, Q, chi)
+    S0, _ = ctx.chi0(rpa.MODE_CHARGE, want=want, **rpa.sloss_args(s))
+    chi = ctx.kk(rpa.KK_SLOSS_REAL, want=want)
+    WT, _, head = ctx.dyson(s.c0, s.cfg.eps, want_wt=want, want_epsinv=False, want_head=want)
+    out["loss"] = (S0, chi, WT, head)
+    return out
+
+
+def step_work(ctx, s, rpa):
+    """Algorithmic work of one step, from the library's own counters."""
+    work = {}
+    tot_acc = tot_vert = 0.0
+    t = {"accumulate": 0.0, "vertices": 0.0, "pairs": 0.0, "kk": 0.0, "dyson": 0.0}
+    n2 = float(s.nlf) ** 2
+    for pol in ("xx", "zz"):
+        ctx.chi0(rpa.MODE_CURRENT, want=False, **rpa.optabs_args(s, pol))
+        st, tm = ctx.chi0_stats(), ctx.stage_times()
+        tot_acc += 8.0 * n2 * st["sum_nwin"]
+        tot_vert += 8.0 * st["vertex_macs"]
+        for k in ("accumulate", "vertices", "pairs"):
+            t[k] += tm[k]
+        ctx.kk(rpa.KK_OPTABS_COMPLEX, want=False)
+        t["kk"] += ctx.stage_times()["kk"]
+        work[pol] = st
+    ctx.chi0(rpa.MODE_CHARGE, want=False, **rpa.sloss_args(s))
+    st, tm = ctx.chi0_stats(), ctx.stage_times()
+    tot_acc += 8.0 * n2 * st["sum_nwin"]
+    tot_vert += 8.0 * st["vertex_macs"]
+    for k in ("accumulate", "vertices", "pairs"):
+        t[k] += tm[k]
+    ctx.kk(rpa.KK_SLOSS_REAL, want=False)
+    t["kk"] += ctx.stage_times()["kk"]
+    ctx.dyson(s.c0, s.cfg.eps, want_wt=False, want_epsinv=False, want_head=False)
+    t["dyson"] += ctx.stage_times()["dyson"]
+    work["loss"] = st
+    return {"acc_flops": tot_acc, "vertex_flops": tot_vert, "stage_ms": t, "stats": work}
+
+
+def cpu_sample(cfg_name: str, q_steps: int, budget_s: float):
+    """Times the CPU restatement (oracle, all host threads) on a k / frequency
+    sample of one q-point and extrapolates to the whole q-point (seconds)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    synth = pkg("synth")
+    cfg = config_of(cfg_name, q_steps)
+    ntot = cfg.nk * cfg.nk
+    nthreads = os.cpu_count() or 1
+    # k sample: evenly spaced FBZ points, sized from a short probe
+    rng_k = np.linspace(0, ntot - 1, num=min(ntot, 4 * nthreads)).astype(int)
+    s = synth.build(cfg, coeff_only=rng_k)
+    parts = {}
+    per_k = 0.0
+    for name, pol in (("optabs_xx", "xx"), ("optabs_zz", "zz"), ("sloss", None)):
+        b = O.Bound(s, nthreads=nthreads, klist=rng_k, pol=pol or "xx")
+        t0 = time.perf_counter()
+        if pol:
+            O.optabs_s0(b)
+        else:
+            O.sloss_s0(b)
+        dt = time.perf_counter() - t0
+        parts[name] = dt / rng_k.size * ntot
+        per_k += dt / rng_k.size
+    # KK over a block of (G,G') pairs, scaled to nlf^2
+    nb = min(8, s.nlf)
+    So = np.random.default_rng(0).standard_normal((nb, nb, 2 * s.no + 1)) * (1 + 0j)
+    t0 = time.perf_counter()
+    O.kk_optabs(So, s.domega)
+    parts["kk_optabs_x2"] = 2 * (time.perf_counter() - t0) * (s.nlf ** 2) / (nb * nb)
+    Sl = np.random.default_rng(1).standard_normal((nb, nb, s.no))
+    t0 = time.perf_counter()
+    chi_blk = O.kk_sloss(Sl, s.domega)
+    parts["kk_sloss"] = (time.perf_counter() - t0) * (s.nlf ** 2) / (nb * nb)
+    # Dyson with the reference's 4-deep W loop on a frequency sample
+    nws = min(s.no - 1, nthreads)
+    chi = np.random.default_rng(2).standard_normal((s.nlf, s.nlf, nws + 0)) * 1e-3 + 0j
+    V = O.genV(s)
+    t0 = time.perf_counter()
+    O.dyson(np.ascontiguousarray(chi), V, fast_wt=False, nthreads=nthreads)
+    parts["dyson"] = (time.perf_counter() - t0) * (s.no - 1) / nws
+    total = sum(parts.values())
+    sample = (f"{rng_k.size} of {ntot} FBZ k-points for each of S0 xx/zz/loss (scaled by Ntot), "
+              f"KK on {nb}x{nb} of {s.nlf}x{s.nlf} (G,G') pairs, Dyson (4-deep WT loop) on {nws} of "
+              f"{s.no - 1} frequencies; extrapolated linearly")
+    return total, parts, sample, nthreads
+
+
+# ---------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo" if args.impl == "reference" else "nccl")
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        vals = []
+        for i in range(args.warmup + args.steps):
+            tq, parts, sample, cores = cpu_sample(args.config, 1, args.cpu_budget)
+            if i >= args.warmup:
+                vals.append(1.0 / tq)
+        v = float(np.median(vals))
+        cfg = config_of(args.config, 1)
+        line = {"metric": "q-point chi/W spectra/sec", "value": v, "unit": "q-spectra/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                "impl": "reference",
+                "config": {"workload": f"{args.config} (see bench.py docstring)", "l2": "n/a (CPU)"},
+                "cpu_baseline": {"value": v, "unit": "q-spectra/s", "cores": cores, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": v, "unit": "q-spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "parts_s": parts}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    rpa, synth = pkg("rpa"), pkg("synth")
+    pkg("build").build()
+    q_steps = 1 + rank  # independent q-point per rank (weak scaling, no collective)
+    cfg = config_of(args.config, q_steps)
+    t0 = time.time()
+    s = synth.build(cfg)
+    t_gen = time.time() - t0
+    prec = rpa.PREC_MIXED if args.precision == "mixed" else rpa.PREC_FP64
+    ctx = rpa.Context(device=local, precision=prec)
+    ctx.load_system(s)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+
+    for _ in range(args.warmup):
+        run_step(ctx, s, rpa)
+    work = step_work(ctx, s, rpa)
+
+    sampler = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    l0 = ctx.launch_count()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        run_step(ctx, s, rpa)
+    ev1.record(stream)
+    launches = ctx.launch_count() - l0
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = world * 1000.0 / ms
+
+    e2e = None
+    if not args.no_e2e:
+        pinned = torch.empty(s.coeff.shape, dtype=torch.complex128, pin_memory=True)
+        pc = pinned.numpy()
+        pc[...] = s.coeff
+        e2e_ms = []
+        h2d = pc.nbytes + s.E.nbytes + s.npw.nbytes + (s.igk.nbytes if s.igk is not None else 0) + \
+            s.ktot.nbytes + 5 * s.K1.nbytes + s.q.nbytes + s.ilf.nbytes + s.parG.nbytes
+        d2h = 0
+        for i in range(1 + args.steps):
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.load_basis(s.npw, s.igk, pc, s.E)
+            ctx.kmap(s.ktot, s.K1, s.R1, s.K2, s.R2, s.iG0)
+            ctx.set_q(s.q, s.ilf, s.parG)
+            out = run_step(ctx, s, rpa, host={})
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i > 0:
+                e2e_ms.append(e0.elapsed_time(e1))
+            if i == 0:
+                for v in out.values():
+                    for a in v:
+                        if a is not None:
+                            d2h += a.nbytes
+        ems = float(np.median(e2e_ms))
+        if dist:
+            t = torch.tensor([ems], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ems = float(t.item())
+        e2e = {"value": world * 1000.0 / ems, "unit": "q-spectra/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": ems}
+
+    # roofline of the dominant stage (accumulation) from the library's CUDA events
+    sm = work["stage_ms"]
+    acc_s = sm["accumulate"] / 1000.0
+    achieved_tf = work["acc_flops"] / acc_s / 1e12 if acc_s > 0 else None
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    if args.precision == "fp64":
+        roof = {"bound": "fp64", "achieved": achieved_tf, "peak": 1.25, "unit": "TFLOP/s",
+                "frac": (achieved_tf / 1.25) if achieved_tf else None, "traffic": None,
+                "peak_source": "nominal GB300 FP64 rate (no measured FP64 peak in MEASURED_PEAKS.json)",
+                "kernel": "k_accum_fp64 (+ per-chunk calls)",
+                "flops_per_step": work["acc_flops"], "flop_count": "8*NGloc^2*sum_t N_win(t)"}
+    else:
+        pk = peaks.get("bf16_tflops_sustained", 1700.0)
+        roof = {"bound": "tensor", "achieved": achieved_tf, "peak": pk, "unit": "TFLOP/s",
+                "frac": (achieved_tf / pk) if achieved_tf else None, "traffic": None}
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        tq, parts, sample, cores = cpu_sample(args.config, q_steps, args.cpu_budget)
+        cpu = {"value": 1.0 / tq, "unit": "q-spectra/s", "cores": cores, "kind": "port", "sample": sample,
+               "parts_s": {k: round(v, 3) for k, v in parts.items()}}
+
+    if rank == 0:
+        cfgd = workload_desc(s, args.config)
+        cfgd.update({"l2": "inputs larger than L2 (basis %.1f GB resident)" % (s.coeff.nbytes / 1e9),
+                     "parallelism": f"q-sharded x{world}" if world > 1 else "single GPU",
+                     "precision_path": args.precision, "setup_s": round(t_gen, 1)})
+        line = {"metric": "q-point chi/W spectra/sec", "value": value, "unit": "q-spectra/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "bf16x3/f32/f64",
+                "data": "synthetic (seeded QE-layout Bloch basis)", "config": cfgd, "clocks": clocks,
+                "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                "stage_ms_per_step": {k: round(v, 3) for k, v in sm.items()},
+                "vertex_tflops": (work["vertex_flops"] / (sm["vertices"] / 1e3) / 1e12) if sm["vertices"] else None}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -48,7 +48,9 @@ typedef struct rpa_opts {
   int device;     /* CUDA device ordinal */
   int precision;  /* RPA_PREC_FP64 (plain drop-in) or RPA_PREC_MIXED */
   int verbose;    /* 0: silent */
-  int reserved[5];
+  int split;      /* RPA_PREC_MIXED operand split: 0 = fp16 hi/lo with power-of-two
+                     scaling (default, ~2^-22 per operand), 1 = bf16 hi/lo (~2^-16) */
+  int reserved[4];
 } rpa_opts;
 
 /* Arguments of one chi0 accumulation (the namelist values the drivers use).
@@ -171,6 +173,21 @@ int rpa_stage_times(const rpa_ctx* ctx, double* ms6);
  * [1] sum over transitions of window lengths (N_win), [2] vertex complex MACs,
  * [3] accumulation launches. */
 int rpa_chi0_stats(const rpa_ctx* ctx, double* out4);
+
+/* On-device self-test of the tensor-core building blocks on the current
+ * device: which = 0, 1, 2 runs a 128 x N x 192 bf16 tcgen05 GEMM (N = 192,
+ * 96, 256) from swizzled shared-memory tiles into TMEM and stores in *result
+ * its max relative deviation from an FP32 CUDA-core product of the same
+ * values.  Returns RPA_ETIMEOUT if the bounded completion wait gave up. */
+int rpa_selftest(int which, double* result);
+
+/* Number of CUDA kernels this context has launched so far (its own kernels;
+ * the radix sort's library kernels are not counted). */
+int rpa_launch_count(const rpa_ctx* ctx, long long* count);
+
+/* The cudaStream_t (as void*) every kernel of ctx is launched on, so that a
+ * caller can order its own work or time the context with CUDA events. */
+int rpa_get_stream(const rpa_ctx* ctx, void** stream);
 
 /* Blocks until the context stream is idle. */
 int rpa_synchronize(rpa_ctx* ctx);

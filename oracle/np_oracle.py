@@ -42,8 +42,7 @@ def gfast_int(s, ik: int, ngd: int | None = None) -> np.ndarray:
     m0 = s.miller[iG0 - 1]
     out = np.empty((s.nlf, g1.size), dtype=np.int32)
     for a in range(s.nlf):
-        mlf = s.miller[s.ilf[a] - 1].copy()
-        mlf[0:2] = 0
+        mlf = s.miller[s.ilf[a] - 1]
         tgt = s.miller[g1] + mlf + m0
         out[a] = [tab2.get(tuple(t), NG2 + 1) for t in tgt.tolist()]
     return out

@@ -50,12 +50,14 @@ struct AccTcCtx {
   double scaleA;        // power of two folded into w
   float scaleB;         // power of two folded into M2
   float inv_scale;      // 1 / (scaleA scaleB)
+  int n_rows;           // rows of M / M2 (n_inter rounded up to a multiple of 32, zero padded)
+  int seg;              // chunks accumulated in one TMEM segment before it is read back
 };
 
 constexpr int TC_TT = 32;       // transitions per chunk (K = 64 16-bit values)
 constexpr int TC_GA = 128;      // G rows per tile (MMA M)
 constexpr int TC_GB = 96;       // G' rows per tile
-constexpr int TC_FLUSH = 16;    // chunks summed in FP32 before a double-float flush
+constexpr int TC_FLUSH = 32;    // chunks summed in FP32 before a double-float flush
 constexpr uint32_t TC_SPINS = 1u << 22;
 
 template <bool F16>
@@ -115,32 +117,85 @@ __device__ __forceinline__ float2 df_add(float2 a, float v) {
   return make_float2(h, l);
 }
 
-template <int NIO, bool CPLX, bool F16>
-__global__ void __launch_bounds__(256, 1) k_accum_tc(AccTcCtx A) {
-  constexpr int NB = CPLX ? 2 * TC_GB : TC_GB;               // MMA N
-  constexpr int DCOLS = NIO * NB;                            // TMEM columns per buffer
-  static_assert(DCOLS == 192, "one warpgroup column half = 96 columns");
-  constexpr uint32_t A_BYTES = TC_GA * 128, B_BYTES = NB * 128;
-  constexpr uint32_t STAGE = 2 * B_BYTES + NIO * 2 * A_BYTES;  // Bh, Bl, (Ah, Al) x NIO
-  constexpr uint32_t NCOL = 512;                               // 2 x 192 used
+// Pre-split B tiles of one 32-transition chunk, laid out exactly as the
+// 128-byte-swizzled K-major shared-memory tiles the MMA reads, so that a CTA
+// fetches them with one bulk copy:
+//   tile 0/1: B1 hi/lo, row G' = [ Re b | Im b ]          (b = sB * M2_t(G'))
+//   tile 2/3: B2 hi/lo, row G' = [ -Im b | Re b ]         (complex S0 only)
+// 96 rows per tile (rows >= nlf are zero), 12 KB per tile.
+constexpr uint32_t TC_TILE = TC_GB * 128;
+
+template <bool F16, bool CPLX>
+__global__ void k_presplit(const float2* __restrict__ M2, int nlf, int nchunks, int nht, float scaleB,
+                           unsigned char* __restrict__ tiles) {
+  const int ntile = CPLX ? 4 : 2;
+  const long long ntask = (long long)nchunks * nht * TC_GB * 4;
+  for (long long task = blockIdx.x * (long long)blockDim.x + threadIdx.x; task < ntask;
+       task += (long long)gridDim.x * blockDim.x) {
+    const int chh = (int)(task / (TC_GB * 4)), rem = (int)(task % (TC_GB * 4));
+    const int ch = chh / nht, ht = chh % nht;
+    const int row = rem % TC_GB, grp = rem / TC_GB;
+    const int g = ht * TC_GB + row;
+    float re[8], im[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      float2 m = g < nlf ? M2[((size_t)ch * TC_TT + grp * 8 + q) * nlf + g] : make_float2(0.f, 0.f);
+      re[q] = m.x * scaleB;
+      im[q] = m.y * scaleB;
+    }
+    unsigned char* t = tiles + (size_t)chh * ntile * TC_TILE;
+    uint4 rh, rl, ih, il;
+    split8<F16>(re, rh, rl);
+    split8<F16>(im, ih, il);
+    st16(t, row, grp, rh);
+    st16(t + TC_TILE, row, grp, rl);
+    st16(t, row, 4 + grp, ih);
+    st16(t + TC_TILE, row, 4 + grp, il);
+    if (CPLX) {
+      const uint32_t sg = 0x80008000u;  // split(-x) = -split(x)
+      st16(t + 2 * TC_TILE, row, grp, make_uint4(ih.x ^ sg, ih.y ^ sg, ih.z ^ sg, ih.w ^ sg));
+      st16(t + 3 * TC_TILE, row, grp, make_uint4(il.x ^ sg, il.y ^ sg, il.z ^ sg, il.w ^ sg));
+      st16(t + 2 * TC_TILE, row, 4 + grp, rh);
+      st16(t + 3 * TC_TILE, row, 4 + grp, rl);
+    }
+  }
+}
+
+// One CTA: NIO frequency rows x (128 G) x (96 G').  Per chunk the bulk copies
+// bring the pre-split B tiles, the FP32 vertex rows (for A = w M) and the
+// transition records; threads form only the A tiles.
+//   complex: D_re = A B1^T (TMEM cols 0..95), D_im = A B2^T (cols 96..191)
+//   real:    D(io0) = A(io0) B1^T, D(io1) = A(io1) B1^T
+// STAGE_M (nlf <= 96): the FP32 vertex rows come by bulk copy too; otherwise
+// the A-forming threads read them from global memory.
+template <int NIO, bool CPLX, bool F16, bool STAGE_M>
+__global__ void __launch_bounds__(256, 1) k_accum_tc(AccTcCtx A, const unsigned char* __restrict__ tiles) {
+  constexpr int NTB = CPLX ? 4 : 2;                          // B tiles per chunk
+  constexpr uint32_t A_BYTES = TC_GA * 128;
+  constexpr uint32_t BT_BYTES = NTB * TC_TILE;
+  constexpr uint32_t STAGE = BT_BYTES + NIO * 2 * A_BYTES;    // B tiles, then (Ah, Al) x NIO
+  constexpr int DCOLS = 192;                                 // TMEM columns per buffer
+  constexpr uint32_t NCOL = 512;
+  static_assert((CPLX ? 2 * NIO : NIO) * TC_GB == DCOLS, "accumulator layout");
 
   extern __shared__ unsigned char smraw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
-  __shared__ uint64_t bar[2];
+  float2* mstage = reinterpret_cast<float2*>(base + 2 * STAGE);  // [2][TC_TT][nlf]
+  __shared__ __align__(16) Trans rstage[2][TC_TT];
+  __shared__ uint64_t bar[2], mbar[2];
   __shared__ uint32_t tslot;
   __shared__ float wtab[2][NIO][TC_TT];
   __shared__ int range[2];
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int r0 = blockIdx.x * NIO;
-  const int g0 = blockIdx.y * TC_GA, h0 = blockIdx.z * TC_GB;
+  const int g0 = blockIdx.y * TC_GA, ht = blockIdx.z, h0 = ht * TC_GB, nht = gridDim.z;
   const int nrowA = min(TC_GA, A.nlf - g0), nrowB = min(TC_GB, A.nlf - h0);
   const size_t np = (size_t)A.nlf * A.nlf;
 
-  auto Bh = [&](int s) { return base + s * STAGE; };
-  auto Bl = [&](int s) { return base + s * STAGE + B_BYTES; };
-  auto Ah = [&](int s, int j) { return base + s * STAGE + 2 * B_BYTES + j * 2 * A_BYTES; };
-  auto Al = [&](int s, int j) { return base + s * STAGE + 2 * B_BYTES + j * 2 * A_BYTES + A_BYTES; };
+  auto Bt = [&](int s, int i) { return base + s * STAGE + i * TC_TILE; };
+  auto Ah = [&](int s, int j) { return base + s * STAGE + BT_BYTES + j * 2 * A_BYTES; };
+  auto Al = [&](int s, int j) { return base + s * STAGE + BT_BYTES + j * 2 * A_BYTES + A_BYTES; };
 
   if (warp == 0) {
     tc::tmem_alloc(&tslot, NCOL);
@@ -149,11 +204,14 @@ __global__ void __launch_bounds__(256, 1) k_accum_tc(AccTcCtx A) {
   if (tid == 0) {
     tc::mbar_init(&bar[0], 1);
     tc::mbar_init(&bar[1], 1);
+    tc::mbar_init(&mbar[0], 1);
+    tc::mbar_init(&mbar[1], 1);
     tc::fence_mbar_init();
-    range[0] = lb_lo(A.rec, A.n_inter, r0 - A.wmax + 1);
+    // chunks start on multiples of 32 rows; the extra leading rows get w = 0
+    range[0] = lb_lo(A.rec, A.n_inter, r0 - A.wmax + 1) & ~(TC_TT - 1);
     range[1] = lb_lo(A.rec, A.n_inter, r0 + NIO);
   }
-  // zero both stages once: padding rows stay zero for the whole kernel
+  // A padding rows (G >= nlf) stay zero for the whole kernel
   for (uint32_t e = tid; e < 2 * STAGE / 16; e += 256) reinterpret_cast<uint4*>(base)[e] = make_uint4(0, 0, 0, 0);
   tc::fence_async_smem();
   tc::tc_fence_before();
@@ -162,47 +220,62 @@ __global__ void __launch_bounds__(256, 1) k_accum_tc(AccTcCtx A) {
   const uint32_t taddr = tslot;
   const int ta = range[0], tb = range[1];
   const int nchunks = (tb - ta + TC_TT - 1) / TC_TT;
-  const uint32_t idesc = tc::idesc_bf16(TC_GA, NB, F16);
+  const uint32_t idesc = tc::idesc_bf16(TC_GA, TC_GB, F16);
+  const uint32_t mbytes = (uint32_t)(TC_TT * A.nlf * sizeof(float2));
+  const uint32_t rbytes = (uint32_t)(TC_TT * sizeof(Trans));
+
+  auto prefetch = [&](int c, int buf) {
+    const int ts = ta + c * TC_TT;
+    tc::mbar_arrive_expect_tx(&mbar[buf], BT_BYTES + (STAGE_M ? mbytes : 0u) + rbytes);
+    tc::bulk_g2s(Bt(buf, 0), tiles + ((size_t)(ts / TC_TT) * nht + ht) * BT_BYTES, BT_BYTES, &mbar[buf]);
+    if (STAGE_M) tc::bulk_g2s(mstage + (size_t)buf * TC_TT * A.nlf, A.M + (size_t)ts * A.nlf, mbytes, &mbar[buf]);
+    tc::bulk_g2s(&rstage[buf][0], A.rec + ts, rbytes, &mbar[buf]);
+  };
+  if (tid == 0 && nchunks > 0) prefetch(0, 0);
 
   // this thread's slice of the accumulator: TMEM lane quarter wq, column half hf
   const int wq = warp & 3, hf = warp >> 2;
-  const int grow = g0 + wq * 32 + lane;               // G
+  const int grow = g0 + wq * 32 + lane;                // G
   const int io_t = CPLX ? r0 : r0 + hf;                // frequency row of this slice
-  const int comp = CPLX ? hf : 0;                       // Re / Im
+  const int comp = CPLX ? hf : 0;                      // Re / Im
   float acc[96];
 #pragma unroll
   for (int i = 0; i < 96; ++i) acc[i] = 0.f;
 
   auto consume = [&](int buf) {
+    float v[96];
+    const uint32_t a0 = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)(buf * DCOLS + hf * 96);
+    tc::tmem_ld32(a0, v);
+    tc::tmem_ld32(a0 + 32, v + 32);
+    tc::tmem_ld32(a0 + 64, v + 64);
+    tc::tmem_ld_wait();
 #pragma unroll
-    for (int c0 = 0; c0 < 96; c0 += 32) {
-      float v[32];
-      tc::tmem_ld32(taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)(buf * DCOLS + hf * 96 + c0), v);
-      tc::tmem_ld_wait();
-#pragma unroll
-      for (int i = 0; i < 32; ++i) acc[c0 + i] += v[i];
-    }
+    for (int i = 0; i < 96; ++i) acc[i] += v[i];
   };
   auto flush = [&]() {
     if (grow < A.nlf && io_t < A.nw) {
       const int ncomp = CPLX ? 2 : 1;
-#pragma unroll 4
-      for (int j = 0; j < 96; ++j) {
-        if (j < nrowB) {
-          size_t p = (size_t)grow + (size_t)A.nlf * (h0 + j);
-          float2* dst = A.Sdf + ((size_t)io_t * np + p) * ncomp + comp;
-          *dst = df_add(*dst, acc[j] * A.inv_scale);
-        }
-        acc[j] = 0.f;
-      }
-    } else {
+      float2* rowp = A.Sdf + ((size_t)io_t * np + (size_t)grow + (size_t)A.nlf * h0) * ncomp + comp;
+      const size_t step = (size_t)A.nlf * ncomp;
+      const int nb = nrowB;
 #pragma unroll
-      for (int j = 0; j < 96; ++j) acc[j] = 0.f;
+      for (int j0 = 0; j0 < 96; j0 += 16) {
+        float2 old[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (j0 + j < nb) old[j] = rowp[(j0 + j) * step];
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (j0 + j < nb) rowp[(j0 + j) * step] = df_add(old[j], acc[j0 + j] * A.inv_scale);
+      }
     }
+#pragma unroll
+    for (int j = 0; j < 96; ++j) acc[j] = 0.f;
   };
 
   bool abort = false;
   int last_commit = -1, consumed = 0;
+  const int L = A.seg;
 
   for (int c = 0; c < nchunks && !abort; ++c) {
     const int s = c & 1;
@@ -212,34 +285,47 @@ __global__ void __launch_bounds__(256, 1) k_accum_tc(AccTcCtx A) {
       if (!ok) atomicExch(A.status, 1);
       abort = __syncthreads_or(!ok);
       if (abort) break;
-      tc::tc_fence_after();
-      consume(s);  // result of chunk c-2
-      tc::tc_fence_before();
-      if (++consumed % TC_FLUSH == 0) flush();
+      if ((c - 2) % L == L - 1) {  // chunk c-2 closed its segment: read it back
+        tc::tc_fence_after();
+        consume(((c - 2) / L) & 1);
+        tc::tc_fence_before();
+        if (++consumed % TC_FLUSH == 0) flush();
+      }
     }
-    // Lorentzian weights of this chunk for the NIO rows (scaled)
+    // prefetch chunk c+1 (its stage was last read by the MMAs of chunk c-1 and
+    // by the formation of chunk c-1, both finished)
+    if (tid == 0 && c + 1 < nchunks) prefetch(c + 1, s ^ 1);
+    {
+      bool ok = tc::mbar_wait(&mbar[s], (c >> 1) & 1, TC_SPINS);
+      if (!ok) atomicExch(A.status, 1);
+      abort = __syncthreads_or(!ok);
+      if (abort) break;
+    }
+    // Lorentzian weights of this chunk for the NIO rows (scaled); window
+    // membership is the exact [lo, hi] of the record
     if (tid < NIO * TC_TT) {
       int j = tid / TC_TT, tt = tid % TC_TT, t = ts + tt, r = r0 + j;
       float w = 0.f;
       if (t < tb && r < A.nw) {
-        const Trans& R = A.rec[t];
+        const Trans& R = rstage[s][tt];
         if (r >= R.lo && r <= R.hi) {
-          bool in;
-          double L = lorentz_tc(A, r, R.e1, R.e2, &in);
-          if (in) w = (float)(R.c * L * A.scaleA);
+          float dE = (float)fma((double)(r + A.obase), A.domega, R.e1 - R.e2);
+          float eta = (float)A.eta;
+          float L2 = eta / fmaf(dE, dE, eta * eta);
+          w = (float)(R.c * A.scaleA) * L2;
         }
       }
       wtab[s][j][tt] = w;
     }
     __syncthreads();
-    // A tiles: rows G = g0 + row, 8 transitions per task
+    // A tiles: rows G, 8 transitions per task
+    const float2* msrc = STAGE_M ? mstage + (size_t)s * TC_TT * A.nlf : A.M + (size_t)ts * A.nlf + g0;
     for (int e = tid; e < nrowA * 4; e += 256) {
       const int row = e % nrowA, grp = e / nrowA;
       float re[8], im[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        int t = ts + grp * 8 + q;
-        float2 m = t < A.n_inter ? A.M[(size_t)t * A.nlf + g0 + row] : make_float2(0.f, 0.f);
+        float2 m = msrc[(size_t)(grp * 8 + q) * A.nlf + row];
         re[q] = m.x;
         im[q] = m.y;
       }
@@ -261,100 +347,61 @@ __global__ void __launch_bounds__(256, 1) k_accum_tc(AccTcCtx A) {
         st16(Al(s, j), row, 4 + grp, lo);
       }
     }
-    // B tiles: rows G' = h0 + row (and 96 + row for the imaginary part)
-    for (int e = tid; e < nrowB * 4; e += 256) {
-      const int row = e % nrowB, grp = e / nrowB;
-      float re[8], im[8], nim[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        int t = ts + grp * 8 + q;
-        float2 m = t < A.n_inter ? A.M2[(size_t)t * A.nlf + h0 + row] : make_float2(0.f, 0.f);
-        re[q] = m.x * A.scaleB;
-        im[q] = m.y * A.scaleB;
-        nim[q] = -im[q];
-      }
-      uint4 hi, lo;
-      split8<F16>(re, hi, lo);
-      st16(Bh(s), row, grp, hi);
-      st16(Bl(s), row, grp, lo);
-      if (CPLX) {
-        st16(Bh(s), TC_GB + row, 4 + grp, hi);
-        st16(Bl(s), TC_GB + row, 4 + grp, lo);
-      }
-      split8<F16>(im, hi, lo);
-      st16(Bh(s), row, 4 + grp, hi);
-      st16(Bl(s), row, 4 + grp, lo);
-      if (CPLX) {
-        split8<F16>(nim, hi, lo);
-        st16(Bh(s), TC_GB + row, grp, hi);
-        st16(Bl(s), TC_GB + row, grp, lo);
-      }
-    }
     tc::fence_async_smem();
     __syncthreads();
     if (tid == 0) {
       tc::tc_fence_after();
-      const uint32_t bh = tc::smem_u32(Bh(s)), bl = tc::smem_u32(Bl(s));
+      const uint32_t first = (c % L) == 0 ? 0u : 1u;
+      const int dbuf = (c / L) & 1;
 #pragma unroll
       for (int j = 0; j < NIO; ++j) {
         const uint32_t ah = tc::smem_u32(Ah(s, j)), al = tc::smem_u32(Al(s, j));
-        const uint32_t d = taddr + (uint32_t)(s * DCOLS + j * NB);
-        // cross products first (fresh accumulator), the large hi*hi products last
 #pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-          const uint32_t ko = ks * 32;
-          tc::mma_bf16(d, tc::desc_sw128(ah + ko), tc::desc_sw128(bl + ko), idesc, ks > 0 ? 1u : 0u);
-          tc::mma_bf16(d, tc::desc_sw128(al + ko), tc::desc_sw128(bh + ko), idesc, 1u);
-        }
+        for (int part = 0; part < (CPLX ? 2 : 1); ++part) {
+          const uint32_t bh = tc::smem_u32(Bt(s, 2 * part)), bl = tc::smem_u32(Bt(s, 2 * part + 1));
+          const uint32_t d = taddr + (uint32_t)(dbuf * DCOLS + (j + part) * TC_GB);
+          // cross products first, the large hi*hi products last
 #pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-          const uint32_t ko = ks * 32;
-          tc::mma_bf16(d, tc::desc_sw128(ah + ko), tc::desc_sw128(bh + ko), idesc, 1u);
+          for (int ks = 0; ks < 4; ++ks) {
+            const uint32_t ko = ks * 32;
+            tc::mma_bf16(d, tc::desc_sw128(ah + ko), tc::desc_sw128(bl + ko), idesc, ks > 0 ? 1u : first);
+            tc::mma_bf16(d, tc::desc_sw128(al + ko), tc::desc_sw128(bh + ko), idesc, 1u);
+          }
+#pragma unroll
+          for (int ks = 0; ks < 4; ++ks) {
+            const uint32_t ko = ks * 32;
+            tc::mma_bf16(d, tc::desc_sw128(ah + ko), tc::desc_sw128(bh + ko), idesc, 1u);
+          }
         }
       }
       tc::mma_commit(&bar[s]);
     }
     last_commit = c;
   }
-  // drain the last (up to) two chunks
+  // drain the last (up to) two chunks: read back the segments they close
   if (!abort) {
     for (int cc = (nchunks >= 2 ? nchunks - 2 : 0); cc < nchunks; ++cc) {
+      if (!(cc % L == L - 1 || cc == nchunks - 1)) continue;
       const int s = cc & 1;
       bool ok = tc::mbar_wait(&bar[s], (cc >> 1) & 1, TC_SPINS);
       if (!ok) atomicExch(A.status, 1);
       abort = __syncthreads_or(!ok);
       if (abort) break;
       tc::tc_fence_after();
-      consume(s);
+      consume((cc / L) & 1);
       tc::tc_fence_before();
     }
     if (!abort) flush();
   }
-  if (abort && tid == 0 && last_commit >= 0) {
-    // let the MMAs already issued finish before the TMEM is released
-    tc::mbar_wait(&bar[last_commit & 1], (last_commit >> 1) & 1, TC_SPINS);
+  if (abort && tid == 0) {
+    // let the MMAs and bulk copies already issued finish before the TMEM and
+    // shared memory are released
+    if (last_commit >= 0) tc::mbar_wait(&bar[last_commit & 1], (last_commit >> 1) & 1, TC_SPINS);
+    for (int b = 0; b < 2; ++b) tc::mbar_wait(&mbar[b], 0, 1024), tc::mbar_wait(&mbar[b], 1, 1024);
   }
   tc::tc_fence_before();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
-}
-
-// Sorted FP32 copies of the FP64 vertices, Mf[i] = M[order[i]], and the
-// largest |component| (as float bits) for the power-of-two operand scaling.
-__global__ void k_pack_sorted(const Trans* __restrict__ rec, const double2* __restrict__ M, float2* __restrict__ Mf,
-                              int n, int nlf, unsigned* amax) {
-  size_t tot = (size_t)n * nlf;
-  float mx = 0.f;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
-    size_t i = e / nlf;
-    int g = (int)(e % nlf);
-    double2 v = M[(size_t)rec[i].k * nlf + g];
-    float2 f = make_float2((float)v.x, (float)v.y);
-    Mf[e] = f;
-    mx = fmaxf(mx, fmaxf(fabsf(f.x), fabsf(f.y)));
-  }
-  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(amax, __float_as_uint(mx));
 }
 
 __global__ void k_cmax(const Trans* __restrict__ rec, int n, unsigned long long* cmax) {
@@ -371,15 +418,24 @@ __global__ void k_df_to_f64(const float2* __restrict__ Sdf, double* __restrict__
   }
 }
 
-template <int NIO, bool CPLX, bool F16>
-static int launch_tc(rpa_ctx* c, const AccTcCtx& A, int nw) {
-  constexpr int NB = CPLX ? 2 * TC_GB : TC_GB;
-  constexpr size_t STAGE = 2 * (size_t)NB * 128 + (size_t)NIO * 2 * TC_GA * 128;
-  const size_t smem = 2 * STAGE + 1024;
-  auto kern = k_accum_tc<NIO, CPLX, F16>;
+template <int NIO, bool CPLX, bool F16, bool STAGE_M>
+static int launch_tc(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char* tiles) {
+  constexpr int NTB = CPLX ? 4 : 2;
+  constexpr size_t STAGE = (size_t)NTB * TC_TILE + (size_t)NIO * 2 * TC_GA * 128;
+  const size_t smem = 2 * STAGE + 1024 + (STAGE_M ? 2 * (size_t)TC_TT * A.nlf * sizeof(float2) : 0);
+  auto kern = k_accum_tc<NIO, CPLX, F16, STAGE_M>;
   RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((nw + NIO - 1) / NIO, (A.nlf + TC_GA - 1) / TC_GA, (A.nlf + TC_GB - 1) / TC_GB);
-  kern<<<grid, 256, smem, c->stream>>>(A);
+  kern<<<grid, 256, smem, c->stream>>>(A, tiles);
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  return RPA_OK;
+}
+
+template <bool F16, bool CPLX>
+static int launch_presplit(rpa_ctx* c, const float2* M2, int nchunks, float scaleB, unsigned char* tiles) {
+  const int nht = (c->nlf + TC_GB - 1) / TC_GB;
+  k_presplit<F16, CPLX><<<4096, 256, 0, c->stream>>>(M2, c->nlf, nchunks, nht, scaleB, tiles);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
   return RPA_OK;
@@ -411,43 +467,82 @@ int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const fl
   A.scaleA = (f16 && amA > 0) ? 16384.0 / pow2_floor(amA) : 1.0;
   A.scaleB = (f16 && amB > 0) ? (float)(16384.0 / pow2_floor(amB)) : 1.0f;
   A.inv_scale = (float)(1.0 / (A.scaleA * (double)A.scaleB));
-  if (P.mode == RPA_MODE_CURRENT)
-    return f16 ? launch_tc<1, true, true>(c, A, P.nw) : launch_tc<1, true, false>(c, A, P.nw);
-  return f16 ? launch_tc<2, false, true>(c, A, P.nw) : launch_tc<2, false, false>(c, A, P.nw);
+  A.n_rows = (n_inter + TC_TT - 1) / TC_TT * TC_TT;
+  A.seg = c->tc_seg > 0 ? c->tc_seg : 1;
+  const bool cplx = P.mode == RPA_MODE_CURRENT;
+  const int nch = A.n_rows / TC_TT + 1;  // one spare chunk for the last prefetch
+  const int nht = (c->nlf + TC_GB - 1) / TC_GB;
+  const size_t tbytes = (size_t)nch * nht * (cplx ? 4 : 2) * TC_TILE;
+  RPA_TRY(ensure(c, c->d_tiles, tbytes));
+  unsigned char* tiles = c->d_tiles.as<unsigned char>();
+  const bool st = c->nlf <= TC_GB;  // whole vertex rows fit the bulk-copy staging
+  if (cplx) {
+    RPA_TRY(f16 ? launch_presplit<true, true>(c, Mf2, nch, A.scaleB, tiles)
+                : launch_presplit<false, true>(c, Mf2, nch, A.scaleB, tiles));
+    if (st) return f16 ? launch_tc<1, true, true, true>(c, A, P.nw, tiles) : launch_tc<1, true, false, true>(c, A, P.nw, tiles);
+    return f16 ? launch_tc<1, true, true, false>(c, A, P.nw, tiles) : launch_tc<1, true, false, false>(c, A, P.nw, tiles);
+  }
+  RPA_TRY(f16 ? launch_presplit<true, false>(c, Mf2, nch, A.scaleB, tiles)
+              : launch_presplit<false, false>(c, Mf2, nch, A.scaleB, tiles));
+  if (st) return f16 ? launch_tc<2, false, true, true>(c, A, P.nw, tiles) : launch_tc<2, false, false, true>(c, A, P.nw, tiles);
+  return f16 ? launch_tc<2, false, true, false>(c, A, P.nw, tiles) : launch_tc<2, false, false, false>(c, A, P.nw, tiles);
 }
 
-// Packs the sorted FP32 vertices and returns the scaling statistics.
-int pack_sorted_fp32(rpa_ctx* c, int n_inter, float2* Mf, float2* Mf2, bool two, float* amaxM, float* amaxM2,
-                     double* cmax) {
-  *amaxM = *amaxM2 = 0.f;
+__global__ void k_inverse_perm(const int* __restrict__ order, int* __restrict__ pos_of, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) pos_of[order[i]] = i;
+}
+
+// Qeff += c M conj(M2) over the intraband rows [t_begin, t_end) of the sorted
+// FP32 vertices (one (G,G') element per thread, rows in emission order).
+__global__ void k_qeff_f32(const Trans* __restrict__ rec, int t_begin, int t_end, const float2* __restrict__ M,
+                           const float2* __restrict__ M2, int nlf, double2* __restrict__ Q) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nlf * nlf) return;
+  int gi = p % nlf, gj = p / nlf;
+  double qr = 0.0, qi = 0.0;
+  for (int t = t_begin; t < t_end; ++t) {
+    float2 a = M[(size_t)t * nlf + gi], b = M2[(size_t)t * nlf + gj];
+    double xr = (double)a.x * b.x + (double)a.y * b.y, xi = (double)a.y * b.x - (double)a.x * b.y;
+    double cc = rec[t].c;
+    qr += cc * xr;
+    qi += cc * xi;
+  }
+  double2 v = Q[p];
+  v.x += qr;
+  v.y += qi;
+  Q[p] = v;
+}
+
+int inverse_perm(rpa_ctx* c, int n, int* pos_of) {
+  if (n == 0) return RPA_OK;
+  k_inverse_perm<<<(n + 255) / 256, 256, 0, c->stream>>>(c->d_vals_alt.as<int>(), pos_of, n);
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  return RPA_OK;
+}
+
+int qeff_f32(rpa_ctx* c, int n_inter, int n_trans, const float2* Mf, const float2* Mf2) {
+  if (n_trans <= n_inter) return RPA_OK;
+  int np = c->nlf * c->nlf;
+  k_qeff_f32<<<(np + 127) / 128, 128, 0, c->stream>>>(c->d_sorted.as<Trans>(), n_inter, n_trans, Mf, Mf2, c->nlf,
+                                                      c->d_Q.as<double2>());
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  return RPA_OK;
+}
+
+// max |c| over the interband records (for the power-of-two operand scaling)
+int cmax_of(rpa_ctx* c, int n_inter, double* cmax) {
   *cmax = 0.0;
   if (n_inter == 0) return RPA_OK;
-  RPA_TRY(ensure(c, c->d_ntrans, 32));
-  RPA_CUDA(c, cudaMemsetAsync(c->d_ntrans.p, 0, 32, c->stream));
-  unsigned* am = c->d_ntrans.as<unsigned>();
-  k_pack_sorted<<<2048, 256, 0, c->stream>>>(c->d_sorted.as<Trans>(), c->d_M.as<double2>(), Mf, n_inter, c->nlf, am);
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(c->d_ntrans.as<char>() + 8);
+  RPA_CUDA(c, cudaMemsetAsync(d, 0, 8, c->stream));
+  k_cmax<<<256, 256, 0, c->stream>>>(c->d_sorted.as<Trans>(), n_inter, d);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
-  if (two) {
-    k_pack_sorted<<<2048, 256, 0, c->stream>>>(c->d_sorted.as<Trans>(), c->d_M2.as<double2>(), Mf2, n_inter,
-                                               c->nlf, am + 1);
-    RPA_CUDA(c, cudaGetLastError());
-    ++c->launches;
-  }
-  k_cmax<<<256, 256, 0, c->stream>>>(c->d_sorted.as<Trans>(), n_inter,
-                                     reinterpret_cast<unsigned long long*>(c->d_ntrans.as<char>() + 8));
-  RPA_CUDA(c, cudaGetLastError());
-  ++c->launches;
-  unsigned char h[16];
-  RPA_CUDA(c, cudaMemcpyAsync(h, c->d_ntrans.p, 16, cudaMemcpyDeviceToHost, c->stream));
+  RPA_CUDA(c, cudaMemcpyAsync(cmax, d, 8, cudaMemcpyDeviceToHost, c->stream));
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
-  unsigned u0, u1;
-  std::memcpy(&u0, h, 4);
-  std::memcpy(&u1, h + 4, 4);
-  std::memcpy(cmax, h + 8, 8);
-  std::memcpy(amaxM, &u0, 4);
-  std::memcpy(amaxM2, &u1, 4);
-  if (!two) *amaxM2 = *amaxM;
   return RPA_OK;
 }
 

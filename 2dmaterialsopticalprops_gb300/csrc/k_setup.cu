@@ -259,7 +259,7 @@ int sort_trans(rpa_ctx* c, int n_trans, int nw) {
   RPA_CUDA(c, cub::DeviceRadixSort::SortPairs(c->d_cub.p, tb, c->d_keys.as<int>(), c->d_keys_alt.as<int>(),
                                               c->d_vals.as<int>(), c->d_vals_alt.as<int>(), n_trans, 0,
                                               end_bit, c->stream));
-  RPA_TRY(ensure(c, c->d_sorted, sizeof(Trans) * (size_t)n_trans));
+  RPA_TRY(ensure(c, c->d_sorted, sizeof(Trans) * ((size_t)n_trans + 64)));  // whole chunks for bulk copies
   k_gather_sorted<<<(n_trans + 255) / 256, 256, 0, c->stream>>>(c->d_trans.as<Trans>(), c->d_vals_alt.as<int>(),
                                                                 c->d_sorted.as<Trans>(), n_trans);
   RPA_CUDA(c, cudaGetLastError());

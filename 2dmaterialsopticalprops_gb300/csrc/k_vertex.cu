@@ -205,6 +205,158 @@ __global__ void __launch_bounds__(256) k_vertex_fp64(MapCtx C, const double2* __
   }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed path: FP32 complex coefficients, FP32 sums over slices of IC
+// coefficients carried in double-float (hi + lo) across slices, result
+// written as complex64 straight into the window-sorted row pos[t] that the
+// tensor-core accumulation reads.  amax collects max |Re|, |Im| (float bits).
+__device__ __forceinline__ void df_acc(float& hi, float& lo, float v) {
+  float s = hi + v;
+  float bb = s - hi;
+  float e = (hi - (s - bb)) + (v - bb);
+  lo += e;
+  float h = s + lo;
+  lo = lo - (h - s);
+  hi = h;
+}
+
+template <int IC, int MAXO, bool CURRENT, bool TWO>
+__global__ void __launch_bounds__(256) k_vertex_f32(MapCtx C, const float2* __restrict__ coeff,
+                                                    const Trans* __restrict__ trans,
+                                                    const long long* __restrict__ offsets,
+                                                    const int* __restrict__ pos_of, int k0, int GC, int nbnd,
+                                                    int ca, int cb, float2* __restrict__ M, float2* __restrict__ M2,
+                                                    unsigned* __restrict__ amax) {
+  extern __shared__ float2 smf[];
+  const int kl = blockIdx.x;
+  const int ik = k0 + kl;
+  const long long t0 = offsets[kl], t1 = offsets[kl + 1];
+  const int P = (int)(t1 - t0);
+  if (P == 0) return;
+  const int g0 = blockIdx.y * GC;
+  const int ng_here = min(GC, C.nlf - g0);
+  if (ng_here <= 0) return;
+  const int* km = C.kmap + 5 * ik;
+  const int K1 = km[0], K2 = km[2];
+  const int nsum = C.legacy ? C.nsum_legacy : C.npw[K1];
+  const double* kv = C.ktot + 3 * ik;
+
+  float2* C1s = smf;                               // [IC][nbnd]
+  float2* C2s = C1s + IC * nbnd;                   // [GC][IC][nbnd]
+  float2* C2b = C2s + (size_t)GC * IC * nbnd;      // second component (TWO)
+  int* pos_s = reinterpret_cast<int*>(C2b + (TWO ? (size_t)GC * IC * nbnd : 0));  // [GC][IC]
+  float2* fac_s = reinterpret_cast<float2*>(pos_s + GC * IC);                     // [GC][IC]
+
+  const int nout = P * ng_here;
+  float ahr[MAXO], alr[MAXO], ahi[MAXO], ali[MAXO];
+  float bhr[MAXO], blr[MAXO], bhi[MAXO], bli[MAXO];
+  int on[MAXO], om[MAXO];
+#pragma unroll
+  for (int u = 0; u < MAXO; ++u) {
+    ahr[u] = alr[u] = ahi[u] = ali[u] = bhr[u] = blr[u] = bhi[u] = bli[u] = 0.f;
+    int o = threadIdx.x + 256 * u;
+    if (o < nout) {
+      int nm = trans[t0 + o / ng_here].nm;
+      on[u] = nm & 0xffff;
+      om[u] = ((o % ng_here) * IC) * nbnd + (nm >> 16);
+    } else {
+      on[u] = 0;
+      om[u] = -1;
+    }
+  }
+
+  for (int i0 = 0; i0 < nsum; i0 += IC) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < ng_here * IC; e += 256) {
+      int g = e / IC, ii = e % IC, i = i0 + ii;
+      int pos = -1;
+      float2 f = make_float2(1.f, 1.f);
+      if (i < nsum) {
+        pos = gfast_pos(C, km, g0 + g, i);
+        if (CURRENT) {
+          double2 fd = current_factor(C, km, kv, g0 + g, i, ca, cb);
+          f = make_float2((float)fd.x, (float)fd.y);
+        }
+      }
+      pos_s[e] = pos;
+      fac_s[e] = f;
+    }
+    for (int e = threadIdx.x; e < IC * nbnd; e += 256) {
+      int ii = e / nbnd, b = e % nbnd, i = i0 + ii;
+      C1s[e] = i < nsum ? coeff[((size_t)K1 * C.npwx + i) * nbnd + b] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < ng_here * IC * nbnd; e += 256) {
+      int gi = e / nbnd, b = e % nbnd;
+      int pos = pos_s[gi];
+      float2 v = pos >= 0 ? coeff[((size_t)K2 * C.npwx + pos) * nbnd + b] : make_float2(0.f, 0.f);
+      if (CURRENT) {
+        float2 f = fac_s[gi];
+        C2s[e] = make_float2(v.x * f.x, v.y * f.x);
+        if (TWO) C2b[e] = make_float2(v.x * f.y, v.y * f.y);
+      } else {
+        C2s[e] = v;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < MAXO; ++u) {
+      if (om[u] < 0) continue;
+      const float2* c1 = C1s + on[u];
+      const float2* c2 = C2s + om[u];
+      const float2* c2b = C2b + om[u];
+      float ar = 0.f, ai = 0.f, br = 0.f, bi = 0.f;
+#pragma unroll 8
+      for (int ii = 0; ii < IC; ++ii) {
+        float2 a = c1[ii * nbnd];
+        float2 b = c2[ii * nbnd];
+        ar = fmaf(a.x, b.x, ar);
+        ar = fmaf(a.y, b.y, ar);
+        ai = fmaf(a.x, b.y, ai);
+        ai = fmaf(-a.y, b.x, ai);
+        if (TWO) {
+          float2 d = c2b[ii * nbnd];
+          br = fmaf(a.x, d.x, br);
+          br = fmaf(a.y, d.y, br);
+          bi = fmaf(a.x, d.y, bi);
+          bi = fmaf(-a.y, d.x, bi);
+        }
+      }
+      df_acc(ahr[u], alr[u], ar);
+      df_acc(ahi[u], ali[u], ai);
+      if (TWO) {
+        df_acc(bhr[u], blr[u], br);
+        df_acc(bhi[u], bli[u], bi);
+      }
+    }
+  }
+  float mx = 0.f, mx2 = 0.f;
+#pragma unroll
+  for (int u = 0; u < MAXO; ++u) {
+    int o = threadIdx.x + 256 * u;
+    if (o >= nout) continue;
+    long long t = t0 + o / ng_here;
+    int g = g0 + o % ng_here;
+    size_t row = (size_t)pos_of[t];
+    float2 v = make_float2(ahr[u] + alr[u], ahi[u] + ali[u]);
+    M[row * C.nlf + g] = v;
+    mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+    if (TWO) {
+      float2 w = make_float2(bhr[u] + blr[u], bhi[u] + bli[u]);
+      M2[row * C.nlf + g] = w;
+      mx2 = fmaxf(mx2, fmaxf(fabsf(w.x), fabsf(w.y)));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(amax, __float_as_uint(mx));
+    if (TWO) atomicMax(amax + 1, __float_as_uint(mx2));
+  }
+}
+
 MapCtx make_map_ctx(rpa_ctx* c) {
   MapCtx C;
   C.kmap = c->d_kmap.as<int>();
@@ -282,6 +434,77 @@ int vertices_fp64(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, l
     RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<grid, 256, smem, c->stream>>>(C, coeff, tr, off, k0, GC, c->nbnd, ca, cb, M, M2);
   }
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  return RPA_OK;
+}
+
+// Mixed-path vertices of the n_trans transitions of FBZ k-points [k0, k0+nk),
+// written to rows pos_of[t] of Mf (and Mf2).
+int vertices_f32(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, long long n_trans, const int* pos_of,
+                 float2* Mf, float2* Mf2, unsigned* amax) {
+  if (n_trans == 0) return RPA_OK;
+  const bool current = P.mode == RPA_MODE_CURRENT;
+  const bool two = current && (P.pol == RPA_POL_YZ || P.pol == RPA_POL_ZY);
+  MapCtx C = make_map_ctx(c);
+  C.nsum_legacy = P.nsum_legacy;
+  C.Gcar = P.Gcar;
+  constexpr int IC = 32, MAXO = 8;
+  int GC = maxpairs > 0 ? (MAXO * 256) / maxpairs : 1;
+  GC = GC < 1 ? 1 : (GC > 16 ? 16 : GC);
+  if (GC > c->nlf) GC = c->nlf;
+  if (maxpairs * GC > MAXO * 256) return fail(c, RPA_EINVAL, "too many band pairs per k-point (%d)", maxpairs);
+  int ca = 0, cb = 0;
+  switch (P.pol) {
+    case RPA_POL_XX: ca = cb = 0; break;
+    case RPA_POL_YY: ca = cb = 1; break;
+    case RPA_POL_ZZ: ca = cb = 2; break;
+    case RPA_POL_YZ: ca = 1; cb = 2; break;
+    default: ca = 2; cb = 1; break;
+  }
+  size_t smem = sizeof(float2) * ((size_t)IC * c->nbnd + (size_t)GC * IC * c->nbnd * (two ? 2 : 1)) +
+                sizeof(int) * (size_t)GC * IC + sizeof(float2) * (size_t)GC * IC;
+  dim3 grid(nk, (c->nlf + GC - 1) / GC);
+  const float2* coeff = c->d_coeff32.as<float2>();
+  const Trans* tr = c->d_trans.as<Trans>();
+  const long long* off = c->d_offsets.as<long long>();
+  if (!current) {
+    auto kern = k_vertex_f32<IC, MAXO, false, false>;
+    RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<grid, 256, smem, c->stream>>>(C, coeff, tr, off, pos_of, k0, GC, c->nbnd, ca, cb, Mf, Mf, amax);
+  } else if (!two) {
+    auto kern = k_vertex_f32<IC, MAXO, true, false>;
+    RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<grid, 256, smem, c->stream>>>(C, coeff, tr, off, pos_of, k0, GC, c->nbnd, ca, cb, Mf, Mf, amax);
+  } else {
+    auto kern = k_vertex_f32<IC, MAXO, true, true>;
+    RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<grid, 256, smem, c->stream>>>(C, coeff, tr, off, pos_of, k0, GC, c->nbnd, ca, cb, Mf, Mf2, amax);
+  }
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  return RPA_OK;
+}
+
+// Gfast maps of the FBZ k-points [k0, k0+nk) as int16 basis positions
+// (-1 absent), gmap[k_local][G][i] for i < nsum_max (-1 beyond nsum).
+__global__ void k_gmap(MapCtx C, int k0, int nk, int nsum_max, int16_t* __restrict__ gmap) {
+  const size_t per_k = (size_t)C.nlf * nsum_max;
+  const size_t n = (size_t)nk * per_k;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    int kl = (int)(e / per_k);
+    size_t r = e % per_k;
+    int g = (int)(r / nsum_max), i = (int)(r % nsum_max);
+    const int* km = C.kmap + 5 * (k0 + kl);
+    int nsum = C.legacy ? C.nsum_legacy : C.npw[km[0]];
+    gmap[e] = (int16_t)(i < nsum ? gfast_pos(C, km, g, i) : -1);
+  }
+}
+
+int build_gmap(rpa_ctx* c, int k0, int nk, int nsum_max, int16_t* gmap, int nsum_legacy) {
+  MapCtx C = make_map_ctx(c);
+  C.nsum_legacy = nsum_legacy;
+  k_gmap<<<4096, 256, 0, c->stream>>>(C, k0, nk, nsum_max, gmap);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
   return RPA_OK;

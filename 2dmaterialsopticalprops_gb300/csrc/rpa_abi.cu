@@ -23,9 +23,14 @@ int vertices_fp64(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, l
 int accumulate_fp64(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax);
 int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const float2* Mf, const float2* Mf2,
                   float amaxM, float amaxM2, double cmax);
-int pack_sorted_fp32(rpa_ctx* c, int n_inter, float2* Mf, float2* Mf2, bool two, float* amaxM, float* amaxM2,
-                     double* cmax);
 int df_to_f64(rpa_ctx* c, size_t n);
+int inverse_perm(rpa_ctx* c, int n, int* pos_of);
+int qeff_f32(rpa_ctx* c, int n_inter, int n_trans, const float2* Mf, const float2* Mf2);
+int cmax_of(rpa_ctx* c, int n_inter, double* cmax);
+int vertices_f32(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, long long n_trans, const int* pos_of,
+                 float2* Mf, float2* Mf2, unsigned* amax);
+int vertices_tc(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans, const int* pos_of, float2* Mf,
+                float2* Mf2, unsigned* amax, bool* used);
 int qeff_fp64(rpa_ctx* c, const Chi0Plan& P, int n_inter, int n_trans);
 int kk_run(rpa_ctx* c, int variant, int no, double domega);
 int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singular, int* n_zero);
@@ -86,6 +91,13 @@ __global__ void k_basis_transpose(const double2* __restrict__ src, double2* __re
     int i = (int)(r % npwx);
     int k = (int)(r / npwx);
     dst[e] = src[((size_t)k * nbnd + b) * npwx + i];
+  }
+}
+
+__global__ void k_to_f32(const double2* __restrict__ src, float2* __restrict__ dst, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    double2 v = src[e];
+    dst[e] = make_float2((float)v.x, (float)v.y);
   }
 }
 
@@ -232,6 +244,8 @@ int rpa_create(rpa_ctx** out, const rpa_opts* opts) {
   c->precision = opts ? opts->precision : RPA_PREC_FP64;
   c->verbose = opts ? opts->verbose : 0;
   c->split_f16 = opts ? opts->split == 0 : true;
+  c->tc_seg = (opts && opts->reserved[0] > 0) ? opts->reserved[0] : 1;
+  c->vertex_tc = !(opts && opts->reserved[1] == 1);
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete c;
@@ -250,7 +264,7 @@ int rpa_destroy(rpa_ctx* c) {
   DevBuf* bufs[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
                     &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_E, &c->d_kmap, &c->d_ktot, &c->d_lf_miller,
                     &c->d_Glf, &c->d_occ, &c->d_counts, &c->d_offsets, &c->d_trans, &c->d_keys, &c->d_keys_alt,
-                    &c->d_vals, &c->d_vals_alt, &c->d_sorted, &c->d_M, &c->d_M2, &c->d_Mf, &c->d_Mf2, &c->d_cub, &c->d_wmax,
+                    &c->d_vals, &c->d_vals_alt, &c->d_sorted, &c->d_M, &c->d_M2, &c->d_Mf, &c->d_Mf2, &c->d_tiles, &c->d_gmap, &c->d_cub, &c->d_wmax,
                     &c->d_ntrans, &c->d_S, &c->d_Sdf, &c->d_Q, &c->d_chi0, &c->d_kk, &c->d_V, &c->d_eps, &c->d_WT,
                     &c->d_flags, &c->d_tmp};
   for (DevBuf* b : bufs) release(*b);
@@ -264,6 +278,7 @@ int rpa_destroy(rpa_ctx* c) {
 const char* rpa_last_error(const rpa_ctx* c) { return c ? c->err.c_str() : g_create_err.c_str(); }
 
 int rpa_set_gvectors(rpa_ctx* c, int ng, const int* miller, const double* G, const double* KC) {
+  if (c) c->gmap_valid = false;
   if (!c || ng <= 0 || !miller || !G || !KC) return fail(c, RPA_EINVAL, "rpa_set_gvectors: bad arguments");
   cudaSetDevice(c->device);
   if (miller[0] != 0 || miller[1] != 0 || miller[2] != 0)
@@ -302,6 +317,7 @@ int rpa_set_gvectors(rpa_ctx* c, int ng, const int* miller, const double* G, con
 }
 
 int rpa_set_symmetry(rpa_ctx* c, int nsym, const double* R, const double* RI) {
+  if (c) c->gmap_valid = false;
   if (!c || nsym < 1 || nsym > 48 || !R || !RI) return fail(c, RPA_EINVAL, "rpa_set_symmetry: bad arguments");
   if (c->ng == 0) return fail(c, RPA_ESTATE, "rpa_set_symmetry: call rpa_set_gvectors first");
   cudaSetDevice(c->device);
@@ -313,6 +329,7 @@ int rpa_set_symmetry(rpa_ctx* c, int nsym, const double* R, const double* RI) {
 
 int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, const int* igk, const double* coeff,
                    const double* E) {
+  if (c) c->gmap_valid = false;
   if (!c || nks <= 0 || nbnd <= 0 || npwx <= 0 || !npw || !coeff || !E)
     return fail(c, RPA_EINVAL, "rpa_load_basis: bad arguments");
   if (c->ng == 0) return fail(c, RPA_ESTATE, "rpa_load_basis: call rpa_set_gvectors first");
@@ -372,6 +389,12 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
     RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
   }
+  if (c->precision == RPA_PREC_MIXED) {
+    RPA_TRY(ensure(c, c->d_coeff32, sizeof(float2) * per_k * nks));
+    k_to_f32<<<2048, 256, 0, c->stream>>>(c->d_coeff.as<double2>(), c->d_coeff32.as<float2>(), per_k * nks);
+    RPA_CUDA(c, cudaGetLastError());
+    ++c->launches;
+  }
   cudaEventRecord(c->ev[7], c->stream);
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
   c->stage_ms[5] = elapsed(c, 6, 7);
@@ -381,6 +404,7 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
 
 int rpa_kmap(rpa_ctx* c, int ntot, const double* ktot, const int* K1, const int* R1, const int* K2, const int* R2,
              const int* iG0) {
+  if (c) c->gmap_valid = false;
   if (!c || ntot <= 0 || !ktot || !K1 || !R1 || !K2 || !R2 || !iG0)
     return fail(c, RPA_EINVAL, "rpa_kmap: bad arguments");
   if (c->nks == 0) return fail(c, RPA_ESTATE, "rpa_kmap: call rpa_load_basis first");
@@ -407,6 +431,7 @@ int rpa_kmap(rpa_ctx* c, int ntot, const double* ktot, const int* K1, const int*
 }
 
 int rpa_set_q(rpa_ctx* c, const double* q, int nlf, const int* ilf, const int* parG) {
+  if (c) c->gmap_valid = false;
   if (!c || !q || nlf <= 0 || !ilf) return fail(c, RPA_EINVAL, "rpa_set_q: bad arguments");
   if (nlf > 1000) return fail(c, RPA_EINVAL, "Nlf = %d exceeds the gjel limit NMAX = 1000", nlf);
   if (c->ng == 0) return fail(c, RPA_ESTATE, "rpa_set_q: call rpa_set_gvectors first");
@@ -547,22 +572,44 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
     cudaEventRecord(c->ev[1], c->stream);
     RPA_TRY(emit_pairs(c, P, k0, nk, off, tot, &wmax, &n_inter, &winsum));
     RPA_TRY(sort_trans(c, (int)tot, P.nw));
-    cudaEventRecord(c->ev[2], c->stream);
-    RPA_TRY(vertices_fp64(c, P, k0, nk, maxp, tot));
-    cudaEventRecord(c->ev[3], c->stream);
     if (c->precision == RPA_PREC_MIXED) {
-      RPA_TRY(ensure(c, c->d_Mf, sizeof(float2) * ((size_t)n_inter + 1) * c->nlf));
-      if (two) RPA_TRY(ensure(c, c->d_Mf2, sizeof(float2) * ((size_t)n_inter + 1) * c->nlf));
+      // FP32 vertices written straight into the window-sorted rows
+      const size_t mrows = ((size_t)tot + 31) / 32 * 32 + 32;
+      RPA_TRY(ensure(c, c->d_Mf, sizeof(float2) * mrows * c->nlf));
+      if (two) RPA_TRY(ensure(c, c->d_Mf2, sizeof(float2) * mrows * c->nlf));
+      RPA_TRY(ensure(c, c->d_counts, sizeof(int) * ((size_t)tot + 1 > (size_t)c->ntot + 1 ? (size_t)tot + 1
+                                                                                            : (size_t)c->ntot + 1)));
       float2* Mf = c->d_Mf.as<float2>();
       float2* Mf2 = two ? c->d_Mf2.as<float2>() : Mf;
-      float amM = 0.f, amM2 = 0.f;
+      const size_t pad0 = (size_t)tot * c->nlf, pad1 = mrows * c->nlf;
+      RPA_CUDA(c, cudaMemsetAsync(Mf + pad0, 0, sizeof(float2) * (pad1 - pad0), c->stream));
+      if (two) RPA_CUDA(c, cudaMemsetAsync(Mf2 + pad0, 0, sizeof(float2) * (pad1 - pad0), c->stream));
+      int* pos_of = c->d_counts.as<int>();
+      RPA_TRY(inverse_perm(c, (int)tot, pos_of));
+      RPA_TRY(ensure(c, c->d_ntrans, 32));
+      RPA_CUDA(c, cudaMemsetAsync(c->d_ntrans.p, 0, 32, c->stream));
+      cudaEventRecord(c->ev[2], c->stream);
+      bool used_tc = false;
+      if (c->vertex_tc) RPA_TRY(vertices_tc(c, P, k0, nk, tot, pos_of, Mf, Mf2, c->d_ntrans.as<unsigned>(), &used_tc));
+      if (!used_tc) RPA_TRY(vertices_f32(c, P, k0, nk, maxp, tot, pos_of, Mf, Mf2, c->d_ntrans.as<unsigned>()));
+      cudaEventRecord(c->ev[3], c->stream);
       double cmax = 0.0;
-      RPA_TRY(pack_sorted_fp32(c, n_inter, Mf, Mf2, two, &amM, &amM2, &cmax));
+      RPA_TRY(cmax_of(c, n_inter, &cmax));
+      unsigned am[2] = {0, 0};
+      RPA_CUDA(c, cudaMemcpy(am, c->d_ntrans.p, 8, cudaMemcpyDeviceToHost));
+      float amM, amM2;
+      std::memcpy(&amM, &am[0], 4);
+      std::memcpy(&amM2, &am[1], 4);
+      if (!two) amM2 = amM;
       RPA_TRY(accumulate_tc(c, P, n_inter, wmax, Mf, Mf2, amM, amM2, cmax));
+      if (cplx) RPA_TRY(qeff_f32(c, n_inter, (int)tot, Mf, Mf2));
     } else {
+      cudaEventRecord(c->ev[2], c->stream);
+      RPA_TRY(vertices_fp64(c, P, k0, nk, maxp, tot));
+      cudaEventRecord(c->ev[3], c->stream);
       RPA_TRY(accumulate_fp64(c, P, n_inter, wmax));
+      if (cplx) RPA_TRY(qeff_fp64(c, P, n_inter, (int)tot));
     }
-    if (cplx) RPA_TRY(qeff_fp64(c, P, n_inter, (int)tot));
     cudaEventRecord(c->ev[4], c->stream);
     RPA_CUDA(c, cudaStreamSynchronize(c->stream));
     t_pairs += elapsed(c, 1, 2);

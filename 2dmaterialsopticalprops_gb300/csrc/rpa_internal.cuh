@@ -42,6 +42,8 @@ struct rpa_ctx {
   int precision = RPA_PREC_FP64;
   int verbose = 0;
   bool split_f16 = true;  // mixed path: fp16 (scaled) or bf16 hi/lo operands
+  int tc_seg = 1;         // mixed path: chunks per TMEM accumulation segment
+  bool vertex_tc = true;  // mixed path: vertices on the tensor cores (else FP32 CUDA cores)
   cudaStream_t stream = nullptr;
   std::string err;
 
@@ -81,7 +83,10 @@ struct rpa_ctx {
 
   // per-call scratch
   rpa::DevBuf d_occ, d_counts, d_offsets, d_trans, d_keys, d_keys_alt, d_vals, d_vals_alt, d_sorted,
-      d_M, d_M2, d_Mf, d_Mf2, d_cub, d_wmax, d_ntrans;
+      d_M, d_M2, d_Mf, d_Mf2, d_tiles, d_gmap, d_cub, d_wmax, d_ntrans;
+  // cached Gfast map (int16) of the last k-chunk, valid until the basis, k map or q change
+  bool gmap_valid = false;
+  int gmap_k0 = 0, gmap_nk = 0, gmap_nsum = 0, gmap_legacy_n = 0;
   // results
   int last_mode = -1, last_no = 0, last_nw = 0;
   double last_domega = 0.0, last_Gcar = 0.0;
@@ -106,10 +111,10 @@ void release(DevBuf& b);
     if (e_ != cudaSuccess) return rpa::cuda_fail(ctx, e_, #call); \
   } while (0)
 
-#define RPA_TRY(x)            \
-  do {                        \
-    int rc_ = (x);            \
-    if (rc_ != RPA_OK) return rc_; \
+#define RPA_TRY(...)                 \
+  do {                               \
+    int rc_ = (__VA_ARGS__);         \
+    if (rc_ != RPA_OK) return rc_;   \
   } while (0)
 
 // ---------------------------------------------------------------------------

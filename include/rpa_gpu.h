@@ -50,7 +50,10 @@ typedef struct rpa_opts {
   int verbose;    /* 0: silent */
   int split;      /* RPA_PREC_MIXED operand split: 0 = fp16 hi/lo with power-of-two
                      scaling (default, ~2^-22 per operand), 1 = bf16 hi/lo (~2^-16) */
-  int reserved[4];
+  int reserved[4]; /* reserved[0]: mixed path, chunks of 32 transitions summed in one
+                      TMEM accumulator before read-back (0 -> 1); keep 0.
+                      reserved[1] = 1: mixed-path vertices on FP32 CUDA cores
+                      instead of the tensor cores */
 } rpa_opts;
 
 /* Arguments of one chi0 accumulation (the namelist values the drivers use).

@@ -371,7 +371,7 @@ def config_small(**kw) -> SynthConfig:
     return SynthConfig(**base)
 
 
-def config_c1(**kw) -> SynthConfig:
+def config_grid24(**kw) -> SynthConfig:
     """24x24 grid, 8 bands (4 occupied), 300 coefficients, NGloc=19, nw=201,
     q = 0.01 2pi/a along Gamma-M, eta = 50 meV."""
     base = dict(nk=24, nbnd=8, nocc=4, npw=300, nlf=19, no=201, omax_ev=30.0, eta_ev=0.05, q_frac=0.01)
@@ -379,7 +379,7 @@ def config_c1(**kw) -> SynthConfig:
     return SynthConfig(**base)
 
 
-def config_c2(**kw) -> SynthConfig:
+def config_grid120(**kw) -> SynthConfig:
     """120x120 grid, 30 bands (8 occupied), 1500 coefficients, NGloc=91,
     nw=1001 on 0-30 eV, eta = 25 meV, q one grid step along Gamma-M."""
     base = dict(nk=120, nbnd=30, nocc=8, npw=1500, nlf=91, no=1001, omax_ev=30.0, eta_ev=0.025, q_steps=1)

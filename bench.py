@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """One q-point of the production-size RPA workload per step.
 
-Workload (default ``--config c2``): 120x120 k-grid (14400 FBZ points, Nsym=1),
+Workload (default ``--config grid120``): 120x120 k-grid (14400 FBZ points, Nsym=1),
 30 bands (8 occupied), ~1500 plane-wave coefficients per band (igk-ordered
 k+G spheres), NGloc = 91 local fields, nw = 1001 frequencies on 0-30 eV,
 eta = 25 meV, q one grid step along Gamma-M.  A step computes, for that q:
@@ -41,10 +41,10 @@ def pkg(name):
 
 def config_of(name: str, q_steps: int):
     synth = pkg("synth")
-    if name == "c2":
-        return synth.config_c2(q_steps=q_steps)
-    if name == "c1":
-        return synth.config_c1()
+    if name == "grid120":
+        return synth.config_grid120(q_steps=q_steps)
+    if name == "grid24":
+        return synth.config_grid24()
     if name == "small":
         return synth.config_small(q_steps=q_steps)
     raise SystemExit(f"unknown config {name}")
@@ -207,7 +207,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2")
+    ap.add_argument("--config", default="grid120")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

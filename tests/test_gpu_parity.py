@@ -96,10 +96,10 @@ def test_edge_sizes(synth, rpa, orc):
         ctx.close()
 
 
-def test_c1_off_grid_q_full(synth, rpa, orc):
+def test_grid24_off_grid_q_full(synth, rpa, orc):
     """The 24x24, 8-band, NGloc=19, nw=201 workload with q = 0.01 2pi/a off the
     grid (shifted k+q basis), every stage."""
-    s = synth.build(synth.config_c1())
+    s = synth.build(synth.config_grid24())
     ctx = rpa.Context()
     ctx.load_system(s)
     b = orc.Bound(s)

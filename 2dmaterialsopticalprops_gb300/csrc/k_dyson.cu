@@ -249,3 +249,83 @@ int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singul
 }
 
 }  // namespace rpa
+
+namespace rpa {
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the Dyson step.
+//
+// Some callers cannot allocate device memory at the point where they need the
+// Dyson solve: code running inside a host framework that owns every device
+// allocation through its own pool, or latency-critical serving code that must
+// not pay for cudaMalloc/cudaFree (an implicit device synchronisation) per
+// request.  For them rpa_dyson_noalloc() runs k_dyson_fp64 with its per-block
+// workspace in the fixed array below instead of a context-owned buffer.
+//
+// Limits: n <= NOALLOC_NMAX local fields; the kernel uses at most
+// NOALLOC_BLOCKS blocks (one frequency per block at a time), so the array
+// holds NOALLOC_BLOCKS * 3 * NOALLOC_NMAX^2 complex doubles = 13.5 MiB, which
+// every GPU that loads this library keeps until the process exits.  All calls
+// share the array: calls that overlap on the GPU (e.g. on two streams) race.
+// The singular/zero-pivot counters at the head of g_noalloc_flags are cleared
+// by every call; the workspace itself needs no clearing (each block writes
+// every entry it reads).
+static constexpr int NOALLOC_NMAX = 96;
+static constexpr int NOALLOC_BLOCKS = 32;
+static __device__ __align__(256) double2 g_noalloc_scratch[(size_t)NOALLOC_BLOCKS * 3 * NOALLOC_NMAX * NOALLOC_NMAX];
+static __device__ __align__(256) int g_noalloc_flags[4];
+
+// Device addresses of the two arrays, looked up once per device with that
+// device current (the host-side names are only stand-ins, not device addresses).
+static void* g_noalloc_scratch_dev[64];
+static void* g_noalloc_flags_dev[64];
+
+static __global__ void k_noalloc_clear_flags() {
+  if (threadIdx.x < 4) g_noalloc_flags[threadIdx.x] = 0;
+}
+
+}  // namespace rpa
+
+extern "C" int rpa_dyson_noalloc(const double* chi0, const double* V, int n, int nwo, double* WT, double* head,
+                                 void* stream, int* n_singular) {
+  using namespace rpa;
+  if (!chi0 || !V || !WT || n < 1 || nwo < 1) return RPA_EINVAL;
+  if (n > NOALLOC_NMAX) return RPA_EINVAL;  // workspace holds matrices up to NOALLOC_NMAX x NOALLOC_NMAX
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return RPA_ECUDA;
+  // One-time set-up on this device: the first call looks up the device
+  // addresses of the workspace; make that first call before any stream capture.
+  if (!g_noalloc_scratch_dev[dev]) {
+    void* ps = nullptr;
+    void* pf = nullptr;
+    if (cudaGetSymbolAddress(&ps, g_noalloc_scratch) != cudaSuccess) return RPA_ECUDA;
+    if (cudaGetSymbolAddress(&pf, g_noalloc_flags) != cudaSuccess) return RPA_ECUDA;
+    g_noalloc_flags_dev[dev] = pf;
+    g_noalloc_scratch_dev[dev] = ps;
+  }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int grid = nwo < NOALLOC_BLOCKS ? nwo : NOALLOC_BLOCKS;
+  DysonArgs D;
+  D.chi0 = reinterpret_cast<const double2*>(chi0);
+  D.V = V;
+  D.WT = reinterpret_cast<double2*>(WT);
+  D.epsinv = nullptr;
+  D.head = reinterpret_cast<double2*>(head);
+  D.scratch = reinterpret_cast<double2*>(g_noalloc_scratch_dev[dev]);
+  D.flags = reinterpret_cast<int*>(g_noalloc_flags_dev[dev]);
+  D.n = n;
+  D.nwo = nwo;
+  const size_t smem = ((3 * (size_t)n * sizeof(int) + 15) & ~(size_t)15) + sizeof(double2) * n;
+  k_noalloc_clear_flags<<<1, 32, 0, s>>>();
+  k_dyson_fp64<<<grid, 256, smem, s>>>(D);
+  if (cudaGetLastError() != cudaSuccess) return RPA_ECUDA;
+  if (n_singular) {
+    int fl[2] = {0, 0};
+    if (cudaMemcpyAsync(fl, D.flags, sizeof fl, cudaMemcpyDeviceToHost, s) != cudaSuccess) return RPA_ECUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return RPA_ECUDA;
+    *n_singular = fl[0];
+    if (fl[0]) return RPA_ESINGULAR;
+  }
+  return RPA_OK;
+}
+

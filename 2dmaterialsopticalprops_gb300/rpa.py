@@ -24,7 +24,7 @@ KK_OPTABS_COMPLEX, KK_SLOSS_REAL = 1, 2
 
 EXPORTS = ["rpa_create", "rpa_destroy", "rpa_last_error", "rpa_set_gvectors", "rpa_set_symmetry",
            "rpa_load_basis", "rpa_kmap", "rpa_set_q", "rpa_chi0", "rpa_kk", "rpa_dyson", "rpa_gfast",
-           "rpa_init_igk", "rpa_kk_matrix", "rpa_stage_times", "rpa_chi0_stats", "rpa_selftest", "rpa_launch_count", "rpa_get_stream", "rpa_synchronize"]
+           "rpa_init_igk", "rpa_kk_matrix", "rpa_stage_times", "rpa_chi0_stats", "rpa_dyson_noalloc", "rpa_selftest", "rpa_launch_count", "rpa_get_stream", "rpa_synchronize"]
 
 
 class RpaOpts(C.Structure):
@@ -74,6 +74,7 @@ def load_library(path: str = LIB_PATH):
     L.rpa_kk_matrix.argtypes = [ip, ip, dp, vp]
     L.rpa_stage_times.argtypes = [vp, vp]
     L.rpa_chi0_stats.argtypes = [vp, vp]
+    L.rpa_dyson_noalloc.argtypes = [vp, vp, ip, ip, vp, vp, vp, C.POINTER(C.c_int)]
     L.rpa_selftest.argtypes = [ip, C.POINTER(C.c_double)]
     L.rpa_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.rpa_get_stream.argtypes = [vp, C.POINTER(vp)]

@@ -167,6 +167,30 @@ int rpa_gfast(rpa_ctx* ctx, int ik, int ngd, int* out);
  * RPA_KK_SLOSS_REAL, j = -no..no for RPA_KK_OPTABS_COMPLEX).  Needs no device. */
 int rpa_kk_matrix(int variant, int no, double domega, double* K);
 
+/* Allocation-free Dyson step.  No counterpart in the reference: it serves
+ * callers that cannot allocate device memory when they need the solve -- code
+ * inside a host framework that owns every device allocation through its own
+ * pool, or latency-critical serving code that cannot afford cudaMalloc/cudaFree
+ * (which synchronise the device) per request.  It runs the same FP64 kernel as
+ * rpa_dyson (eps = I - chi0 V, gjel, chi = eps^-1 chi0, WT = V + V chi V) on
+ * device buffers the caller owns, with its workspace in a fixed 13.5 MiB device
+ * array compiled into the library (held by every GPU that loads it, until the
+ * process exits); it calls no allocating routine.
+ *   chi0 : device, complex chi0 for nwo frequencies, [nwo][n*n], each n x n
+ *          matrix column-major (the layout rpa_kk leaves on the device)
+ *   V    : device, real V(n,n) column-major
+ *   WT   : device, complex [nwo][n*n] output;  head: device, complex [nwo]
+ *          output eps^-1_{11} (may be NULL)
+ *   stream : cudaStream_t (as void*) the kernels are launched on
+ *   n_singular : host; if not NULL the call waits for the stream and returns
+ *          the number of frequencies where gjel would stop (RPA_ESINGULAR)
+ * Limits: n <= 96 (RPA_EINVAL otherwise), any nwo >= 1.  The first call on a
+ * device looks up the workspace's device address with that device current;
+ * make that first call before any stream capture.  Every call shares the one
+ * workspace: calls that overlap on the GPU race.  Uses the current device. */
+int rpa_dyson_noalloc(const double* chi0, const double* V, int n, int nwo, double* WT, double* head,
+                      void* stream, int* n_singular);
+
 /* Timing of the stages of the last rpa_chi0/rpa_kk/rpa_dyson calls (ms, CUDA
  * events on the context stream): [0] pairs+sort, [1] vertices,
  * [2] accumulation, [3] KK, [4] Dyson, [5] host<->device copies. */

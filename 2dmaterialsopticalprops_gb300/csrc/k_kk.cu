@@ -158,6 +158,89 @@ __global__ void __launch_bounds__(256) k_kk_fp64(const double* __restrict__ K, c
   }
 }
 
+// FP32 form for the mixed path: FP32 products summed over BK-wide slices of
+// the kernel, slices carried in double-float (hi + lo FP32), so the long KK
+// sums keep ~2^-40 relative accuracy at FP32 speed.  S is read in FP64.
+__device__ __forceinline__ void kk_df_add(float& hi, float& lo, float v) {
+  float s = hi + v;
+  float bb = s - hi;
+  float e = (hi - (s - bb)) + (v - bb);
+  lo += e;
+  float h = s + lo;
+  lo = lo - (h - s);
+  hi = h;
+}
+
+template <bool CPLX>
+__global__ void __launch_bounds__(256) k_kk_f32(const float* __restrict__ K, const double* __restrict__ S,
+                                                double2* __restrict__ out, int nrow, int nw, int np, int pi_row0) {
+  constexpr int BM = 32, BN = 128, BK = 32;
+  __shared__ float Ks[BK][BM + 1];
+  __shared__ float Ss[BK][BN];
+  const int ncols = CPLX ? 2 * np : np;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads: 4 rows x 4 cols each
+  float hi[4][4], lo[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) hi[i][j] = lo[i][j] = 0.f;
+  for (int k0 = 0; k0 < nw; k0 += BK) {
+    for (int e = threadIdx.x; e < BM * BK; e += 256) {
+      int mm = e / BK, kk = e % BK;
+      int r = m0 + mm, k = k0 + kk;
+      Ks[kk][mm] = (r < nrow && k < nw) ? K[(size_t)r * nw + k] : 0.f;
+    }
+    for (int e = threadIdx.x; e < BK * BN; e += 256) {
+      int kk = e / BN, nn = e % BN;
+      int k = k0 + kk, col = n0 + nn;
+      Ss[kk][nn] = (k < nw && col < ncols) ? (float)S[(size_t)k * ncols + col] : 0.f;
+    }
+    __syncthreads();
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+#pragma unroll 8
+    for (int kk = 0; kk < BK; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = Ks[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Ss[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) kk_df_add(hi[i][j], lo[i][j], acc[i][j]);
+    __syncthreads();
+  }
+  const double pi = 3.141592653589793238462643383279502884;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int r = m0 + ty * 4 + i;
+    if (r >= nrow) continue;
+    const double* srow = S + (size_t)(pi_row0 + r) * ncols;
+#pragma unroll
+    for (int j = 0; j < 4; j += (CPLX ? 2 : 1)) {
+      int col = n0 + tx * 4 + j;
+      if (col >= ncols) continue;
+      if (CPLX) {
+        double re = (double)hi[i][j] + (double)lo[i][j], im = (double)hi[i][j + 1] + (double)lo[i][j + 1];
+        out[(size_t)r * np + (col >> 1)] = make_double2(re + pi * srow[col + 1], im - pi * srow[col]);
+      } else {
+        double re = (double)hi[i][j] + (double)lo[i][j];
+        out[(size_t)r * np + col] = make_double2(re, -pi * srow[col]);
+      }
+    }
+  }
+}
+
 int kk_run(rpa_ctx* c, int variant, int no, double domega) {
   std::vector<double> K;
   int nw = 0;
@@ -171,6 +254,22 @@ int kk_run(rpa_ctx* c, int variant, int no, double domega) {
   dim3 grid((ncols + 63) / 64, (nrow + 31) / 32);
   // S row holding S0(io-1): Sloss row io-1 (io0), Optabs row (io-1)+no
   const int pi_row0 = cplx ? no : 0;
+  if (c->precision == RPA_PREC_MIXED) {
+    std::vector<float> Kf(K.begin(), K.end());
+    RPA_TRY(ensure(c, c->d_kkf, sizeof(float) * Kf.size()));
+    RPA_CUDA(c, cudaMemcpyAsync(c->d_kkf.p, Kf.data(), sizeof(float) * Kf.size(), cudaMemcpyHostToDevice, c->stream));
+    dim3 g2((ncols + 127) / 128, (nrow + 31) / 32);
+    if (cplx)
+      k_kk_f32<true><<<g2, 256, 0, c->stream>>>(c->d_kkf.as<float>(), c->d_S.as<double>(), c->d_chi0.as<double2>(),
+                                                nrow, nw, np, pi_row0);
+    else
+      k_kk_f32<false><<<g2, 256, 0, c->stream>>>(c->d_kkf.as<float>(), c->d_S.as<double>(), c->d_chi0.as<double2>(),
+                                                 nrow, nw, np, pi_row0);
+    RPA_CUDA(c, cudaGetLastError());
+    ++c->launches;
+    RPA_CUDA(c, cudaStreamSynchronize(c->stream));  // the host copy of K goes out of scope
+    return RPA_OK;
+  }
   if (cplx)
     k_kk_fp64<true><<<grid, 256, 0, c->stream>>>(c->d_kk.as<double>(), c->d_S.as<double>(),
                                                  c->d_chi0.as<double2>(), nrow, nw, np, pi_row0);

@@ -91,7 +91,7 @@ struct rpa_ctx {
   int last_mode = -1, last_no = 0, last_nw = 0;
   double last_domega = 0.0, last_Gcar = 0.0;
   bool have_S = false, have_chi0 = false;
-  rpa::DevBuf d_S, d_Sdf, d_Q, d_chi0, d_kk, d_V, d_eps, d_WT, d_flags, d_tmp;
+  rpa::DevBuf d_S, d_Sdf, d_Q, d_chi0, d_kk, d_kkf, d_V, d_eps, d_WT, d_flags, d_tmp;
   double stage_ms[6] = {0, 0, 0, 0, 0, 0};
   long long launches = 0;  // kernels launched by this context
   double stats[4] = {0, 0, 0, 0};

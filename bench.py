@@ -208,8 +208,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="grid120")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison step")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     args = ap.parse_args()
@@ -321,6 +322,37 @@ def main():
         e2e = {"value": world * 1000.0 / ems, "unit": "q-spectra/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": ems}
 
+    # plain FP64 GPU path on the same inputs: its time per q-point and the
+    # mixed path's errors against it (one step, host outputs)
+    fp64 = None
+    if args.precision == "mixed" and not args.no_fp64 and e2e is not None:
+        mixed_out = out
+        ctx.close()
+        ctx64 = rpa.Context(device=local, precision=rpa.PREC_FP64)
+        ctx64.load_system(s)
+        st64 = torch.cuda.ExternalStream(ctx64.stream_handle())
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        f0.record(st64)
+        ref = run_step(ctx64, s, rpa, host={})
+        f1.record(st64)
+        torch.cuda.synchronize()
+        ms64 = f0.elapsed_time(f1)
+        ctx64.close()
+
+        def err(a, b):
+            d = np.abs(a - b)
+            return {"max_rel": float(d.max() / np.abs(b).max()),
+                    "rms_rel": float(np.sqrt(np.mean(d ** 2)) / np.sqrt(np.mean(np.abs(b) ** 2)))}
+        errs = {"S0_xx": err(mixed_out["xx"][0], ref["xx"][0]), "chi0_xx": err(mixed_out["xx"][2], ref["xx"][2]),
+                "S0_zz": err(mixed_out["zz"][0], ref["zz"][0]), "chi0_zz": err(mixed_out["zz"][2], ref["zz"][2]),
+                "S0_loss": err(mixed_out["loss"][0], ref["loss"][0]), "W": err(mixed_out["loss"][2], ref["loss"][2]),
+                "Im_epsinv_00": err(mixed_out["loss"][3].imag, ref["loss"][3].imag)}
+        fp64 = {"ms_per_step": ms64, "value": 1000.0 / ms64, "unit": "q-spectra/s",
+                "mixed_over_fp64": ms64 / ms, "errors_vs_fp64_gpu": errs}
+        ctx = None
+
     # roofline of the dominant stage (accumulation) from the library's CUDA events
     sm = work["stage_ms"]
     acc_s = sm["accumulate"] / 1000.0
@@ -354,13 +386,15 @@ def main():
                      "precision_path": args.precision, "setup_s": round(t_gen, 1)})
         line = {"metric": "q-point chi/W spectra/sec", "value": value, "unit": "q-spectra/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "bf16x3/f32/f64",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f16x3->f32 (vertices, S0), f32 (KK), f64 (Dyson)",
                 "data": "synthetic (seeded QE-layout Bloch basis)", "config": cfgd, "clocks": clocks,
                 "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "stage_ms_per_step": {k: round(v, 3) for k, v in sm.items()},
+                "fp64_gpu": fp64,
                 "vertex_tflops": (work["vertex_flops"] / (sm["vertices"] / 1e3) / 1e12) if sm["vertices"] else None}
         print(json.dumps(line), flush=True)
-    ctx.close()
+    if ctx is not None:
+        ctx.close()
     if dist:
         dist.destroy_process_group()
 

@@ -554,8 +554,17 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
   RPA_TRY(count_pairs(c, P, 0, c->ntot, counts, &maxp));
   // k chunks bounded by the vertex buffer budget
   const bool two = cplx && (a->pol == RPA_POL_YZ || a->pol == RPA_POL_ZY);
-  const size_t per_trans = (size_t)c->nlf * sizeof(double2) * (two ? 2 : 1) + sizeof(Trans) + 16;
-  const size_t budget = (size_t)6 << 30;
+  // per-transition device memory: FP64 vertices (FP64 path) or FP32 vertex rows
+  // plus pre-split tiles (mixed path), records, keys and sort buffers
+  const size_t per_trans =
+      (c->precision == RPA_PREC_MIXED
+           ? (size_t)c->nlf * sizeof(float2) * (two ? 2 : 1) + (cplx ? 4 : 2) * 96 * 128 / 32 *
+                                                                    (size_t)((c->nlf + 95) / 96)
+           : (size_t)c->nlf * sizeof(double2) * (two ? 2 : 1)) +
+      2 * sizeof(Trans) + 24;
+  size_t free_b = 0, total_b = 0;
+  RPA_CUDA(c, cudaMemGetInfo(&free_b, &total_b));
+  const size_t budget = std::max<size_t>((size_t)1 << 30, std::min<size_t>(free_b / 2, (size_t)96 << 30));
   size_t max_trans = std::max<size_t>(budget / per_trans, (size_t)maxp + 1);
   max_trans = std::min<size_t>(max_trans, (size_t)1 << 30);
   int k0 = 0;

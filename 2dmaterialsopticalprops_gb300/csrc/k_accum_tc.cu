@@ -58,7 +58,7 @@ constexpr int TC_TT = 32;       // transitions per chunk (K = 64 16-bit values)
 constexpr int TC_GA = 128;      // G rows per tile (MMA M)
 constexpr int TC_GB = 96;       // G' rows per tile
 constexpr int TC_FLUSH = 32;    // chunks summed in FP32 before a double-float flush
-constexpr uint32_t TC_SPINS = 1u << 22;
+constexpr uint32_t TC_SPINS = 1u << 16;  // suspending polls: about 1.3 s at most
 
 template <bool F16>
 __device__ __forceinline__ void split8(const float* x, uint4& hi, uint4& lo) {

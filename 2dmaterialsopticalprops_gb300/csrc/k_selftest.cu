@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(128) k_umma_selftest(int nchunks, uint32_t see
                      idesc, (c > 0 || ks > 0) ? 1u : 0u);
       tc::mma_commit(&bar);
     }
-    ok = tc::mbar_wait(&bar, c & 1, 1u << 24);
+    ok = tc::mbar_wait(&bar, c & 1, 1u << 16);
     if (!ok) atomicExch(status, 1);
     tc::tc_fence_after();
     __syncthreads();

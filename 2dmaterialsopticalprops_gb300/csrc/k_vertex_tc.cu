@@ -4,19 +4,28 @@
 // Optabs.f90:1354-1472), written per FBZ k-point as a GEMM over the plane
 // waves i of K1:
 //     M_nm(G) = sum_i conj(C1[n,i]) * f(G,i) * C2[m, Gfast(G,i)]
-// rows = (G, m) pairs (4 local fields x 32 bands of K2 per 128-row tile),
-// columns = bands n of K1, K = plane waves.  Complex values are folded into
-// one real GEMM by stacking the K axis (32 plane waves -> 64 K columns):
-//     X((G,m), :) = [ Re y | Im y ],   y = f(G,i) C2[m, Gfast(G,i)]
-//     Y(n, :)     = [ Re c | Im c ]  ->  D((G,m), n)        = Re M
-//     Y(NB+n, :)  = [ -Im c | Re c ] ->  D((G,m), NB + n)   = Im M      (c = C1[n,i])
-// The current factor of Optabs separates, f(G,i) = 0.5 Gcar (q + 2k + Glf_G)_mu
-// + Gcar (R1 G1_i)_mu, so it costs one add per element.  Operands are split
-// into power-of-two-scaled fp16 hi + lo halves (D = Xh Yh + Xh Yl + Xl Yh); each
-// 32-plane-wave chunk accumulates in a fresh TMEM buffer (two, ping-pong) that
-// is added to FP32 registers, as in k_accum_tc.cu.  The Gfast map comes
-// precomputed (k_gmap) as int16 basis positions.  Results go straight to the
-// window-sorted vertex rows pos_of[t] read by the accumulation.
+// rows = (G, m) pairs, 128 / mcount local fields per 128-row tile; columns =
+// bands n of K1; K = plane waves, 32 per chunk, each contributing its (re, im)
+// pair as two adjacent K elements:
+//     X((G,m), i) = ( Re y,  Im y ),   y = C2[m, Gfast(G,i)]
+//     Y(n, i)     = ( Re c,  Im c )  ->  D((G,m), n)      = Re sum conj(c) y
+//     Y(NB+n, i)  = ( -Im c, Re c )  ->  D((G,m), NB + n) = Im sum conj(c) y
+// The current factor of Optabs separates, f(G,i) = a(G) + b(i) with
+// a(G) = 0.5 Gcar (q + 2k + Glf_G)_mu and b(i) = Gcar (R1 G1_i)_mu, so b(i) goes
+// into a second column block of the band operand (c -> b(i) c) and a(G) is
+// applied per row when the accumulator is read:
+//     M = a(G) * D[Y] + D[b Y]
+// The coefficients are stored once, scaled by 2^14, as packed fp16 hi + lo
+// words {re_hi | im_hi << 16, re_lo | im_lo << 16}.  With the (re, im) pair
+// order the gathered operand X is those words unchanged, so cp.async copies
+// them from global memory straight into the 128-byte-swizzled hi and lo tiles
+// through a ring of S shared-memory stages (zero-filled where Gfast has no
+// match); the Re rows of Y arrive the same way.  Threads only form the Im rows
+// and the b(i) rows.  D = Xh Yl + Xl Yh + Xh Yh (small products first); each
+// chunk accumulates in a fresh TMEM buffer (two, ping-pong) that is added to
+// FP32 registers, as in k_accum_tc.cu.  Inside a chunk the K slot s holds plane
+// wave 8 (s % 4) + s / 4, which makes both the gathers (4 plane waves x 8
+// bands per warp instruction) and the shared-memory writes conflict-free.
 
 #include <cuda_fp16.h>
 
@@ -27,7 +36,6 @@
 
 namespace rpa {
 
-struct MapCtx;  // k_vertex.cu
 int build_gmap(rpa_ctx* c, int k0, int nk, int nsum_max, int16_t* gmap, int nsum_legacy);
 
 struct VtxTcCtx {
@@ -38,81 +46,105 @@ struct VtxTcCtx {
   const int* gidx;        // [kibz][npwx]
   const int* npw;
   const double* Glf;      // [nlf][3]
-  const float2* coeff;    // FP32 coefficients [kibz][npwx][nbnd]
+  const uint2* coeffs;    // split fp16 coefficients x 2^14 [kibz][npwx][nbnd]
   const int16_t* gmap;    // [k_local][nlf][nsum_max]
+  const float* btab;      // b(i) sB / 2^14, [k_local][nsum_max] (current vertices)
   const Trans* trans;
   const long long* offsets;
   const int* pos_of;
   float2* M;
-  float2* M2;
   unsigned* amax;
   int* status;
   int k0, nlf, npwx, nbnd, legacy, nsum_legacy, nsum_max;
-  int m0, mcount, n0, ncount;
-  int ca, cb;
+  int m0, mcount, n0, ncount, gpt;
+  int comp;               // Cartesian component of the current vertex
   double q0, q1, q2, Gcar;
-  float sX, sY, inv_scale;
+  float sB;               // scale of the b(i) Y block (X and Y carry the 2^14 of the split coefficients)
+  float out_scale;        // 2^-28 (charge) or 1 / (2^14 sB) (current)
+  float a_scale;          // sB / 2^14: a(G) D[Y] in units of D[b Y]
 };
 
-constexpr int VT_I = 32;      // plane waves per chunk (K = 64)
-constexpr int VT_MB = 32;     // K2 bands per local field in a tile
-constexpr int VT_GPT = 4;     // local fields per 128-row tile
-constexpr uint32_t VT_SPINS = 1u << 22;
+constexpr int VT_I = 32;          // plane waves per chunk (K = 64)
+constexpr int VT_THREADS = 512;   // 16 warps: 4 TMEM lane quadrants x 4 column groups
+constexpr uint32_t VT_SPINS = 1u << 16;  // suspending polls: about 1.3 s at most
+constexpr int VT_SMEM_MAX = 232448 - 4608;  // dynamic shared memory left beside the static tables
 
-__device__ __forceinline__ void st16v(unsigned char* tile, int row, int chunk, uint4 v) {
-  *reinterpret_cast<uint4*>(tile + row * 128 + ((chunk ^ (row & 7)) << 4)) = v;
+template <int NB, bool CURRENT>
+struct VtCfg {
+  static constexpr int NY = CURRENT ? 2 : 1;  // column blocks: c, b c
+  static constexpr int N = NY * 2 * NB;
+  static constexpr uint32_t X_BYTES = 128 * 128, Y_BYTES = N * 128;
+  static constexpr uint32_t B_OFF = 2 * X_BYTES + 2 * Y_BYTES;                 // b(i) of the chunk, 32 floats
+  static constexpr uint32_t STAGE = (B_OFF + (CURRENT ? 128 : 0) + 1023) / 1024 * 1024;
+  static constexpr int S0 = (VT_SMEM_MAX - 1024) / (int)STAGE;
+  static constexpr int S = S0 > 5 ? 5 : S0;                                      // ring depth
+  static constexpr uint32_t NCOL = 2 * N <= 32 ? 32 : 2 * N <= 64 ? 64 : 2 * N <= 128 ? 128 : 256;
+  static constexpr uint32_t BUF = NCOL / 2;  // TMEM column stride of the two buffers
+  static constexpr int CW = NB / 2;          // accumulator columns per thread per block
+  static constexpr size_t SMEM = (size_t)S * STAGE + 1024;
+};
+
+// plane wave (within the chunk) held by K slot s
+__device__ __forceinline__ int vt_pw(int s) { return 8 * (s & 3) + (s >> 2); }
+
+// byte offset of the 4-byte K slot s of row r in a 128-byte-swizzled tile
+__device__ __forceinline__ uint32_t vt_off(int r, int s) {
+  return (uint32_t)r * 128u + ((uint32_t)((s >> 2) ^ (r & 7)) << 4) + (uint32_t)(s & 3) * 4u;
 }
 
-__device__ __forceinline__ void split8h(const float* x, uint4& hi, uint4& lo) {
-  uint32_t h[4], l[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    __half2 hh = __floats2half2_rn(x[2 * i], x[2 * i + 1]);
-    float2 f = __half22float2(hh);
-    __half2 ll = __floats2half2_rn(x[2 * i] - f.x, x[2 * i + 1] - f.y);
-    h[i] = *reinterpret_cast<uint32_t*>(&hh);
-    l[i] = *reinterpret_cast<uint32_t*>(&ll);
-  }
-  hi = make_uint4(h[0], h[1], h[2], h[3]);
-  lo = make_uint4(l[0], l[1], l[2], l[3]);
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory");
 }
 
-// NB: bands n per tile (8, 16 or 32); N = 2 NB.  NACC = 2 for the yz/zy pair.
-template <int NB, bool CURRENT, bool TWO>
-__global__ void __launch_bounds__(256, 2) k_vertex_tc(VtxTcCtx V) {
-  constexpr int N = 2 * NB;
-  constexpr int NACC = TWO ? 2 : 1;
-  constexpr uint32_t X_BYTES = 128 * 128, Y_BYTES = N * 128;
-  constexpr uint32_t STAGE = NACC * 2 * X_BYTES + 2 * Y_BYTES;  // (Xh, Xl) x NACC, Yh, Yl
-  constexpr int DCOLS = NACC * N;                               // TMEM columns per buffer
-  constexpr uint32_t NCOL = 2 * DCOLS <= 32 ? 32 : 2 * DCOLS <= 64 ? 64 : 2 * DCOLS <= 128 ? 128 : 256;
+// (re, im) fp16 pair -> (-im, re), exactly
+__device__ __forceinline__ uint32_t negswap(uint32_t w) { return __byte_perm(w, 0, 0x1032) ^ 0x00008000u; }
+
+__device__ __forceinline__ uint32_t pack_h2(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
+
+template <int CW>
+__device__ __forceinline__ void tmem_ld_cw(uint32_t addr, float* v) {
+  if constexpr (CW == 16) tc::tmem_ld16(addr, v);
+  else if constexpr (CW == 8) tc::tmem_ld8(addr, v);
+  else tc::tmem_ld4(addr, v);
+}
+
+// One CTA per FBZ k-point.  NB: bands n per tile (8, 16 or 32).
+template <int NB, bool CURRENT>
+__global__ void __launch_bounds__(VT_THREADS, 1) k_vertex_tc(VtxTcCtx V) {
+  using Cfg = VtCfg<NB, CURRENT>;
+  constexpr int NY = Cfg::NY, N = Cfg::N, CW = Cfg::CW, S = Cfg::S;
+  constexpr uint32_t STAGE = Cfg::STAGE, X_BYTES = Cfg::X_BYTES, Y_BYTES = Cfg::Y_BYTES;
+  static_assert(S >= 3, "shared-memory ring too shallow");
 
   extern __shared__ unsigned char smraw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+  const uint32_t sbase = tc::smem_u32(base);
   __shared__ uint64_t bar[2];
   __shared__ uint32_t tslot;
-  __shared__ int ptab[32][VT_MB];            // sorted vertex row of (n - n0, m - m0), -1 if none
-  __shared__ float bfac[2][VT_I][2];         // b(i) for the two current components
-  __shared__ float afac[VT_GPT][2];          // a(G)
-
-  auto Xh = [&](int s, int a) { return base + s * STAGE + a * 2 * X_BYTES; };
-  auto Xl = [&](int s, int a) { return base + s * STAGE + a * 2 * X_BYTES + X_BYTES; };
-  auto Yh = [&](int s) { return base + s * STAGE + NACC * 2 * X_BYTES; };
-  auto Yl = [&](int s) { return base + s * STAGE + NACC * 2 * X_BYTES + Y_BYTES; };
+  __shared__ int ptab[32][32];  // sorted vertex row of (n - n0, m - m0), -1 if none
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int kl = blockIdx.x, ik = V.k0 + kl;
   const long long t0 = V.offsets[kl], t1 = V.offsets[kl + 1];
   if (t1 == t0) return;
   const int* km = V.kmap + 5 * ik;
-  const int K1 = km[0], R1 = km[1], K2 = km[2];
+  const int K1 = km[0], K2 = km[2];
   const int nsum = V.legacy ? V.nsum_legacy : V.npw[K1];
   const int nchunk = (nsum + VT_I - 1) / VT_I;
-  const int ngt = (V.nlf + VT_GPT - 1) / VT_GPT;
+  const int GPT = V.gpt, mcount = V.mcount;
+  const int ngt = (V.nlf + GPT - 1) / GPT;
   const int total = ngt * nchunk;
 
   if (warp == 0) {
-    tc::tmem_alloc(&tslot, NCOL);
+    tc::tmem_alloc(&tslot, Cfg::NCOL);
     tc::tmem_relinquish();
   }
   if (tid == 0) {
@@ -120,256 +152,298 @@ __global__ void __launch_bounds__(256, 2) k_vertex_tc(VtxTcCtx V) {
     tc::mbar_init(&bar[1], 1);
     tc::fence_mbar_init();
   }
-  for (int e = tid; e < 32 * VT_MB; e += 256) (&ptab[0][0])[e] = -1;
-  for (uint32_t e = tid; e < 2 * STAGE / 16; e += 256) reinterpret_cast<uint4*>(base)[e] = make_uint4(0, 0, 0, 0);
-  tc::fence_async_smem();
+  for (int e = tid; e < 32 * 32; e += VT_THREADS) (&ptab[0][0])[e] = -1;
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
-  for (long long t = t0 + tid; t < t1; t += 256) {
+  for (long long t = t0 + tid; t < t1; t += VT_THREADS) {
     int nm = V.trans[t].nm;
     int n = (nm & 0xffff) - V.n0, m = (nm >> 16) - V.m0;
-    if (n >= 0 && n < V.ncount && m >= 0 && m < V.mcount) ptab[n][m] = V.pos_of[t];
+    if (n >= 0 && n < V.ncount && m >= 0 && m < mcount) ptab[n][m] = V.pos_of[t];
   }
   const uint32_t taddr = tslot;
   const uint32_t idesc = tc::idesc_bf16(128, N, true);
-  const double* kv = V.ktot + 3 * ik;
-  const float2* C1 = V.coeff + (size_t)K1 * V.npwx * V.nbnd;
-  const float2* C2 = V.coeff + (size_t)K2 * V.npwx * V.nbnd;
   const int16_t* gm = V.gmap + (size_t)kl * V.nlf * V.nsum_max;
+  const float* bt = CURRENT ? V.btab + (size_t)kl * V.nsum_max : nullptr;
 
-  // accumulator slice of this thread: row = TMEM lane, columns half hf
-  const int wq = warp & 3, hf = warp >> 2;
-  const int row_t = wq * 32 + lane;  // (G_local = wq, m = lane)
-  float acc[NACC][NB];
-#pragma unroll
-  for (int a = 0; a < NACC; ++a)
-#pragma unroll
-    for (int j = 0; j < NB; ++j) acc[a][j] = 0.f;
+  // gather task of this thread: X row xr, plane waves 8 xp .. 8 xp + 7 -> K slots xp + 4 j
+  const int xr = 8 * warp + (lane >> 2), xp = lane & 3;
+  const int xgl = xr / mcount, xm = xr - xgl * mcount;
+  const bool xrow = xgl < GPT;
+  const uint2* C2 = V.coeffs + (size_t)K2 * V.npwx * V.nbnd + V.m0 + xm;
+  const uint2* C1 = V.coeffs + (size_t)K1 * V.npwx * V.nbnd + V.n0;
 
+  // band-operand elements of this thread: (n, K slot) pairs e = tid + VT_THREADS j
+  constexpr int YJ = (NB * 32 + VT_THREADS - 1) / VT_THREADS;
+  int yn[YJ], ypw[YJ];
+  uint32_t yoff[YJ], yoffi[YJ];
+#pragma unroll
+  for (int j = 0; j < YJ; ++j) {
+    const int e = tid + VT_THREADS * j, blk = e >> 5, l = e & 31;
+    const int n = 8 * (blk % (NB / 8)) + (l >> 2), sl = 4 * (blk / (NB / 8)) + (l & 3);
+    yn[j] = e < NB * 32 ? n : -1;
+    ypw[j] = vt_pw(sl);
+    yoff[j] = vt_off(n, sl);
+    yoffi[j] = vt_off(NB + n, sl);
+  }
+  uint32_t xoff[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) xoff[j] = vt_off(xr, xp + 4 * j);
+
+  // (local-field tile, chunk) of a running chunk index, advanced without division
+  struct Cur {
+    int gt, c;
+  };
+  auto advance = [&](Cur& u) {
+    if (++u.c == nchunk) u.c = 0, ++u.gt;
+  };
+  auto load_gm = [&](Cur u) -> uint4 {
+    uint4 g = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+    const int G = u.gt * GPT + xgl;
+    if (u.gt < ngt && xrow && G < V.nlf)
+      g = *reinterpret_cast<const uint4*>(gm + (size_t)G * V.nsum_max + u.c * VT_I + xp * 8);
+    return g;
+  };
+  // chunk u -> stage st: X tiles, Re rows of Y, b(i); always one commit group
+  auto issue = [&](Cur u, int stage, uint4 g) {
+    if (u.gt < ngt) {
+      const uint32_t st = sbase + (uint32_t)stage * STAGE;
+      const int i0 = u.c * VT_I;
+      const uint32_t w[4] = {g.x, g.y, g.z, g.w};
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int pos = (int)(int16_t)(uint16_t)(w[j >> 1] >> ((j & 1) * 16));
+        const uint2* src = C2 + (pos >= 0 ? pos : 0) * V.nbnd;
+        const uint32_t sz = pos >= 0 ? 4u : 0u;
+        cp_async4(st + xoff[j], &src->x, sz);
+        cp_async4(st + X_BYTES + xoff[j], &src->y, sz);
+      }
+#pragma unroll
+      for (int j = 0; j < YJ; ++j) {
+        if (yn[j] < 0) continue;
+        const int i = i0 + ypw[j];
+        const bool ok = yn[j] < V.ncount && i < nsum;
+        const uint2* src = C1 + (ok ? i * V.nbnd + yn[j] : 0);
+        cp_async4(st + 2 * X_BYTES + yoff[j], &src->x, ok ? 4u : 0u);
+        cp_async4(st + 2 * X_BYTES + Y_BYTES + yoff[j], &src->y, ok ? 4u : 0u);
+      }
+      if (CURRENT && tid < 8) cp_async16(st + Cfg::B_OFF + 16 * tid, bt + i0 + 4 * tid);
+    }
+    cp_async_commit();
+  };
+  // Im rows of Y (and the b(i) block) of the chunk in a stage, from its Re rows
+  auto form = [&](int stage) {
+    unsigned char* st = base + (size_t)stage * STAGE;
+    unsigned char* yh = st + 2 * X_BYTES;
+    unsigned char* yl = yh + Y_BYTES;
+    const float* bs = reinterpret_cast<const float*>(st + Cfg::B_OFF);
+#pragma unroll
+    for (int j = 0; j < YJ; ++j) {
+      if (yn[j] < 0) continue;
+      const uint32_t wh = *reinterpret_cast<const uint32_t*>(yh + yoff[j]);
+      const uint32_t wl = *reinterpret_cast<const uint32_t*>(yl + yoff[j]);
+      *reinterpret_cast<uint32_t*>(yh + yoffi[j]) = negswap(wh);
+      *reinterpret_cast<uint32_t*>(yl + yoffi[j]) = negswap(wl);
+      if (CURRENT) {
+        const float b = bs[ypw[j]];
+        const float2 h = __half22float2(*reinterpret_cast<const __half2*>(&wh));
+        const float2 lo = __half22float2(*reinterpret_cast<const __half2*>(&wl));
+        const float re = (h.x + lo.x) * b, im = (h.y + lo.y) * b;
+        const __half2 hh = __floats2half2_rn(re, im);
+        const float2 hf = __half22float2(hh);
+        const __half2 ll = __floats2half2_rn(re - hf.x, im - hf.y);
+        const uint32_t bh = pack_h2(hh), bl = pack_h2(ll);
+        const uint32_t ob = yoff[j] + 2 * NB * 128, obi = yoffi[j] + 2 * NB * 128;
+        *reinterpret_cast<uint32_t*>(yh + ob) = bh;
+        *reinterpret_cast<uint32_t*>(yl + ob) = bl;
+        *reinterpret_cast<uint32_t*>(yh + obi) = negswap(bh);
+        *reinterpret_cast<uint32_t*>(yl + obi) = negswap(bl);
+      }
+    }
+  };
+
+  // accumulator slice of this thread: TMEM lane quadrant wq, column group cg
+  const int wq = warp & 3, cg = warp >> 2;
+  const int row_t = wq * 32 + lane;
+  const int egl = row_t / mcount, em = row_t - egl * mcount;
+  float acc[CW];
+#pragma unroll
+  for (int j = 0; j < CW; ++j) acc[j] = 0.f;
+  float fa = 0.f;
+  auto set_afac = [&](int gt) {
+    const int G = gt * GPT + egl;
+    fa = 0.f;
+    if (CURRENT && egl < GPT && G < V.nlf) {
+      const double* kv = V.ktot + 3 * ik;
+      const double* gl = V.Glf + 3 * G;
+      const int mu = V.comp;
+      const double qmu = mu == 0 ? V.q0 : (mu == 1 ? V.q1 : V.q2);
+      fa = (float)(0.5 * V.Gcar * (qmu + 2.0 * kv[mu] + gl[mu])) * V.a_scale;
+    }
+  };
   auto consume = [&](int buf) {
+    const uint32_t ad = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)(buf * Cfg::BUF + cg * CW);
+    float v[NY][CW];
 #pragma unroll
-    for (int a = 0; a < NACC; ++a) {
-      const uint32_t ad = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)(buf * DCOLS + a * N + hf * NB);
-      float v[NB];
-      if (NB == 32) tc::tmem_ld32(ad, v);
-      else if (NB == 16) tc::tmem_ld16(ad, v);
-      else tc::tmem_ld8(ad, v);
-      tc::tmem_ld_wait();
+    for (int b = 0; b < NY; ++b) tmem_ld_cw<CW>(ad + b * 2 * NB, v[b]);
+    tc::tmem_ld_wait();
 #pragma unroll
-      for (int j = 0; j < NB; ++j) acc[a][j] += v[j];
+    for (int j = 0; j < CW; ++j) {
+      if (CURRENT) acc[j] += fmaf(fa, v[0][j], v[NY - 1][j]);
+      else acc[j] += v[0][j];
     }
   };
-  float amx[NACC];
-#pragma unroll
-  for (int a = 0; a < NACC; ++a) amx[a] = 0.f;
+  float amx = 0.f;
   auto write_out = [&](int gt) {
-    const int G = gt * VT_GPT + wq;
-    const int m = lane;
-    if (G < V.nlf && m < V.mcount) {
+    const int G = gt * GPT + egl;
+    if (egl < GPT && G < V.nlf) {
+      const int part = cg >> 1;
 #pragma unroll
-      for (int j = 0; j < NB; ++j) {
-        int r = j < V.ncount ? ptab[j][m] : -1;
+      for (int j = 0; j < CW; ++j) {
+        const int n = (cg & 1) * CW + j;
+        const int r = n < V.ncount ? ptab[n][em] : -1;
         if (r >= 0) {
-#pragma unroll
-          for (int a = 0; a < NACC; ++a) {
-            float v = acc[a][j] * V.inv_scale;
-            float* dst = reinterpret_cast<float*>((a == 0 ? V.M : V.M2) + (size_t)r * V.nlf + G) + hf;
-            *dst = v;
-            amx[a] = fmaxf(amx[a], fabsf(v));
-          }
+          const float v = acc[j] * V.out_scale;
+          reinterpret_cast<float*>(V.M + (size_t)r * V.nlf + G)[part] = v;
+          amx = fmaxf(amx, fabsf(v));
         }
       }
     }
 #pragma unroll
-    for (int a = 0; a < NACC; ++a)
-#pragma unroll
-      for (int j = 0; j < NB; ++j) acc[a][j] = 0.f;
+    for (int j = 0; j < CW; ++j) acc[j] = 0.f;
   };
 
-  bool abort = false;
-  for (int q = 0; q < total && !abort; ++q) {
-    const int s = q & 1;
-    const int gt = q / nchunk, c = q % nchunk, i0 = c * VT_I;
-    // per-chunk factors: b(i) (current vertices) and a(G)
-    if (CURRENT) {
-      if (tid < VT_I) {
-        int i = i0 + tid;
-        float b0 = 0.f, b1 = 0.f;
-        if (i < nsum) {
-          const double* g1 = V.G + 3 * V.gidx[(size_t)K1 * V.npwx + i];
-          const double* R = V.Rcart + 9 * R1;
-          double k3[3] = {R[0] * g1[0] + R[1] * g1[1] + R[2] * g1[2], R[3] * g1[0] + R[4] * g1[1] + R[5] * g1[2],
-                          R[6] * g1[0] + R[7] * g1[1] + R[8] * g1[2]};
-          b0 = (float)(V.Gcar * k3[V.ca]);
-          b1 = (float)(V.Gcar * k3[V.cb]);
-        }
-        bfac[s][tid][0] = b0;
-        bfac[s][tid][1] = b1;
-      } else if (tid < VT_I + VT_GPT && c == 0) {
-        int G = gt * VT_GPT + (tid - VT_I);
-        float a0 = 0.f, a1 = 0.f;
-        if (G < V.nlf) {
-          const double* gl = V.Glf + 3 * G;
-          double j3[3] = {V.q0 + 2.0 * kv[0] + gl[0], V.q1 + 2.0 * kv[1] + gl[1], V.q2 + 2.0 * kv[2] + gl[2]};
-          a0 = (float)(0.5 * V.Gcar * j3[V.ca]);
-          a1 = (float)(0.5 * V.Gcar * j3[V.cb]);
-        }
-        afac[tid - VT_I][0] = a0;
-        afac[tid - VT_I][1] = a1;
-      }
-      __syncthreads();
-    }
-    // X tiles: row = (G_local, m), 8 plane waves per task
-    for (int e = tid; e < 128 * 4; e += 256) {
-      const int row = e & 127, grp = e >> 7;
-      const int gl = row >> 5, m = row & 31, G = gt * VT_GPT + gl;
-      float xr[NACC][8], xi[NACC][8];
-      if (G < V.nlf && m < V.mcount) {
-        const int ib = i0 + grp * 8;
-        int16_t pos[8];
-        *reinterpret_cast<uint4*>(pos) = *reinterpret_cast<const uint4*>(gm + (size_t)G * V.nsum_max + ib);
-#pragma unroll
-        for (int qq = 0; qq < 8; ++qq) {
-          float2 v = make_float2(0.f, 0.f);
-          if (ib + qq < nsum && pos[qq] >= 0) v = C2[(size_t)pos[qq] * V.nbnd + V.m0 + m];
-          if (CURRENT) {
-            float f0 = (afac[gl][0] + bfac[s][grp * 8 + qq][0]) * V.sX;
-            xr[0][qq] = v.x * f0;
-            xi[0][qq] = v.y * f0;
-            if (TWO) {
-              float f1 = (afac[gl][1] + bfac[s][grp * 8 + qq][1]) * V.sX;
-              xr[NACC - 1][qq] = v.x * f1;
-              xi[NACC - 1][qq] = v.y * f1;
-            }
-          } else {
-            xr[0][qq] = v.x * V.sX;
-            xi[0][qq] = v.y * V.sX;
-          }
-        }
-      } else {
-#pragma unroll
-        for (int a = 0; a < NACC; ++a)
-#pragma unroll
-          for (int qq = 0; qq < 8; ++qq) xr[a][qq] = xi[a][qq] = 0.f;
-      }
-#pragma unroll
-      for (int a = 0; a < NACC; ++a) {
-        uint4 hi, lo;
-        split8h(xr[a], hi, lo);
-        st16v(Xh(s, a), row, grp, hi);
-        st16v(Xl(s, a), row, grp, lo);
-        split8h(xi[a], hi, lo);
-        st16v(Xh(s, a), row, 4 + grp, hi);
-        st16v(Xl(s, a), row, 4 + grp, lo);
-      }
-    }
-    // Y tiles: rows n (Re part) and NB + n (Im part)
-    for (int e = tid; e < NB * 4; e += 256) {
-      const int n = e % NB, grp = e / NB;
-      float cr[8], ci[8], nci[8];
-#pragma unroll
-      for (int qq = 0; qq < 8; ++qq) {
-        int i = i0 + grp * 8 + qq;
-        float2 v = (n < V.ncount && i < nsum) ? C1[(size_t)i * V.nbnd + V.n0 + n] : make_float2(0.f, 0.f);
-        cr[qq] = v.x * V.sY;
-        ci[qq] = v.y * V.sY;
-        nci[qq] = -ci[qq];
-      }
-      uint4 hi, lo;
-      split8h(cr, hi, lo);
-      st16v(Yh(s), n, grp, hi);
-      st16v(Yl(s), n, grp, lo);
-      st16v(Yh(s), NB + n, 4 + grp, hi);
-      st16v(Yl(s), NB + n, 4 + grp, lo);
-      split8h(ci, hi, lo);
-      st16v(Yh(s), n, 4 + grp, hi);
-      st16v(Yl(s), n, 4 + grp, lo);
-      split8h(nci, hi, lo);
-      st16v(Yh(s), NB + n, grp, hi);
-      st16v(Yl(s), NB + n, grp, lo);
-    }
-    tc::fence_async_smem();
+  // prologue: chunks 0 .. S-2 in flight, positions of S-1 and S in registers
+  Cur ui = {0, 0};  // next chunk to issue
+  for (int j = 0; j < S - 1; ++j) {
+    issue(ui, j, load_gm(ui));
+    advance(ui);
+  }
+  Cur ug = ui;  // positions in registers: ui (pgA), ui + 1 (pgB)
+  uint4 pgA = load_gm(ug);
+  advance(ug);
+  uint4 pgB = load_gm(ug);
+  advance(ug);
+  set_afac(0);
+
+  bool abort = false, fail = false;
+  int sq = 0, si = S - 1;  // stage of chunk q, stage of the next chunk to issue
+  Cur uq = {0, 0};         // chunk q
+  for (int q = 0; q < total; ++q) {
+    cp_async_wait<S - 2>();  // this thread's copies of chunk q landed
     __syncthreads();
+    form(sq);
+    tc::fence_async_smem();
+    tc::tc_fence_before();
+    abort = __syncthreads_or(fail);
+    if (abort) break;
     if (tid == 0) {
       tc::tc_fence_after();
-      const uint32_t yh = tc::smem_u32(Yh(s)), yl = tc::smem_u32(Yl(s));
+      const uint32_t xh = sbase + (uint32_t)sq * STAGE, xl = xh + X_BYTES;
+      const uint32_t yh = xh + 2 * X_BYTES, yl = yh + Y_BYTES;
+      const uint32_t d = taddr + (uint32_t)((q & 1) * Cfg::BUF);
 #pragma unroll
-      for (int a = 0; a < NACC; ++a) {
-        const uint32_t xh = tc::smem_u32(Xh(s, a)), xl = tc::smem_u32(Xl(s, a));
-        const uint32_t d = taddr + (uint32_t)(s * DCOLS + a * N);
-#pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-          const uint32_t ko = ks * 32;
-          tc::mma_bf16(d, tc::desc_sw128(xh + ko), tc::desc_sw128(yl + ko), idesc, ks > 0 ? 1u : 0u);
-          tc::mma_bf16(d, tc::desc_sw128(xl + ko), tc::desc_sw128(yh + ko), idesc, 1u);
-        }
-#pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-          const uint32_t ko = ks * 32;
-          tc::mma_bf16(d, tc::desc_sw128(xh + ko), tc::desc_sw128(yh + ko), idesc, 1u);
-        }
+      for (int ks = 0; ks < 4; ++ks) {
+        const uint32_t ko = ks * 32;
+        tc::mma_bf16(d, tc::desc_sw128(xh + ko), tc::desc_sw128(yl + ko), idesc, ks > 0 ? 1u : 0u);
+        tc::mma_bf16(d, tc::desc_sw128(xl + ko), tc::desc_sw128(yh + ko), idesc, 1u);
       }
-      tc::mma_commit(&bar[s]);
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks) {
+        const uint32_t ko = ks * 32;
+        tc::mma_bf16(d, tc::desc_sw128(xh + ko), tc::desc_sw128(yh + ko), idesc, 1u);
+      }
+      tc::mma_commit(&bar[q & 1]);
     }
-    // read back the previous chunk while this one runs
+    // read back the previous chunk while this one runs, then refill its stage
     if (q >= 1) {
       const int qp = q - 1;
-      bool ok = tc::mbar_wait(&bar[s ^ 1], (qp >> 1) & 1, VT_SPINS);
-      if (!ok) atomicExch(V.status, 1);
-      abort = __syncthreads_or(!ok);
-      if (abort) break;
+      if (!tc::mbar_wait(&bar[qp & 1], (qp >> 1) & 1, VT_SPINS)) {
+        atomicExch(V.status, 1);
+        fail = true;
+      }
       tc::tc_fence_after();
-      consume(s ^ 1);
-      tc::tc_fence_before();
-      if (qp % nchunk == nchunk - 1) write_out(qp / nchunk);
+      consume(qp & 1);
+      if (uq.c == 0) {  // qp closed its local-field tile
+        write_out(uq.gt - 1);
+        set_afac(uq.gt);
+      }
     }
-    __syncthreads();
+    if (!fail) issue(ui, si, pgA);
+    else cp_async_commit();
+    advance(ui);
+    si = si + 1 == S ? 0 : si + 1;
+    sq = sq + 1 == S ? 0 : sq + 1;
+    advance(uq);
+    pgA = pgB;
+    pgB = load_gm(ug);
+    advance(ug);
   }
-  if (!abort && total > 0) {
+  cp_async_wait<0>();
+  if (!abort) {
     const int ql = total - 1;
-    bool ok = tc::mbar_wait(&bar[ql & 1], (ql >> 1) & 1, VT_SPINS);
-    if (!ok) atomicExch(V.status, 1);
-    abort = __syncthreads_or(!ok);
-    if (!abort) {
-      tc::tc_fence_after();
-      consume(ql & 1);
-      tc::tc_fence_before();
-      write_out(ql / nchunk);
+    if (!tc::mbar_wait(&bar[ql & 1], (ql >> 1) & 1, VT_SPINS)) {
+      atomicExch(V.status, 1);
+      fail = true;
     }
-  } else if (abort && tid == 0 && total > 0) {
+    tc::tc_fence_after();
+    consume(ql & 1);
+    write_out(ngt - 1);
+  }
+  abort = __syncthreads_or(fail || abort);
+  if (abort && tid == 0) {
     for (int b = 0; b < 2; ++b) tc::mbar_wait(&bar[b], 0, 1024), tc::mbar_wait(&bar[b], 1, 1024);
   }
   // vertex magnitude for the accumulation's operand scaling
-#pragma unroll
-  for (int a = 0; a < NACC; ++a) {
-    float mx = amx[a];
-    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if (lane == 0) atomicMax(V.amax + a, __float_as_uint(mx));
-  }
+  for (int o = 16; o > 0; o >>= 1) amx = fmaxf(amx, __shfl_xor_sync(0xffffffffu, amx, o));
+  if (lane == 0) atomicMax(V.amax, __float_as_uint(amx));
   tc::tc_fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
+  if (warp == 0) tc::tmem_dealloc(taddr, Cfg::NCOL);
+}
+
+// b(i) = Gcar (R1 G1_i)_mu of every FBZ k-point of the launch, pre-scaled by
+// sB / 2^14; zero beyond nsum.
+__global__ void k_vtx_btab(VtxTcCtx V, int nk, float* __restrict__ out) {
+  const size_t n = (size_t)nk * V.nsum_max;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int kl = (int)(e / V.nsum_max), i = (int)(e % V.nsum_max);
+    const int* km = V.kmap + 5 * (V.k0 + kl);
+    const int K1 = km[0];
+    const int nsum = V.legacy ? V.nsum_legacy : V.npw[K1];
+    float b = 0.f;
+    if (i < nsum) {
+      const double* R = V.Rcart + 9 * km[1] + 3 * V.comp;
+      const double* g1 = V.G + 3 * V.gidx[(size_t)K1 * V.npwx + i];
+      b = (float)(V.Gcar * (R[0] * g1[0] + R[1] * g1[1] + R[2] * g1[2])) * V.sB * (1.0f / 16384.0f);
+    }
+    out[e] = b;
+  }
 }
 
 static double pow2_floor_v(double x) { return std::ldexp(1.0, (int)std::floor(std::log2(x))); }
 
-template <int NB, bool CURRENT, bool TWO>
+template <int NB, bool CURRENT>
 static int launch_vtc(rpa_ctx* c, const VtxTcCtx& V, int nk) {
-  constexpr int NACC = TWO ? 2 : 1;
-  constexpr size_t STAGE = (size_t)NACC * 2 * 128 * 128 + 2 * (size_t)(2 * NB) * 128;
-  const size_t smem = 2 * STAGE + 1024;
-  auto kern = k_vertex_tc<NB, CURRENT, TWO>;
-  RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<nk, 256, smem, c->stream>>>(V);
+  using Cfg = VtCfg<NB, CURRENT>;
+  auto kern = k_vertex_tc<NB, CURRENT>;
+  RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM));
+  kern<<<nk, VT_THREADS, Cfg::SMEM, c->stream>>>(V);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
   return RPA_OK;
 }
 
+template <bool CURRENT>
+static int launch_vtc_nb(rpa_ctx* c, const VtxTcCtx& V, int nk, int NB) {
+  if (NB == 8) return launch_vtc<8, CURRENT>(c, V, nk);
+  if (NB == 16) return launch_vtc<16, CURRENT>(c, V, nk);
+  return launch_vtc<32, CURRENT>(c, V, nk);
+}
+
 // Mixed-path vertices of the FBZ k-points [k0, k0+nk) on the tensor cores.
-// Returns RPA_EINVAL when the band windows do not fit one tile (the caller
-// then uses the CUDA-core kernel).
+// Leaves *used false when the band windows or the plane-wave count do not fit
+// the tiles (the caller then uses the CUDA-core kernel).
 int vertices_tc(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans, const int* pos_of, float2* Mf,
                 float2* Mf2, unsigned* amax, bool* used) {
   *used = false;
@@ -382,8 +456,8 @@ int vertices_tc(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
   } else {
     m0 = P.nocc, mcount = c->nbnd - P.nocc, n0 = 0, ncount = P.nocc;
   }
-  if (mcount > VT_MB || ncount > 32 || c->npwx > 32767) return RPA_OK;
-  int NB = ncount <= 8 ? 8 : (ncount <= 16 ? 16 : 32);
+  if (mcount < 1 || mcount > 32 || ncount > 32 || c->npwx > 32767) return RPA_OK;
+  const int NB = ncount <= 8 ? 8 : (ncount <= 16 ? 16 : 32);
   // Gfast map of the chunk (int16 positions), shared by the chains of one q-point
   int nsum_max = 0;
   for (int i = 0; i < nk; ++i) {
@@ -410,14 +484,12 @@ int vertices_tc(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
   V.gidx = c->d_gidx.as<int>();
   V.npw = c->d_npw.as<int>();
   V.Glf = c->d_Glf.as<double>();
-  V.coeff = c->d_coeff32.as<float2>();
+  V.coeffs = c->d_coeffs.as<uint2>();
   V.gmap = c->d_gmap.as<int16_t>();
+  V.btab = nullptr;
   V.trans = c->d_trans.as<Trans>();
   V.offsets = c->d_offsets.as<long long>();
   V.pos_of = pos_of;
-  V.M = Mf;
-  V.M2 = Mf2;
-  V.amax = amax;
   V.status = c->d_flags.as<int>() + 3;
   V.k0 = k0;
   V.nlf = c->nlf;
@@ -427,53 +499,53 @@ int vertices_tc(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
   V.nsum_legacy = P.nsum_legacy;
   V.nsum_max = nsum_max;
   V.m0 = m0, V.mcount = mcount, V.n0 = n0, V.ncount = ncount;
-  int ca = 0, cb = 0;
-  switch (P.pol) {
-    case RPA_POL_XX: ca = cb = 0; break;
-    case RPA_POL_YY: ca = cb = 1; break;
-    case RPA_POL_ZZ: ca = cb = 2; break;
-    case RPA_POL_YZ: ca = 1; cb = 2; break;
-    default: ca = 2; cb = 1; break;
-  }
-  V.ca = ca;
-  V.cb = cb;
+  V.gpt = 128 / mcount;
   V.q0 = c->q[0];
   V.q1 = c->q[1];
   V.q2 = c->q[2];
   V.Gcar = P.Gcar;
-  // operand scaling: |C| <= 1 (orthonormal bands); |f| bounded by the G vectors in play
-  double fmax = 1.0;
-  if (current) {
-    double gmax = 0.0;
-    for (size_t g = 0; g < c->h_G.size() / 3; ++g) {
-      const double* v = &c->h_G[3 * g];
-      gmax = std::max(gmax, std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
-    }
-    double kq = 0.0;
-    for (int i = 0; i < c->ntot; ++i) {
-      const double* k = &c->h_ktot[3 * (size_t)i];
-      kq = std::max(kq, std::sqrt(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]));
-    }
-    double qn = std::sqrt(c->q[0] * c->q[0] + c->q[1] * c->q[1] + c->q[2] * c->q[2]);
-    fmax = P.Gcar * (0.5 * (qn + 2.0 * kq + gmax) + gmax);
-  }
-  V.sX = (float)(16384.0 / pow2_floor_v(fmax * 1.5));
-  V.sY = 16384.0f;
-  V.inv_scale = (float)(1.0 / ((double)V.sX * (double)V.sY));
-  *used = true;
   if (!current) {
-    if (NB == 8) return launch_vtc<8, false, false>(c, V, nk);
-    if (NB == 16) return launch_vtc<16, false, false>(c, V, nk);
-    return launch_vtc<32, false, false>(c, V, nk);
+    V.comp = 0;
+    V.sB = 1.0f;
+    V.a_scale = 0.0f;
+    V.out_scale = (float)(1.0 / (16384.0 * 16384.0));
+    V.M = Mf;
+    V.amax = amax;
+    *used = true;
+    return launch_vtc_nb<false>(c, V, nk, NB);
   }
-  if (two) {
-    if (NB == 8) return launch_vtc<8, true, true>(c, V, nk);
-    if (NB == 16) return launch_vtc<16, true, true>(c, V, nk);
-    return launch_vtc<32, true, true>(c, V, nk);
+  // current vertices: |C| <= 1 (orthonormal bands), |b(i)| <= Gcar max|G|
+  double gmax = 0.0;
+  for (size_t g = 0; g < c->h_G.size() / 3; ++g) {
+    const double* v = &c->h_G[3 * g];
+    gmax = std::max(gmax, std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
   }
-  if (NB == 8) return launch_vtc<8, true, false>(c, V, nk);
-  if (NB == 16) return launch_vtc<16, true, false>(c, V, nk);
-  return launch_vtc<32, true, false>(c, V, nk);
+  const double bmax = std::max(P.Gcar * gmax, 1e-30);
+  V.sB = (float)(16384.0 / pow2_floor_v(bmax * 1.5));
+  V.a_scale = V.sB / 16384.0f;
+  V.out_scale = (float)(1.0 / (16384.0 * (double)V.sB));
+  int comps[2];
+  switch (P.pol) {
+    case RPA_POL_XX: comps[0] = comps[1] = 0; break;
+    case RPA_POL_YY: comps[0] = comps[1] = 1; break;
+    case RPA_POL_ZZ: comps[0] = comps[1] = 2; break;
+    case RPA_POL_YZ: comps[0] = 1; comps[1] = 2; break;
+    default: comps[0] = 2; comps[1] = 1; break;
+  }
+  RPA_TRY(ensure(c, c->d_vbt, sizeof(float) * (size_t)nk * nsum_max));
+  V.btab = c->d_vbt.as<float>();
+  // the yz / zy pair: one pass per Cartesian component
+  for (int a = 0; a < (two ? 2 : 1); ++a) {
+    V.comp = comps[a];
+    V.M = a == 0 ? Mf : Mf2;
+    V.amax = amax + a;
+    k_vtx_btab<<<2048, 256, 0, c->stream>>>(V, nk, c->d_vbt.as<float>());
+    RPA_CUDA(c, cudaGetLastError());
+    ++c->launches;
+    RPA_TRY(launch_vtc_nb<true>(c, V, nk, NB));
+  }
+  *used = true;
+  return RPA_OK;
 }
 
 }  // namespace rpa

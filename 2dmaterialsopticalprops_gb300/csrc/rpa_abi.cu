@@ -10,6 +10,8 @@
 #include <cstdarg>
 #include <cstring>
 
+#include <cuda_fp16.h>
+
 #include "rpa_internal.cuh"
 
 namespace rpa {
@@ -98,6 +100,20 @@ __global__ void k_to_f32(const double2* __restrict__ src, float2* __restrict__ d
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     double2 v = src[e];
     dst[e] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+// Coefficients scaled by 2^14 and split into fp16 hi + lo halves, packed per
+// element as {re_hi | im_hi << 16, re_lo | im_lo << 16}: the tensor-core
+// vertex kernel moves these words into its operand tiles without arithmetic.
+__global__ void k_to_split16(const double2* __restrict__ src, uint2* __restrict__ dst, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    double2 v = src[e];
+    float re = (float)v.x * 16384.0f, im = (float)v.y * 16384.0f;
+    __half2 hi = __floats2half2_rn(re, im);
+    float2 h = __half22float2(hi);
+    __half2 lo = __floats2half2_rn(re - h.x, im - h.y);
+    dst[e] = make_uint2(*reinterpret_cast<uint32_t*>(&hi), *reinterpret_cast<uint32_t*>(&lo));
   }
 }
 
@@ -262,9 +278,9 @@ int rpa_destroy(rpa_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   DevBuf* bufs[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
-                    &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_E, &c->d_kmap, &c->d_ktot, &c->d_lf_miller,
+                    &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_coeffs, &c->d_E, &c->d_kmap, &c->d_ktot, &c->d_lf_miller,
                     &c->d_Glf, &c->d_occ, &c->d_counts, &c->d_offsets, &c->d_trans, &c->d_keys, &c->d_keys_alt,
-                    &c->d_vals, &c->d_vals_alt, &c->d_sorted, &c->d_M, &c->d_M2, &c->d_Mf, &c->d_Mf2, &c->d_tiles, &c->d_gmap, &c->d_cub, &c->d_wmax,
+                    &c->d_vals, &c->d_vals_alt, &c->d_sorted, &c->d_M, &c->d_M2, &c->d_Mf, &c->d_Mf2, &c->d_tiles, &c->d_gmap, &c->d_vbt, &c->d_cub, &c->d_wmax,
                     &c->d_ntrans, &c->d_S, &c->d_Sdf, &c->d_Q, &c->d_chi0, &c->d_kk, &c->d_kkf, &c->d_V, &c->d_eps, &c->d_WT,
                     &c->d_flags, &c->d_tmp};
   for (DevBuf* b : bufs) release(*b);
@@ -392,6 +408,10 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
   if (c->precision == RPA_PREC_MIXED) {
     RPA_TRY(ensure(c, c->d_coeff32, sizeof(float2) * per_k * nks));
     k_to_f32<<<2048, 256, 0, c->stream>>>(c->d_coeff.as<double2>(), c->d_coeff32.as<float2>(), per_k * nks);
+    RPA_CUDA(c, cudaGetLastError());
+    ++c->launches;
+    RPA_TRY(ensure(c, c->d_coeffs, sizeof(uint2) * per_k * nks));
+    k_to_split16<<<2048, 256, 0, c->stream>>>(c->d_coeff.as<double2>(), c->d_coeffs.as<uint2>(), per_k * nks);
     RPA_CUDA(c, cudaGetLastError());
     ++c->launches;
   }

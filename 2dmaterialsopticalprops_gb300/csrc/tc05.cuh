@@ -3,7 +3,7 @@
 // mbarriers and bulk async copies), sm_100a family.
 //
 // Every wait on an mbarrier is bounded: mbar_wait() gives up after
-// `spins` polls and returns false, and the callers turn that into an error
+// `polls` suspending polls and returns false, and the callers turn that into an error
 // status instead of hanging.
 #pragma once
 #include <cuda_bf16.h>
@@ -38,10 +38,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Polls until the phase with the given parity completed, at most `spins` times.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t spins) {
-  for (uint32_t i = 0; i < spins; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
+// One poll that suspends the thread until the phase completes or about `ns`
+// nanoseconds pass, so waiting warps neither issue instructions nor load the
+// shared-memory pipe the tensor core reads its operands through.
+__device__ __forceinline__ bool mbar_try_wait_ns(uint64_t* bar, uint32_t parity, uint32_t ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits until the phase with the given parity completed, at most `polls`
+// suspending polls of up to 20 us each; false when it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t polls) {
+  for (uint32_t i = 0; i < polls; ++i)
+    if (mbar_try_wait_ns(bar, parity, 20000u)) return true;
   return false;
 }
 
@@ -93,7 +109,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 #pragma unroll
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
-// 8 / 16 consecutive fp32 columns of this warp's 32 TMEM lanes.
+// 4 / 8 / 16 consecutive fp32 columns of this warp's 32 TMEM lanes.
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr)
+               : "memory");
+#pragma unroll
+  for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
+}
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
   uint32_t r[8];
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"

@@ -50,6 +50,7 @@ struct AccTcCtx {
   double scaleA;        // power of two folded into w
   float scaleB;         // power of two folded into M2
   float inv_scale;      // 1 / (scaleA scaleB)
+  float inv_src;        // 1 / (scale of the pre-split A-side tile)
   int n_rows;           // rows of M / M2 (n_inter rounded up to a multiple of 32, zero padded)
   int seg;              // chunks accumulated in one TMEM segment before it is read back
 };
@@ -292,9 +293,13 @@ __global__ void __launch_bounds__(256, 1) k_accum_tc(AccTcCtx A, const unsigned 
         if (++consumed % TC_FLUSH == 0) flush();
       }
     }
-    // prefetch chunk c+1 (its stage was last read by the MMAs of chunk c-1 and
-    // by the formation of chunk c-1, both finished)
-    if (tid == 0 && c + 1 < nchunks) prefetch(c + 1, s ^ 1);
+    // prefetch chunk c+1 into the stage of chunk c-1 once chunk c-1's MMAs
+    // (which read its B tiles) have completed
+    if (tid == 0 && c + 1 < nchunks) {
+      bool ok = c < 1 || tc::mbar_wait(&bar[s ^ 1], ((c - 1) >> 1) & 1, TC_SPINS);
+      if (!ok) atomicExch(A.status, 1);
+      else prefetch(c + 1, s ^ 1);
+    }
     {
       bool ok = tc::mbar_wait(&mbar[s], (c >> 1) & 1, TC_SPINS);
       if (!ok) atomicExch(A.status, 1);
@@ -404,6 +409,370 @@ __global__ void __launch_bounds__(256, 1) k_accum_tc(AccTcCtx A, const unsigned 
   if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
 }
 
+// ---------------------------------------------------------------------------
+// Warp-specialised form for NGloc <= 96 (one 96-row G' tile holds every local
+// field, so the pre-split B tile of a chunk also carries the A-side vertices
+// when M2 = M).
+//   warpgroup 3 (lane 0 of warp 12): streams the pre-split B tiles and records
+//     of each chunk through a ring of S shared-memory stages (bulk copies,
+//     mbarrier tx counts) and issues chunk c's MMAs as soon as its A tiles are
+//     formed and its TMEM buffer has been read back; it runs on 56 registers
+//     (setmaxnreg) so that the formation warps get 152;
+//   warpgroups 0-2 (12 warps): read back chunk c-2 from TMEM into FP32
+//     register sums (64 of the 192 accumulator columns per thread), compute the
+//     Lorentzian weights of chunk c, and form its A tiles (w * M, re-split from
+//     the staged hi + lo halves) into slot c % 2.
+// The complex S0 keeps B1 = [Re b | Im b] and B2 = [-Im b | Re b] as one
+// 192-row operand, so D = A [B1; B2]^T is a single N = 192 MMA per product.
+// No block-wide barrier in the steady state: the hand-offs are mbarriers and
+// one named barrier of the formation warps (the weights), which also ORs
+// their failures.  Every wait is bounded and gives up early once a timeout
+// has been recorded in the shared abort flag.
+constexpr int WS_SIMT_WARPS = 12;
+constexpr int WS_SIMT = 32 * WS_SIMT_WARPS;
+constexpr int WS_THREADS = WS_SIMT + 128;
+constexpr uint32_t WS_POLLS = 1u << 16;
+// register split: 384 x 152 + 128 x 56 = 65536 = 512 x 128 registers at launch (and per SM
+// sub-partition 3 x 152 x 32 + 56 x 32 = 16384)
+constexpr int WS_REG_SIMT = 152, WS_REG_PROD = 56;
+
+__device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+  for (uint32_t i = 0; i < WS_POLLS; ++i) {
+    if (tc::mbar_try_wait_ns(bar, parity, 20000u)) return true;
+    if (*abort_flag) return false;
+  }
+  *abort_flag = 1;
+  return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
+}
+
+// Named barrier 1 of the formation warps that also ORs a flag over them.
+__device__ __forceinline__ bool simt_barrier_or(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.or.pred p, 1, %2, q;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)v), "n"(WS_SIMT)
+      : "memory");
+  return r != 0;
+}
+
+template <int NIO, bool CPLX, bool TWO>
+struct WsCfg {
+  static constexpr uint32_t A_BYTES = TC_GA * 128;                  // one 16-bit A tile
+  static constexpr uint32_t BROWS = CPLX ? 2 * TC_GB : TC_GB;       // [B1; B2] or B1
+  static constexpr uint32_t BHALF = BROWS * 128;                    // hi (or lo) rows of B
+  static constexpr uint32_t BSRC = 2 * BHALF;                       // hi, then lo
+  static constexpr uint32_t ASRC = 2 * TC_TILE;                     // separate A-side tiles (M2 != M)
+  static constexpr uint32_t REC_OFF = BSRC + (TWO ? ASRC : 0);
+  static constexpr uint32_t DATA = (REC_OFF + TC_TT * sizeof(Trans) + 1023) / 1024 * 1024;
+  static constexpr uint32_t FORMED = NIO * 2 * A_BYTES;             // (Ah, Al) x NIO
+  static constexpr int S0 = (int)((232448 - 2 * FORMED - 1024 - 3072) / DATA);
+  static constexpr int S = S0 > 6 ? 6 : S0;
+  static constexpr size_t SMEM = (size_t)S * DATA + 2 * FORMED + 1024;
+};
+
+template <int NIO, bool CPLX, bool TWO>
+__global__ void __launch_bounds__(WS_THREADS, 1)
+    k_accum_ws(AccTcCtx A, const unsigned char* __restrict__ tiles, const unsigned char* __restrict__ tilesA) {
+  using Cfg = WsCfg<NIO, CPLX, TWO>;
+  constexpr int S = Cfg::S;
+  constexpr uint32_t DATA = Cfg::DATA, FORMED = Cfg::FORMED, A_BYTES = Cfg::A_BYTES;
+  constexpr uint32_t DCOLS = 192, NCOL = 512;
+  static_assert(S >= 2, "shared-memory ring too shallow");
+  static_assert((CPLX ? 2 * NIO : NIO) * TC_GB == (int)DCOLS, "accumulator layout");
+
+  extern __shared__ unsigned char smraw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+  unsigned char* fbase = base + S * DATA;  // formed slots
+  __shared__ uint64_t dfull[S], dfree[S], formed[2], mdone[2], tfree[2];
+  __shared__ uint32_t tslot;
+  __shared__ __align__(16) float wtab[2][NIO][TC_TT];
+  __shared__ int range[2];
+  __shared__ volatile int abort_flag;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int r0 = blockIdx.x * NIO;
+  const int nrowA = A.nlf;  // every local field sits in the one G tile
+  const size_t np = (size_t)A.nlf * A.nlf;
+
+  if (warp == 0) {
+    tc::tmem_alloc(&tslot, NCOL);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int i = 0; i < S; ++i) {
+      tc::mbar_init(&dfull[i], 1);
+      tc::mbar_init(&dfree[i], WS_SIMT_WARPS + 1);  // formation warps + the MMA commit
+    }
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&formed[i], WS_SIMT_WARPS);
+      tc::mbar_init(&mdone[i], 1);
+      tc::mbar_init(&tfree[i], WS_SIMT_WARPS);
+    }
+    tc::fence_mbar_init();
+    abort_flag = 0;
+    range[0] = lb_lo(A.rec, A.n_inter, r0 - A.wmax + 1) & ~(TC_TT - 1);
+    range[1] = lb_lo(A.rec, A.n_inter, r0 + NIO);
+  }
+  // A padding rows (G >= nlf) stay zero for the whole kernel
+  for (uint32_t e = tid; e < 2 * FORMED / 16; e += WS_THREADS)
+    reinterpret_cast<uint4*>(fbase)[e] = make_uint4(0, 0, 0, 0);
+  tc::fence_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t taddr = tslot;
+  const int ta = range[0], tb = range[1];
+  const int nchunks = (tb - ta + TC_TT - 1) / TC_TT;
+  const int chunk0 = ta / TC_TT;
+
+  auto stage = [&](int c) { return base + (size_t)(c % S) * DATA; };
+  auto slot = [&](int c) { return fbase + (size_t)(c & 1) * FORMED; };
+  bool ok = true;
+
+  if (warp >= WS_SIMT_WARPS) {
+    // ---------------- producer / MMA issuer ----------------
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(WS_REG_PROD));
+    if (warp == WS_SIMT_WARPS && lane == 0) {
+      constexpr uint32_t bytes = Cfg::BSRC + (TWO ? Cfg::ASRC : 0) + TC_TT * sizeof(Trans);
+      int loaded = 0, issued = 0;
+      auto load = [&](int c) {
+        unsigned char* st = stage(c);
+        uint64_t* b = &dfull[c % S];
+        tc::mbar_arrive_expect_tx(b, bytes);
+        tc::bulk_g2s(st, tiles + (size_t)(chunk0 + c) * Cfg::BSRC, Cfg::BSRC, b);
+        if (TWO) tc::bulk_g2s(st + Cfg::BSRC, tilesA + (size_t)(chunk0 + c) * Cfg::ASRC, Cfg::ASRC, b);
+        tc::bulk_g2s(st + Cfg::REC_OFF, A.rec + ta + (size_t)c * TC_TT, TC_TT * sizeof(Trans), b);
+      };
+      const uint32_t idesc = tc::idesc_bf16(TC_GA, CPLX ? 2 * TC_GB : TC_GB, true);
+      for (; loaded < S - 1 && loaded < nchunks; ++loaded) load(loaded);
+      for (int c = 0; c < nchunks && ok; ++c) {
+        ok = ws_wait(&formed[c & 1], (c >> 1) & 1, &abort_flag);
+        if (ok && c >= 2) ok = ws_wait(&tfree[c & 1], ((c - 2) >> 1) & 1, &abort_flag);
+        if (!ok) break;
+        tc::tc_fence_after();
+        const uint32_t bh = tc::smem_u32(stage(c)), bl = bh + Cfg::BHALF;
+        const uint32_t as = tc::smem_u32(slot(c));
+        const uint32_t d0 = taddr + (uint32_t)((c & 1) * DCOLS);
+#pragma unroll
+        for (int j = 0; j < NIO; ++j) {
+          const uint32_t ah = as + j * 2 * A_BYTES, al = ah + A_BYTES;
+          const uint32_t d = d0 + (uint32_t)(j * TC_GB);
+          // cross products first, the large hi * hi products last
+#pragma unroll
+          for (int ks = 0; ks < 4; ++ks) {
+            const uint32_t ko = ks * 32;
+            tc::mma_bf16(d, tc::desc_sw128(ah + ko), tc::desc_sw128(bl + ko), idesc, ks > 0 ? 1u : 0u);
+            tc::mma_bf16(d, tc::desc_sw128(al + ko), tc::desc_sw128(bh + ko), idesc, 1u);
+          }
+#pragma unroll
+          for (int ks = 0; ks < 4; ++ks) {
+            const uint32_t ko = ks * 32;
+            tc::mma_bf16(d, tc::desc_sw128(ah + ko), tc::desc_sw128(bh + ko), idesc, 1u);
+          }
+        }
+        tc::mma_commit(&mdone[c & 1]);
+        tc::mma_commit(&dfree[c % S]);
+        issued = c + 1;
+        // refill the stage chunk c-1 used (its MMAs finish before chunk c's start)
+        if (loaded < nchunks) {
+          if (loaded >= S) ok = ws_wait(&dfree[loaded % S], ((loaded / S) - 1) & 1, &abort_flag);
+          if (!ok) break;
+          load(loaded++);
+        }
+      }
+      if (!ok) {
+        atomicExch(A.status, 1);
+        abort_flag = 1;
+        // bounded drain of this CTA's own MMAs and bulk copies
+        if (issued > 0) tc::mbar_wait(&mdone[(issued - 1) & 1], ((issued - 1) >> 1) & 1, 1024);
+        for (int c = (loaded > S ? loaded - S : 0); c < loaded; ++c) tc::mbar_wait(&dfull[c % S], (c / S) & 1, 1024);
+      }
+    }
+  } else {
+    // ---------------- read-back, weights, A formation ----------------
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(WS_REG_SIMT));
+    // accumulator slice: TMEM lane quadrant wq, columns cg * 64 .. cg * 64 + 63
+    const int wq = warp & 3, cg = warp >> 2;
+    const int grow = wq * 32 + lane;  // G
+    float acc[64];
+#pragma unroll
+    for (int i = 0; i < 64; ++i) acc[i] = 0.f;
+    int consumed = 0;
+    auto consume = [&](int c) {
+      const uint32_t a0 = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)((c & 1) * DCOLS + cg * 64);
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        float v[32];
+        tc::tmem_ld32(a0 + 32 * p, v);
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int i = 0; i < 32; ++i) acc[32 * p + i] += v[i];
+      }
+    };
+    // column col of the accumulator = (part, G'): part = Re / Im (complex) or
+    // the frequency row of the pair (real)
+    auto flush = [&]() {
+      if (grow < A.nlf) {
+        const int ncomp = CPLX ? 2 : 1;
+#pragma unroll
+        for (int j0 = 0; j0 < 64; j0 += 8) {
+          float2* dst[8];
+          float2 old[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int col = cg * 64 + j0 + j, part = col / TC_GB, gp = col - part * TC_GB;
+            const int io = CPLX ? r0 : r0 + part, comp = CPLX ? part : 0;
+            dst[j] = (gp < A.nlf && io < A.nw)
+                         ? A.Sdf + ((size_t)io * np + (size_t)grow + (size_t)A.nlf * gp) * ncomp + comp
+                         : nullptr;
+            if (dst[j]) old[j] = *dst[j];
+          }
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            if (dst[j]) *dst[j] = df_add(old[j], acc[j0 + j] * A.inv_scale);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 64; ++j) acc[j] = 0.f;
+    };
+    for (int c = 0; c < nchunks; ++c) {
+      ok = ws_wait(&dfull[c % S], (c / S) & 1, &abort_flag);
+      if (ok && c >= 2) ok = ws_wait(&mdone[c & 1], ((c - 2) >> 1) & 1, &abort_flag);
+      ok = __all_sync(0xffffffffu, ok);
+      unsigned char* st = stage(c);
+      unsigned char* fs = slot(c);
+      if (ok) {
+        if (c >= 2) {
+          tc::tc_fence_after();
+          consume(c - 2);
+          tc::tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&tfree[c & 1]);
+          if (++consumed % TC_FLUSH == 0) flush();
+        }
+        // Lorentzian weights of chunk c (scaled, 1 / source scale folded in);
+        // window membership is the exact [lo, hi] of the record
+        if (tid < NIO * TC_TT) {
+          const int j = tid / TC_TT, tt = tid % TC_TT, t = ta + c * TC_TT + tt, r = r0 + j;
+          float w = 0.f;
+          const Trans& R = reinterpret_cast<const Trans*>(st + Cfg::REC_OFF)[tt];
+          if (t < tb && r < A.nw && r >= R.lo && r <= R.hi) {
+            float dE = (float)fma((double)(r + A.obase), A.domega, R.e1 - R.e2);
+            float eta = (float)A.eta;
+            float L2 = eta / fmaf(dE, dE, eta * eta);
+            w = (float)(R.c * A.scaleA) * L2 * A.inv_src;
+          }
+          wtab[c & 1][j][tt] = w;
+        }
+      }
+      if (simt_barrier_or(!ok)) {
+        ok = false;
+        break;
+      }
+      // A tiles: A = w * (hi + lo) of the staged vertex tile (B1 rows, or the
+      // separate A-side tile), re-split
+      const unsigned char* srch = st + (TWO ? Cfg::BSRC : 0);
+      const unsigned char* srcl = srch + (TWO ? TC_TILE : Cfg::BHALF);
+      for (int e = tid; e < nrowA * 8; e += WS_SIMT) {
+        const int row = e >> 3, ch = e & 7;
+        const uint32_t off = (uint32_t)row * 128u + ((uint32_t)(ch ^ (row & 7)) << 4);
+        const uint4 h = *reinterpret_cast<const uint4*>(srch + off);
+        const uint4 l = *reinterpret_cast<const uint4*>(srcl + off);
+        float x[8];
+        const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float2 fh = __half22float2(*reinterpret_cast<const __half2*>(&hw[i]));
+          const float2 fl = __half22float2(*reinterpret_cast<const __half2*>(&lw[i]));
+          x[2 * i] = fh.x + fl.x;
+          x[2 * i + 1] = fh.y + fl.y;
+        }
+        const int tt0 = (ch & 3) * 8;
+#pragma unroll
+        for (int j = 0; j < NIO; ++j) {
+          const float4 w0 = *reinterpret_cast<const float4*>(&wtab[c & 1][j][tt0]);
+          const float4 w1 = *reinterpret_cast<const float4*>(&wtab[c & 1][j][tt0 + 4]);
+          const float y[8] = {x[0] * w0.x, x[1] * w0.y, x[2] * w0.z, x[3] * w0.w,
+                              x[4] * w1.x, x[5] * w1.y, x[6] * w1.z, x[7] * w1.w};
+          uint4 hi, lo;
+          split8<true>(y, hi, lo);
+          *reinterpret_cast<uint4*>(fs + j * 2 * A_BYTES + off) = hi;
+          *reinterpret_cast<uint4*>(fs + j * 2 * A_BYTES + A_BYTES + off) = lo;
+        }
+      }
+      tc::fence_async_smem();
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(&formed[c & 1]);
+        mbar_arrive(&dfree[c % S]);
+      }
+    }
+    // drain: read back the last (up to) two chunks
+    if (ok) {
+      for (int c = (nchunks >= 2 ? nchunks - 2 : 0); c < nchunks && ok; ++c) {
+        ok = __all_sync(0xffffffffu, ws_wait(&mdone[c & 1], (c >> 1) & 1, &abort_flag));
+        if (!ok) break;
+        tc::tc_fence_after();
+        consume(c);
+      }
+      if (ok) flush();
+    }
+    if (!ok) {
+      atomicExch(A.status, 1);
+      abort_flag = 1;
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
+}
+
+// Pre-split B operand of the warp-specialised kernel, per chunk: the hi rows,
+// then the lo rows; rows 0-95 = [Re b | Im b] (B1), rows 96-191 = [-Im b | Re b]
+// (B2, complex S0 only), b = scale * M(G'), rows >= nlf zero.
+template <bool CPLX>
+__global__ void k_presplit_ws(const float2* __restrict__ M, int nlf, int nchunks, float scale,
+                              unsigned char* __restrict__ tiles) {
+  constexpr uint32_t BROWS = CPLX ? 2 * TC_GB : TC_GB, BHALF = BROWS * 128;
+  const long long ntask = (long long)nchunks * TC_GB * 4;
+  for (long long task = blockIdx.x * (long long)blockDim.x + threadIdx.x; task < ntask;
+       task += (long long)gridDim.x * blockDim.x) {
+    const int ch = (int)(task / (TC_GB * 4)), rem = (int)(task % (TC_GB * 4));
+    const int row = rem % TC_GB, grp = rem / TC_GB;
+    float re[8], im[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      float2 m = row < nlf ? M[((size_t)ch * TC_TT + grp * 8 + q) * nlf + row] : make_float2(0.f, 0.f);
+      re[q] = m.x * scale;
+      im[q] = m.y * scale;
+    }
+    unsigned char* t = tiles + (size_t)ch * 2 * BHALF;
+    uint4 rh, rl, ih, il;
+    split8<true>(re, rh, rl);
+    split8<true>(im, ih, il);
+    st16(t, row, grp, rh);
+    st16(t + BHALF, row, grp, rl);
+    st16(t, row, 4 + grp, ih);
+    st16(t + BHALF, row, 4 + grp, il);
+    if (CPLX) {
+      const uint32_t sg = 0x80008000u;  // split(-x) = -split(x)
+      const int r2 = TC_GB + row;
+      st16(t, r2, grp, make_uint4(ih.x ^ sg, ih.y ^ sg, ih.z ^ sg, ih.w ^ sg));
+      st16(t + BHALF, r2, grp, make_uint4(il.x ^ sg, il.y ^ sg, il.z ^ sg, il.w ^ sg));
+      st16(t, r2, 4 + grp, rh);
+      st16(t + BHALF, r2, 4 + grp, rl);
+    }
+  }
+}
+
 __global__ void k_cmax(const Trans* __restrict__ rec, int n, unsigned long long* cmax) {
   double mx = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) mx = fmax(mx, fabs(rec[i].c));
@@ -427,6 +796,25 @@ static int launch_tc(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char*
   RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((nw + NIO - 1) / NIO, (A.nlf + TC_GA - 1) / TC_GA, (A.nlf + TC_GB - 1) / TC_GB);
   kern<<<grid, 256, smem, c->stream>>>(A, tiles);
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  return RPA_OK;
+}
+
+template <int NIO, bool CPLX, bool TWO>
+static int launch_ws(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char* tiles, const unsigned char* tilesA) {
+  using Cfg = WsCfg<NIO, CPLX, TWO>;
+  auto kern = k_accum_ws<NIO, CPLX, TWO>;
+  RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM));
+  kern<<<(nw + NIO - 1) / NIO, WS_THREADS, Cfg::SMEM, c->stream>>>(A, tiles, tilesA);
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  return RPA_OK;
+}
+
+template <bool CPLX>
+static int launch_presplit_ws(rpa_ctx* c, const float2* M, int nchunks, float scale, unsigned char* tiles) {
+  k_presplit_ws<CPLX><<<4096, 256, 0, c->stream>>>(M, c->nlf, nchunks, scale, tiles);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
   return RPA_OK;
@@ -472,6 +860,28 @@ int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const fl
   const bool cplx = P.mode == RPA_MODE_CURRENT;
   const int nch = A.n_rows / TC_TT + 1;  // one spare chunk for the last prefetch
   const int nht = (c->nlf + TC_GB - 1) / TC_GB;
+  const bool two = Mf2 != Mf;
+  if (f16 && c->nlf <= TC_GB && A.seg == 1) {
+    // warp-specialised kernel: the A side reads the B1 rows when M2 = M, else
+    // its own pre-split copy
+    const size_t tbytes = (size_t)nch * (cplx ? 4 : 2) * TC_TILE;
+    RPA_TRY(ensure(c, c->d_tiles, tbytes));
+    unsigned char* tiles = c->d_tiles.as<unsigned char>();
+    RPA_TRY(cplx ? launch_presplit_ws<true>(c, Mf2, nch, A.scaleB, tiles)
+                 : launch_presplit_ws<false>(c, Mf2, nch, A.scaleB, tiles));
+    const unsigned char* tilesA = tiles;
+    A.inv_src = 1.0f / A.scaleB;
+    if (two) {
+      const double amS = (double)amaxM * 1.5;
+      const float sM = amS > 0 ? (float)(16384.0 / pow2_floor(amS)) : 1.0f;
+      RPA_TRY(ensure(c, c->d_tilesA, (size_t)nch * 2 * TC_TILE));
+      RPA_TRY(launch_presplit<true, false>(c, Mf, nch, sM, c->d_tilesA.as<unsigned char>()));
+      tilesA = c->d_tilesA.as<unsigned char>();
+      A.inv_src = 1.0f / sM;
+    }
+    if (cplx) return two ? launch_ws<1, true, true>(c, A, P.nw, tiles, tilesA) : launch_ws<1, true, false>(c, A, P.nw, tiles, tilesA);
+    return launch_ws<2, false, false>(c, A, P.nw, tiles, tilesA);
+  }
   const size_t tbytes = (size_t)nch * nht * (cplx ? 4 : 2) * TC_TILE;
   RPA_TRY(ensure(c, c->d_tiles, tbytes));
   unsigned char* tiles = c->d_tiles.as<unsigned char>();

@@ -413,21 +413,27 @@ __global__ void __launch_bounds__(256, 1) k_accum_tc(AccTcCtx A, const unsigned 
 // Warp-specialised form for NGloc <= 96 (one 96-row G' tile holds every local
 // field, so the pre-split B tile of a chunk also carries the A-side vertices
 // when M2 = M).
-//   warpgroup 3 (lane 0 of warp 12): streams the pre-split B tiles and records
-//     of each chunk through a ring of S shared-memory stages (bulk copies,
-//     mbarrier tx counts) and issues chunk c's MMAs as soon as its A tiles are
-//     formed and its TMEM buffer has been read back; it runs on 56 registers
-//     (setmaxnreg) so that the formation warps get 152;
-//   warpgroups 0-2 (12 warps): read back chunk c-2 from TMEM into FP32
-//     register sums (64 of the 192 accumulator columns per thread), compute the
-//     Lorentzian weights of chunk c, and form its A tiles (w * M, re-split from
-//     the staged hi + lo halves) into slot c % 2.
+//   warpgroup 3, on 56 registers (setmaxnreg) so that the formation warps get
+//     152: lane 0 of warp 14 streams the pre-split B tiles and records of each
+//     chunk through a ring of S shared-memory stages (bulk copies, mbarrier tx
+//     counts), refilling a stage as soon as it is released; lane 0 of warp 12
+//     issues chunk c's MMAs as soon as its A tiles are formed and its TMEM
+//     buffer has been read back;
+//   warp 13: computes the Lorentzian weights of chunk c from its staged
+//     records into wtab[c % 2] and hands them over through an mbarrier;
+//   warpgroups 0-2 (12 warps): read back the TMEM accumulator of each pair
+//     of chunks (a segment) into FP32 register sums (64 of the 192 columns per
+//     thread) and form the A tiles of chunk c (w * M, re-split from the staged
+//     hi + lo halves) into slot c % 2.
+// Precision: a TMEM accumulator sums the 2 x 12 MMAs of one segment (the
+// tensor core's FP32 accumulation drops low bits as more products are chained,
+// measured 4e-7 for one chunk and 8e-7 for two), the segments are summed in
+// FP32 registers and flushed to the double-float S0 every TC_FLUSH segments.
 // The complex S0 keeps B1 = [Re b | Im b] and B2 = [-Im b | Re b] as one
 // 192-row operand, so D = A [B1; B2]^T is a single N = 192 MMA per product.
-// No block-wide barrier in the steady state: the hand-offs are mbarriers and
-// one named barrier of the formation warps (the weights), which also ORs
-// their failures.  Every wait is bounded and gives up early once a timeout
-// has been recorded in the shared abort flag.
+// No barrier in the steady state: every hand-off is an mbarrier.  Every wait
+// is bounded and gives up early once a timeout has been recorded in the shared
+// abort flag.
 constexpr int WS_SIMT_WARPS = 12;
 constexpr int WS_SIMT = 32 * WS_SIMT_WARPS;
 constexpr int WS_THREADS = WS_SIMT + 128;
@@ -436,10 +442,15 @@ constexpr uint32_t WS_POLLS = 1u << 16;
 // sub-partition 3 x 152 x 32 + 56 x 32 = 16384)
 constexpr int WS_REG_SIMT = 152, WS_REG_PROD = 56;
 
+// Bounded wait with a growing sleep between polls, so that waiting warps give
+// their issue slots to the warps that form operands.
 __device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+  uint32_t ns = 32;
   for (uint32_t i = 0; i < WS_POLLS; ++i) {
     if (tc::mbar_try_wait_ns(bar, parity, 20000u)) return true;
     if (*abort_flag) return false;
+    __nanosleep(ns);
+    ns = ns < 256 ? 2 * ns : 256;
   }
   *abort_flag = 1;
   return false;
@@ -447,20 +458,6 @@ __device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
-}
-
-// Named barrier 1 of the formation warps that also ORs a flag over them.
-__device__ __forceinline__ bool simt_barrier_or(bool v) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\t"
-      "setp.ne.u32 q, %1, 0;\n\t"
-      "bar.red.or.pred p, 1, %2, q;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(r)
-      : "r"((uint32_t)v), "n"(WS_SIMT)
-      : "memory");
-  return r != 0;
 }
 
 template <int NIO, bool CPLX, bool TWO>
@@ -491,7 +488,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
   extern __shared__ unsigned char smraw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
   unsigned char* fbase = base + S * DATA;  // formed slots
-  __shared__ uint64_t dfull[S], dfree[S], formed[2], mdone[2], tfree[2];
+  __shared__ uint64_t dfull[S], dfree[S], formed[2], mdone[2], tfree[2], wready[2];
   __shared__ uint32_t tslot;
   __shared__ __align__(16) float wtab[2][NIO][TC_TT];
   __shared__ int range[2];
@@ -509,12 +506,13 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
   if (tid == 0) {
     for (int i = 0; i < S; ++i) {
       tc::mbar_init(&dfull[i], 1);
-      tc::mbar_init(&dfree[i], WS_SIMT_WARPS + 1);  // formation warps + the MMA commit
+      tc::mbar_init(&dfree[i], WS_SIMT_WARPS + 2);  // formation warps, the weights warp, the MMA commit
     }
     for (int i = 0; i < 2; ++i) {
       tc::mbar_init(&formed[i], WS_SIMT_WARPS);
       tc::mbar_init(&mdone[i], 1);
       tc::mbar_init(&tfree[i], WS_SIMT_WARPS);
+      tc::mbar_init(&wready[i], 1);
     }
     tc::fence_mbar_init();
     abort_flag = 0;
@@ -540,27 +538,44 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
   if (warp >= WS_SIMT_WARPS) {
     // ---------------- producer / MMA issuer ----------------
     asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(WS_REG_PROD));
-    if (warp == WS_SIMT_WARPS && lane == 0) {
+    if (warp == WS_SIMT_WARPS + 2 && lane == 0) {
+      // ---------------- loads: a stage is refilled as soon as it is released ----------------
       constexpr uint32_t bytes = Cfg::BSRC + (TWO ? Cfg::ASRC : 0) + TC_TT * sizeof(Trans);
-      int loaded = 0, issued = 0;
-      auto load = [&](int c) {
-        unsigned char* st = stage(c);
-        uint64_t* b = &dfull[c % S];
+      int loaded = 0;
+      for (; loaded < nchunks && ok; ++loaded) {
+        if (loaded >= S) ok = ws_wait(&dfree[loaded % S], ((loaded / S) - 1) & 1, &abort_flag);
+        if (!ok) break;
+        unsigned char* st = stage(loaded);
+        uint64_t* b = &dfull[loaded % S];
         tc::mbar_arrive_expect_tx(b, bytes);
-        tc::bulk_g2s(st, tiles + (size_t)(chunk0 + c) * Cfg::BSRC, Cfg::BSRC, b);
-        if (TWO) tc::bulk_g2s(st + Cfg::BSRC, tilesA + (size_t)(chunk0 + c) * Cfg::ASRC, Cfg::ASRC, b);
-        tc::bulk_g2s(st + Cfg::REC_OFF, A.rec + ta + (size_t)c * TC_TT, TC_TT * sizeof(Trans), b);
-      };
+        tc::bulk_g2s(st, tiles + (size_t)(chunk0 + loaded) * Cfg::BSRC, Cfg::BSRC, b);
+        if (TWO) tc::bulk_g2s(st + Cfg::BSRC, tilesA + (size_t)(chunk0 + loaded) * Cfg::ASRC, Cfg::ASRC, b);
+        tc::bulk_g2s(st + Cfg::REC_OFF, A.rec + ta + (size_t)loaded * TC_TT, TC_TT * sizeof(Trans), b);
+      }
+      if (!ok) {
+        abort_flag = 1;
+        // bounded wait for the copies in flight before shared memory is released
+        for (int c = (loaded > S ? loaded - S : 0); c < loaded; ++c) tc::mbar_wait(&dfull[c % S], (c / S) & 1, 1024);
+      }
+    }
+    if (warp == WS_SIMT_WARPS && lane == 0) {
+      // ---------------- MMA issue ----------------
+      int issued = 0;
       const uint32_t idesc = tc::idesc_bf16(TC_GA, CPLX ? 2 * TC_GB : TC_GB, true);
-      for (; loaded < S - 1 && loaded < nchunks; ++loaded) load(loaded);
       for (int c = 0; c < nchunks && ok; ++c) {
         ok = ws_wait(&formed[c & 1], (c >> 1) & 1, &abort_flag);
-        if (ok && c >= 2) ok = ws_wait(&tfree[c & 1], ((c - 2) >> 1) & 1, &abort_flag);
+        // an even chunk opens segment c / 2 in TMEM buffer (c / 2) % 2, whose
+        // previous segment must have been read back
+        if (ok && (c & 1) == 0 && c >= 4) {
+          const int sg = (c >> 1) - 2;
+          ok = ws_wait(&tfree[sg & 1], (sg >> 1) & 1, &abort_flag);
+        }
         if (!ok) break;
         tc::tc_fence_after();
         const uint32_t bh = tc::smem_u32(stage(c)), bl = bh + Cfg::BHALF;
         const uint32_t as = tc::smem_u32(slot(c));
-        const uint32_t d0 = taddr + (uint32_t)((c & 1) * DCOLS);
+        const uint32_t d0 = taddr + (uint32_t)(((c >> 1) & 1) * DCOLS);
+        const uint32_t first = (c & 1) ? 1u : 0u;
 #pragma unroll
         for (int j = 0; j < NIO; ++j) {
           const uint32_t ah = as + j * 2 * A_BYTES, al = ah + A_BYTES;
@@ -569,7 +584,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
 #pragma unroll
           for (int ks = 0; ks < 4; ++ks) {
             const uint32_t ko = ks * 32;
-            tc::mma_bf16(d, tc::desc_sw128(ah + ko), tc::desc_sw128(bl + ko), idesc, ks > 0 ? 1u : 0u);
+            tc::mma_bf16(d, tc::desc_sw128(ah + ko), tc::desc_sw128(bl + ko), idesc, ks > 0 ? 1u : first);
             tc::mma_bf16(d, tc::desc_sw128(al + ko), tc::desc_sw128(bh + ko), idesc, 1u);
           }
 #pragma unroll
@@ -581,20 +596,45 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
         tc::mma_commit(&mdone[c & 1]);
         tc::mma_commit(&dfree[c % S]);
         issued = c + 1;
-        // refill the stage chunk c-1 used (its MMAs finish before chunk c's start)
-        if (loaded < nchunks) {
-          if (loaded >= S) ok = ws_wait(&dfree[loaded % S], ((loaded / S) - 1) & 1, &abort_flag);
-          if (!ok) break;
-          load(loaded++);
-        }
       }
       if (!ok) {
         atomicExch(A.status, 1);
         abort_flag = 1;
-        // bounded drain of this CTA's own MMAs and bulk copies
+        // bounded drain of this CTA's own MMAs
         if (issued > 0) tc::mbar_wait(&mdone[(issued - 1) & 1], ((issued - 1) >> 1) & 1, 1024);
-        for (int c = (loaded > S ? loaded - S : 0); c < loaded; ++c) tc::mbar_wait(&dfull[c % S], (c / S) & 1, 1024);
       }
+    }
+    if (warp == WS_SIMT_WARPS + 1) {
+      // ---------------- Lorentzian weights ----------------
+      for (int c = 0; c < nchunks && ok; ++c) {
+        ok = ws_wait(&dfull[c % S], (c / S) & 1, &abort_flag);
+        if (ok && c >= 2) ok = ws_wait(&formed[c & 1], ((c - 2) >> 1) & 1, &abort_flag);  // wtab[c % 2] read
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok) break;
+        const Trans* rec = reinterpret_cast<const Trans*>(stage(c) + Cfg::REC_OFF);
+        const int t = ta + c * TC_TT + lane;
+        const Trans& R = rec[lane];
+        const double dE0 = R.e1 - R.e2;
+        const float cs = (float)(R.c * A.scaleA) * A.inv_src;
+        const float eta = (float)A.eta;
+#pragma unroll
+        for (int j = 0; j < NIO; ++j) {
+          // window membership is the exact [lo, hi] of the record
+          const int r = r0 + j;
+          float w = 0.f;
+          if (t < tb && r < A.nw && r >= R.lo && r <= R.hi) {
+            const float dE = (float)fma((double)(r + A.obase), A.domega, dE0);
+            w = cs * (eta / fmaf(dE, dE, eta * eta));
+          }
+          wtab[c & 1][j][lane] = w;
+        }
+        __syncwarp();
+        if (lane == 0) {
+          mbar_arrive(&wready[c & 1]);
+          mbar_arrive(&dfree[c % S]);
+        }
+      }
+      if (!ok) abort_flag = 1;
     }
   } else {
     // ---------------- read-back, weights, A formation ----------------
@@ -606,16 +646,14 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
 #pragma unroll
     for (int i = 0; i < 64; ++i) acc[i] = 0.f;
     int consumed = 0;
-    auto consume = [&](int c) {
-      const uint32_t a0 = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)((c & 1) * DCOLS + cg * 64);
+    auto consume = [&](int buf) {
+      const uint32_t a0 = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)(buf * DCOLS + cg * 64);
+      float v[64];
+      tc::tmem_ld32(a0, v);
+      tc::tmem_ld32(a0 + 32, v + 32);
+      tc::tmem_ld_wait();
 #pragma unroll
-      for (int p = 0; p < 2; ++p) {
-        float v[32];
-        tc::tmem_ld32(a0 + 32 * p, v);
-        tc::tmem_ld_wait();
-#pragma unroll
-        for (int i = 0; i < 32; ++i) acc[32 * p + i] += v[i];
-      }
+      for (int i = 0; i < 64; ++i) acc[i] += v[i];
     };
     // column col of the accumulator = (part, G'): part = Re / Im (complex) or
     // the frequency row of the pair (real)
@@ -649,38 +687,24 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
       ok = __all_sync(0xffffffffu, ok);
       unsigned char* st = stage(c);
       unsigned char* fs = slot(c);
-      if (ok) {
-        if (c >= 2) {
-          tc::tc_fence_after();
-          consume(c - 2);
-          tc::tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&tfree[c & 1]);
-          if (++consumed % TC_FLUSH == 0) flush();
-        }
-        // Lorentzian weights of chunk c (scaled, 1 / source scale folded in);
-        // window membership is the exact [lo, hi] of the record
-        if (tid < NIO * TC_TT) {
-          const int j = tid / TC_TT, tt = tid % TC_TT, t = ta + c * TC_TT + tt, r = r0 + j;
-          float w = 0.f;
-          const Trans& R = reinterpret_cast<const Trans*>(st + Cfg::REC_OFF)[tt];
-          if (t < tb && r < A.nw && r >= R.lo && r <= R.hi) {
-            float dE = (float)fma((double)(r + A.obase), A.domega, R.e1 - R.e2);
-            float eta = (float)A.eta;
-            float L2 = eta / fmaf(dE, dE, eta * eta);
-            w = (float)(R.c * A.scaleA) * L2 * A.inv_src;
-          }
-          wtab[c & 1][j][tt] = w;
-        }
+      // chunk c-2 done: its slot is free, and for odd c it closed segment
+      // (c - 3) / 2, which is read back now
+      if (ok && c >= 3 && (c & 1)) {
+        const int sg = (c - 3) >> 1;
+        tc::tc_fence_after();
+        consume(sg & 1);
+        tc::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&tfree[sg & 1]);
+        if (++consumed % TC_FLUSH == 0) flush();
       }
-      if (simt_barrier_or(!ok)) {
-        ok = false;
-        break;
-      }
+      if (ok) ok = __all_sync(0xffffffffu, ws_wait(&wready[c & 1], (c >> 1) & 1, &abort_flag));
+      if (!ok) break;
       // A tiles: A = w * (hi + lo) of the staged vertex tile (B1 rows, or the
       // separate A-side tile), re-split
       const unsigned char* srch = st + (TWO ? Cfg::BSRC : 0);
       const unsigned char* srcl = srch + (TWO ? TC_TILE : Cfg::BHALF);
+#pragma unroll 2
       for (int e = tid; e < nrowA * 8; e += WS_SIMT) {
         const int row = e >> 3, ch = e & 7;
         const uint32_t off = (uint32_t)row * 128u + ((uint32_t)(ch ^ (row & 7)) << 4);
@@ -715,13 +739,15 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
         mbar_arrive(&dfree[c % S]);
       }
     }
-    // drain: read back the last (up to) two chunks
+    // drain: read back the segments the loop did not reach
     if (ok) {
-      for (int c = (nchunks >= 2 ? nchunks - 2 : 0); c < nchunks && ok; ++c) {
-        ok = __all_sync(0xffffffffu, ws_wait(&mdone[c & 1], (c >> 1) & 1, &abort_flag));
+      const int nseg = (nchunks + 1) / 2, ncons = nchunks >= 3 ? (nchunks - 2) / 2 : 0;
+      for (int sg = ncons; sg < nseg && ok; ++sg) {
+        const int cl = min(2 * sg + 1, nchunks - 1);
+        ok = __all_sync(0xffffffffu, ws_wait(&mdone[cl & 1], (cl >> 1) & 1, &abort_flag));
         if (!ok) break;
         tc::tc_fence_after();
-        consume(c);
+        consume(sg & 1);
       }
       if (ok) flush();
     }

@@ -54,10 +54,15 @@ __device__ __forceinline__ bool mbar_try_wait_ns(uint64_t* bar, uint32_t parity,
 }
 
 // Waits until the phase with the given parity completed, at most `polls`
-// suspending polls of up to 20 us each; false when it gave up.
+// suspending polls of up to 20 us each with a short growing sleep between
+// them; false when it gave up.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t polls) {
-  for (uint32_t i = 0; i < polls; ++i)
+  uint32_t ns = 32;
+  for (uint32_t i = 0; i < polls; ++i) {
     if (mbar_try_wait_ns(bar, parity, 20000u)) return true;
+    __nanosleep(ns);
+    ns = ns < 256 ? 2 * ns : 256;
+  }
   return false;
 }
 

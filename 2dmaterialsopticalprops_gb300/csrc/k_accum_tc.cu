@@ -530,6 +530,12 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
   const int ta = range[0], tb = range[1];
   const int nchunks = (tb - ta + TC_TT - 1) / TC_TT;
   const int chunk0 = ta / TC_TT;
+  // Step c of every CTA handles the chunk of its range congruent to c modulo
+  // the range length, so CTAs of neighbouring frequency rows (whose ranges
+  // overlap almost entirely) read each chunk at the same time and it is
+  // fetched from DRAM about once per wave.
+  const int rot = nchunks > 0 ? ((-chunk0) % nchunks + nchunks) % nchunks : 0;
+  auto phys = [&](int c) { const int p = c + rot; return p >= nchunks ? p - nchunks : p; };
 
   auto stage = [&](int c) { return base + (size_t)(c % S) * DATA; };
   auto slot = [&](int c) { return fbase + (size_t)(c & 1) * FORMED; };
@@ -548,9 +554,10 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
         unsigned char* st = stage(loaded);
         uint64_t* b = &dfull[loaded % S];
         tc::mbar_arrive_expect_tx(b, bytes);
-        tc::bulk_g2s(st, tiles + (size_t)(chunk0 + loaded) * Cfg::BSRC, Cfg::BSRC, b);
-        if (TWO) tc::bulk_g2s(st + Cfg::BSRC, tilesA + (size_t)(chunk0 + loaded) * Cfg::ASRC, Cfg::ASRC, b);
-        tc::bulk_g2s(st + Cfg::REC_OFF, A.rec + ta + (size_t)loaded * TC_TT, TC_TT * sizeof(Trans), b);
+        const int pc = phys(loaded);
+        tc::bulk_g2s(st, tiles + (size_t)(chunk0 + pc) * Cfg::BSRC, Cfg::BSRC, b);
+        if (TWO) tc::bulk_g2s(st + Cfg::BSRC, tilesA + (size_t)(chunk0 + pc) * Cfg::ASRC, Cfg::ASRC, b);
+        tc::bulk_g2s(st + Cfg::REC_OFF, A.rec + ta + (size_t)pc * TC_TT, TC_TT * sizeof(Trans), b);
       }
       if (!ok) {
         abort_flag = 1;
@@ -612,7 +619,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
         ok = __all_sync(0xffffffffu, ok);
         if (!ok) break;
         const Trans* rec = reinterpret_cast<const Trans*>(stage(c) + Cfg::REC_OFF);
-        const int t = ta + c * TC_TT + lane;
+        const int t = ta + phys(c) * TC_TT + lane;
         const Trans& R = rec[lane];
         const double dE0 = R.e1 - R.e2;
         const float cs = (float)(R.c * A.scaleA) * A.inv_src;
@@ -648,12 +655,14 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
     int consumed = 0;
     auto consume = [&](int buf) {
       const uint32_t a0 = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)(buf * DCOLS + cg * 64);
-      float v[64];
-      tc::tmem_ld32(a0, v);
-      tc::tmem_ld32(a0 + 32, v + 32);
-      tc::tmem_ld_wait();
 #pragma unroll
-      for (int i = 0; i < 64; ++i) acc[i] += v[i];
+      for (int p = 0; p < 2; ++p) {
+        float v[32];
+        tc::tmem_ld32(a0 + 32 * p, v);
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int i = 0; i < 32; ++i) acc[32 * p + i] += v[i];
+      }
     };
     // column col of the accumulator = (part, G'): part = Re / Im (complex) or
     // the frequency row of the pair (real)
@@ -661,11 +670,11 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
       if (grow < A.nlf) {
         const int ncomp = CPLX ? 2 : 1;
 #pragma unroll
-        for (int j0 = 0; j0 < 64; j0 += 8) {
-          float2* dst[8];
-          float2 old[8];
+        for (int j0 = 0; j0 < 64; j0 += 4) {
+          float2* dst[4];
+          float2 old[4];
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
+          for (int j = 0; j < 4; ++j) {
             const int col = cg * 64 + j0 + j, part = col / TC_GB, gp = col - part * TC_GB;
             const int io = CPLX ? r0 : r0 + part, comp = CPLX ? part : 0;
             dst[j] = (gp < A.nlf && io < A.nw)
@@ -674,7 +683,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
             if (dst[j]) old[j] = *dst[j];
           }
 #pragma unroll
-          for (int j = 0; j < 8; ++j)
+          for (int j = 0; j < 4; ++j)
             if (dst[j]) *dst[j] = df_add(old[j], acc[j0 + j] * A.inv_scale);
         }
       }

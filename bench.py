@@ -43,6 +43,8 @@ def config_of(name: str, q_steps: int):
     synth = pkg("synth")
     if name == "grid120":
         return synth.config_grid120(q_steps=q_steps)
+    if name == "grid60":  # the grid120 workload on a 60x60 k-grid (profiling-size case)
+        return synth.config_grid120(nk=60, q_steps=q_steps)
     if name == "grid24":
         return synth.config_grid24()
     if name == "small":

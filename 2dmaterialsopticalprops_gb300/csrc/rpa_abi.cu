@@ -273,10 +273,71 @@ int rpa_create(rpa_ctx** out, const rpa_opts* opts) {
   return RPA_OK;
 }
 
+// A context on the parent's device that shares the parent's G list, symmetry
+// and basis on the device (no copy) and owns its own k map, q, per-call buffers,
+// results and stream, so that several q-points run at once on one resident basis.
+int rpa_create_shared(rpa_ctx** out, rpa_ctx* parent) {
+  if (!out || !parent) return fail(nullptr, RPA_EINVAL, "rpa_create_shared: NULL argument");
+  *out = nullptr;
+  if (parent->parent) return fail(parent, RPA_EINVAL, "rpa_create_shared: parent is itself a shared context");
+  if (parent->nks == 0 || parent->ng == 0)
+    return fail(parent, RPA_ESTATE, "rpa_create_shared: parent has no G vectors or basis loaded");
+  cudaError_t e = cudaSetDevice(parent->device);
+  if (e != cudaSuccess) return fail(parent, RPA_ECUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+  rpa_ctx* c = new rpa_ctx();
+  c->device = parent->device;
+  c->precision = parent->precision;
+  c->verbose = parent->verbose;
+  c->split_f16 = parent->split_f16;
+  c->tc_seg = parent->tc_seg;
+  c->vertex_tc = parent->vertex_tc;
+  c->ng = parent->ng;
+  c->h_miller = parent->h_miller;
+  c->h_G = parent->h_G;
+  std::memcpy(c->KC, parent->KC, sizeof(c->KC));
+  std::memcpy(c->box_lo, parent->box_lo, sizeof(c->box_lo));
+  std::memcpy(c->box_dim, parent->box_dim, sizeof(c->box_dim));
+  c->nsym = parent->nsym;
+  c->h_R = parent->h_R;
+  c->h_RI = parent->h_RI;
+  c->h_Rc = parent->h_Rc;
+  c->h_RIc = parent->h_RIc;
+  c->nks = parent->nks;
+  c->nbnd = parent->nbnd;
+  c->npwx = parent->npwx;
+  c->legacy = parent->legacy;
+  c->h_npw = parent->h_npw;
+  c->h_E = parent->h_E;
+  DevBuf* mine[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
+                    &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_coeffs, &c->d_E};
+  const DevBuf* theirs[] = {&parent->d_miller, &parent->d_G, &parent->d_box, &parent->d_Rc, &parent->d_RIc,
+                            &parent->d_Rcart, &parent->d_npw, &parent->d_gidx, &parent->d_inv, &parent->d_coeff,
+                            &parent->d_coeff32, &parent->d_coeffs, &parent->d_E};
+  for (size_t i = 0; i < sizeof(mine) / sizeof(mine[0]); ++i) *mine[i] = *theirs[i];
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(parent, RPA_ECUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  for (auto& ev : c->ev) cudaEventCreate(&ev);
+  c->parent = parent;
+  ++parent->children;
+  *out = c;
+  return RPA_OK;
+}
+
 int rpa_destroy(rpa_ctx* c) {
   if (!c) return RPA_OK;
+  if (c->children > 0) return fail(c, RPA_ESTATE, "rpa_destroy: %d shared contexts still use this basis", c->children);
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  if (c->parent) {
+    // borrowed from the parent: not ours to free
+    DevBuf* borrowed[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
+                          &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_coeffs, &c->d_E};
+    for (DevBuf* b : borrowed) *b = DevBuf();
+    --c->parent->children;
+  }
   DevBuf* bufs[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
                     &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_coeffs, &c->d_E, &c->d_kmap, &c->d_ktot, &c->d_lf_miller,
                     &c->d_Glf, &c->d_occ, &c->d_counts, &c->d_offsets, &c->d_trans, &c->d_keys, &c->d_keys_alt,
@@ -295,6 +356,8 @@ const char* rpa_last_error(const rpa_ctx* c) { return c ? c->err.c_str() : g_cre
 
 int rpa_set_gvectors(rpa_ctx* c, int ng, const int* miller, const double* G, const double* KC) {
   if (c) c->gmap_valid = false;
+  if (c && (c->parent || c->children > 0))
+    return fail(c, RPA_ESTATE, "rpa_set_gvectors: the G list and basis are shared between contexts");
   if (!c || ng <= 0 || !miller || !G || !KC) return fail(c, RPA_EINVAL, "rpa_set_gvectors: bad arguments");
   cudaSetDevice(c->device);
   if (miller[0] != 0 || miller[1] != 0 || miller[2] != 0)
@@ -334,6 +397,8 @@ int rpa_set_gvectors(rpa_ctx* c, int ng, const int* miller, const double* G, con
 
 int rpa_set_symmetry(rpa_ctx* c, int nsym, const double* R, const double* RI) {
   if (c) c->gmap_valid = false;
+  if (c && (c->parent || c->children > 0))
+    return fail(c, RPA_ESTATE, "rpa_set_symmetry: the G list and basis are shared between contexts");
   if (!c || nsym < 1 || nsym > 48 || !R || !RI) return fail(c, RPA_EINVAL, "rpa_set_symmetry: bad arguments");
   if (c->ng == 0) return fail(c, RPA_ESTATE, "rpa_set_symmetry: call rpa_set_gvectors first");
   cudaSetDevice(c->device);
@@ -345,6 +410,8 @@ int rpa_set_symmetry(rpa_ctx* c, int nsym, const double* R, const double* RI) {
 
 int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, const int* igk, const double* coeff,
                    const double* E) {
+  if (c && (c->parent || c->children > 0))
+    return fail(c, RPA_ESTATE, "rpa_load_basis: the G list and basis are shared between contexts");
   if (c) c->gmap_valid = false;
   if (!c || nks <= 0 || nbnd <= 0 || npwx <= 0 || !npw || !coeff || !E)
     return fail(c, RPA_EINVAL, "rpa_load_basis: bad arguments");
@@ -834,6 +901,15 @@ int rpa_launch_count(const rpa_ctx* c, long long* count) {
 int rpa_get_stream(const rpa_ctx* c, void** stream) {
   if (!c || !stream) return RPA_EINVAL;
   *stream = (void*)c->stream;
+  return RPA_OK;
+}
+
+int rpa_basis_info(const rpa_ctx* c, int* out4) {
+  if (!c || !out4) return RPA_EINVAL;
+  out4[0] = c->nks;
+  out4[1] = c->nbnd;
+  out4[2] = c->npwx;
+  out4[3] = c->ng;
   return RPA_OK;
 }
 

@@ -46,6 +46,10 @@ struct rpa_ctx {
   bool vertex_tc = true;  // mixed path: vertices on the tensor cores (else FP32 CUDA cores)
   cudaStream_t stream = nullptr;
   std::string err;
+  // a context made by rpa_create_shared borrows the G list, symmetry and basis
+  // buffers of its parent (read-only); the parent counts its live children
+  rpa_ctx* parent = nullptr;
+  int children = 0;
 
   // G list
   int ng = 0;

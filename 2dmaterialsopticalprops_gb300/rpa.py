@@ -24,7 +24,9 @@ KK_OPTABS_COMPLEX, KK_SLOSS_REAL = 1, 2
 
 EXPORTS = ["rpa_create", "rpa_destroy", "rpa_last_error", "rpa_set_gvectors", "rpa_set_symmetry",
            "rpa_load_basis", "rpa_kmap", "rpa_set_q", "rpa_chi0", "rpa_kk", "rpa_dyson", "rpa_gfast",
-           "rpa_init_igk", "rpa_kk_matrix", "rpa_stage_times", "rpa_chi0_stats", "rpa_dyson_noalloc", "rpa_selftest", "rpa_launch_count", "rpa_get_stream", "rpa_synchronize"]
+           "rpa_init_igk", "rpa_kk_matrix", "rpa_stage_times", "rpa_chi0_stats", "rpa_dyson_noalloc", "rpa_selftest", "rpa_launch_count", "rpa_get_stream", "rpa_synchronize",
+           "rpa_basis_info", "rpa_create_shared", "rpa_server_create", "rpa_server_submit", "rpa_server_wait",
+           "rpa_server_last_error", "rpa_server_destroy"]
 
 
 class RpaOpts(C.Structure):
@@ -37,6 +39,18 @@ class RpaChi0Args(C.Structure):
                 ("ntot_norm", C.c_int), ("domega", C.c_double), ("eta", C.c_double), ("lor_cut", C.c_double),
                 ("df_cut", C.c_double), ("T", C.c_double), ("Efermi", C.c_double), ("Vcell", C.c_double),
                 ("Gcar", C.c_double)]
+
+
+REQ_CHI0, REQ_W = 0, 1
+
+
+class RpaRequest(C.Structure):
+    _fields_ = [("kind", C.c_int), ("kk_variant", C.c_int), ("ntot", C.c_int), ("ktot", C.c_void_p),
+                ("K1", C.c_void_p), ("R1", C.c_void_p), ("K2", C.c_void_p), ("R2", C.c_void_p),
+                ("iG0", C.c_void_p), ("q", C.c_double * 3), ("nlf", C.c_int), ("ilf", C.c_void_p),
+                ("parG", C.c_void_p), ("args", RpaChi0Args), ("c0", C.c_double), ("eps", C.c_double),
+                ("S0_out", C.c_void_p), ("Qeff_out", C.c_void_p), ("chi0_out", C.c_void_p),
+                ("WT_out", C.c_void_p), ("head_out", C.c_void_p)]
 
 
 class RpaError(RuntimeError):
@@ -79,7 +93,17 @@ def load_library(path: str = LIB_PATH):
     L.rpa_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.rpa_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.rpa_synchronize.argtypes = [vp]
+    L.rpa_basis_info.argtypes = [vp, vp]
+    L.rpa_create_shared.argtypes = [C.POINTER(vp), vp]
+    L.rpa_server_create.argtypes = [C.POINTER(vp), vp, ip, dp]
+    L.rpa_server_submit.argtypes = [vp, C.POINTER(RpaRequest), C.POINTER(C.c_longlong)]
+    L.rpa_server_wait.argtypes = [vp, C.c_longlong, vp]
+    L.rpa_server_last_error.argtypes = [vp]
+    L.rpa_server_destroy.argtypes = [vp]
     for name in EXPORTS:
+        if name == "rpa_server_last_error":
+            L.rpa_server_last_error.restype = C.c_char_p
+            continue
         if name != "rpa_last_error":
             getattr(L, name).restype = C.c_int
     _lib = L
@@ -264,6 +288,99 @@ class Context:
 
     def synchronize(self):
         self._chk(self.L.rpa_synchronize(self.h))
+
+
+def shared_context(parent: Context) -> Context:
+    """A Context that uses parent's resident G list, symmetry and basis
+    (rpa_create_shared) with its own q, buffers and stream."""
+    c = Context.__new__(Context)
+    c.L = parent.L
+    c.h = C.c_void_p()
+    rc = c.L.rpa_create_shared(C.byref(c.h), parent.h)
+    if rc != RPA_OK:
+        raise RpaError(rc, c.L.rpa_last_error(parent.h).decode())
+    c.precision, c.nlf, c.no, c.mode = parent.precision, 0, 0, None
+    c.sys = getattr(parent, "sys", None)
+    return c
+
+
+class Server:
+    """rpa_server: requests of any q, local-field set and frequency grid on
+    one resident basis, run by nslots shared contexts with continuous
+    batching.  submit() returns an id; wait(id) returns the outputs and
+    (latency, queue, service) seconds."""
+
+    def __init__(self, parent: Context, nslots: int, mem_bytes: float):
+        self.L = parent.L
+        self.parent = parent
+        self.h = C.c_void_p()
+        rc = self.L.rpa_server_create(C.byref(self.h), parent.h, nslots, float(mem_bytes))
+        if rc != RPA_OK:
+            raise RpaError(rc, "rpa_server_create failed")
+        self.live = {}
+
+    def submit(self, *, kind: int, kmap: dict, ilf, parG, args: dict, mode: int, kk_variant: int,
+               c0: float = 0.0, eps: float = 1e-4, want_s0: bool = False, want_chi0: bool = True,
+               want_wt: bool = False, want_head: bool = True) -> int:
+        keep = {}
+
+        def arr(x, dt):
+            a = np.ascontiguousarray(x, dtype=dt)
+            keep[id(a)] = a
+            return a
+
+        ktot = arr(kmap["ktot"], np.float64)
+        ints = [arr(kmap[k], np.int32) for k in ("K1", "R1", "K2", "R2", "iG0")]
+        ilf_a = arr(ilf, np.int32)
+        par_a = arr(parG, np.int32)
+        nlf, no = ilf_a.size, int(args["no"])
+        a = dict(args)
+        pol = POL[a.pop("pol", "xx")]
+        ca = RpaChi0Args(mode=mode, pol=pol, **{k: v for k, v in a.items()})
+        outs = {}
+        if want_s0:
+            outs["S0"] = (np.zeros((nlf, nlf, 2 * no + 1), dtype=np.complex128) if mode == MODE_CURRENT
+                          else np.zeros((nlf, nlf, no), dtype=np.float64))
+        if want_chi0:
+            outs["chi0"] = np.zeros((nlf, nlf, no - 1), dtype=np.complex128)
+        if kind == REQ_W and want_wt:
+            outs["WT"] = np.zeros((nlf, nlf, no - 1), dtype=np.complex128)
+        if kind == REQ_W and want_head:
+            outs["head"] = np.zeros(no - 1, dtype=np.complex128)
+        r = RpaRequest(kind=kind, kk_variant=kk_variant, ntot=ktot.shape[0], ktot=_p(ktot),
+                       K1=_p(ints[0]), R1=_p(ints[1]), K2=_p(ints[2]), R2=_p(ints[3]), iG0=_p(ints[4]),
+                       nlf=nlf, ilf=_p(ilf_a), parG=_p(par_a), args=ca, c0=c0, eps=eps,
+                       S0_out=_p(outs.get("S0")), Qeff_out=None, chi0_out=_p(outs.get("chi0")),
+                       WT_out=_p(outs.get("WT")), head_out=_p(outs.get("head")))
+        for i in range(3):
+            r.q[i] = float(kmap["q"][i])
+        rid = C.c_longlong()
+        rc = self.L.rpa_server_submit(self.h, C.byref(r), C.byref(rid))
+        if rc != RPA_OK:
+            raise RpaError(rc, "rpa_server_submit failed")
+        self.live[rid.value] = (keep, outs, r)
+        return rid.value
+
+    def wait(self, rid: int):
+        t = np.zeros(3)
+        rc = self.L.rpa_server_wait(self.h, rid, _p(t))
+        keep, outs, _ = self.live.pop(rid)
+        if rc != RPA_OK:
+            raise RpaError(rc, self.L.rpa_server_last_error(self.h).decode())
+        return outs, tuple(t.tolist())
+
+    def close(self):
+        if self.h:
+            rc = self.L.rpa_server_destroy(self.h)
+            self.h = C.c_void_p()
+            if rc != RPA_OK:
+                raise RpaError(rc, "rpa_server_destroy failed")
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def sloss_args(s) -> dict:

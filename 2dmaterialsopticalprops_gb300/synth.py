@@ -363,6 +363,40 @@ def build(cfg: SynthConfig, coeff_only=None, coeff_out: np.ndarray | None = None
     return sysd
 
 
+def q_kmap(s: System, steps: int) -> dict:
+    """K+Q bookkeeping of the commensurate q = steps * b1 / nk (Gamma-M) on the
+    Gamma-centred grid of a system built with q_steps: the basis is unchanged,
+    only K2 and iG0 move.  Returns rpa_kmap / rpa_set_q inputs."""
+    nk = s.cfg.nk
+    if s.cfg.q_steps is None:
+        raise ValueError("q_kmap needs a system on a commensurate grid (q_steps)")
+    b = s.KC.T
+    ii, jj = np.meshgrid(np.arange(nk), np.arange(nk), indexing="ij")
+    ii, jj = ii.ravel(), jj.ravel()
+    i2 = (ii + steps) % nk
+    g0 = (ii + steps) // nk
+    mil_index = {tuple(m): i + 1 for i, m in enumerate(s.miller.tolist())}
+    return dict(q=steps * b[0] / nk, ktot=s.ktot, K1=s.K1, R1=s.R1, R2=s.R2,
+                K2=(i2 * nk + jj + 1).astype(np.int32),
+                iG0=np.array([mil_index[(int(g), 0, 0)] for g in g0], dtype=np.int32))
+
+
+def local_fields(s: System, q: np.ndarray, gcut2: float, lf: str = "xyz", nmax: int | None = None):
+    """Local fields of a q-point as genGlf chooses them: the G vectors (all, or
+    only G_par = 0 for lf='z') with |q + G|^2 <= gcut2 (2pi/a0 units), in
+    G-list order, at most nmax.  Returns (ilf 1-based, parG)."""
+    qg = s.G + np.asarray(q)[None, :]
+    ok = np.einsum("ij,ij->i", qg, qg) <= gcut2
+    if lf == "z":
+        ok &= (s.miller[:, 0] == 0) & (s.miller[:, 1] == 0)
+    sel = np.nonzero(ok)[0]
+    if nmax is not None:
+        sel = sel[:nmax]
+    ilf = (sel + 1).astype(np.int32)
+    parG = np.where(s.miller[sel, 2] % 2 == 0, 1, -1).astype(np.int32)
+    return ilf, parG
+
+
 # Named workloads -------------------------------------------------------------
 def config_small(**kw) -> SynthConfig:
     """A few-second oracle case with the C1 shapes scaled down."""

@@ -206,6 +206,73 @@ def cpu_sample(cfg_name: str, q_steps: int, budget_s: float):
 
 
 # ---------------------------------------------------------------------------
+def serving_run(n_req: int = 32, rate: float = 200.0, nslots: int = 4, mem_gb: float = 40.0, seed: int = 5):
+    """Request loop on a resident grid60 basis (mixed path): seeded Poisson
+    arrivals of W (loss-function) and chi0 (Optabs xx) requests with q of
+    1-15 grid steps along Gamma-M, NGloc 19-91 and nw 200-1000, served by
+    nslots shared contexts with continuous batching.  Latency = submission to
+    completion (server clock)."""
+    import threading
+    rpa, synth = pkg("rpa"), pkg("synth")
+    s = synth.build(config_of("grid60", 1))
+    parent = rpa.Context(precision=rpa.PREC_MIXED)
+    parent.load_system(s)
+    rng = np.random.default_rng(seed)
+
+    def make(i):
+        steps = int(rng.integers(1, 16))
+        km = synth.q_kmap(s, steps)
+        nlf = int(rng.integers(19, 92))
+        ilf, par = synth.local_fields(s, km["q"], 1e9, lf="z", nmax=nlf)
+        no = int(rng.integers(200, 1001))
+        domega = s.domega * (s.no - 1) / (no - 1)
+        if i % 2 == 0:
+            args = dict(no=no, domega=domega, eta=s.eta, Vcell=s.Vcell, Gcar=s.Gcar, nocc=s.nocc)
+            return dict(kind=rpa.REQ_W, kmap=km, ilf=ilf, parG=par, args=args, mode=rpa.MODE_CHARGE,
+                        kk_variant=rpa.KK_SLOSS_REAL, c0=s.c0, eps=s.cfg.eps), (ilf.size, no, "W")
+        a = rpa.optabs_args(s, "xx")
+        a.update(no=no, domega=domega)
+        return dict(kind=rpa.REQ_CHI0, kmap=km, ilf=ilf, parG=par, args=a, mode=rpa.MODE_CURRENT,
+                    kk_variant=rpa.KK_OPTABS_COMPLEX), (ilf.size, no, "chi")
+
+    reqs = [make(i) for i in range(n_req + 4)]
+    srv = rpa.Server(parent, nslots=nslots, mem_bytes=mem_gb * 1e9)
+    for r, _ in reqs[:4]:  # warm-up: device buffers of the slots reach their sizes
+        srv.wait(srv.submit(**r))
+    reqs = reqs[4:]
+    gaps = rng.exponential(1.0 / rate, size=n_req)
+    ids = [None] * n_req
+    t0 = time.perf_counter()
+
+    def feeder():
+        t = t0
+        for i, ((r, _), g) in enumerate(zip(reqs, gaps)):
+            t += g
+            d = t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            ids[i] = srv.submit(**r)
+
+    th = threading.Thread(target=feeder)
+    th.start()
+    th.join()
+    res = [srv.wait(i)[1] for i in ids]
+    t_end = time.perf_counter()
+    srv.close()
+    parent.close()
+    lat = np.array([r[0] for r in res])
+    queue = np.array([r[1] for r in res])
+    serv = np.array([r[2] for r in res])
+    return {"workload": f"grid60 basis resident (mixed path); {n_req} requests, Poisson arrivals at {rate:g}/s "
+                        f"(seed {seed}): W (loss) and chi0 (Optabs xx) alternating, q 1-15 grid steps along "
+                        f"Gamma-M, NGloc 19-91, nw 200-1000; {nslots} slots, {mem_gb:g} GB admission budget",
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "mean_queue_s": float(queue.mean()), "mean_service_s": float(serv.mean()),
+            "throughput_req_s": n_req / (t_end - t0), "n_requests": n_req, "slots": nslots,
+            "ngloc_range": [int(min(r[1][0] for r in reqs)), int(max(r[1][0] for r in reqs))],
+            "nw_range": [int(min(r[1][1] for r in reqs)), int(max(r[1][1] for r in reqs))]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -218,6 +285,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison step")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-serve", action="store_true", help="skip the request-loop (serving) measurement")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -393,6 +461,10 @@ def main():
         cpu = {"value": 1.0 / tq, "unit": "q-spectra/s", "cores": cores, "kind": "port", "sample": sample,
                "parts_s": {k: round(v, 3) for k, v in parts.items()}}
 
+    serving = None
+    if rank == 0 and not args.no_serve and args.precision == "mixed":
+        serving = serving_run()
+
     if rank == 0:
         cfgd = workload_desc(s, args.config)
         cfgd.update({"l2": "inputs larger than L2 (basis %.1f GB resident)" % (s.coeff.nbytes / 1e9),
@@ -404,7 +476,7 @@ def main():
                 "data": "synthetic (seeded QE-layout Bloch basis)", "config": cfgd, "clocks": clocks,
                 "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "stage_ms_per_step": {k: round(v, 3) for k, v in sm.items()},
-                "fp64_gpu": fp64,
+                "fp64_gpu": fp64, "serving": serving,
                 "vertex_tflops": (work["vertex_flops"] / (sm["vertices"] / 1e3) / 1e12) if sm["vertices"] else None}
         print(json.dumps(line), flush=True)
     if ctx is not None:

@@ -219,6 +219,65 @@ int rpa_get_stream(const rpa_ctx* ctx, void** stream);
 /* Blocks until the context stream is idle. */
 int rpa_synchronize(rpa_ctx* ctx);
 
+/* Dimensions of the loaded basis: out4 = {nks, nbnd, npwx, ng} (zeros before
+ * rpa_load_basis / rpa_set_gvectors). */
+int rpa_basis_info(const rpa_ctx* ctx, int* out4);
+
+/* ---- Several q-points on one resident basis --------------------------------
+ * No counterpart in the reference: its drivers compute one q-point per process
+ * and reread the wavefunctions each time. */
+
+/* A context on parent's device that uses parent's G list, symmetry and basis
+ * on the device without copying them, and has its own k map, q, per-call
+ * buffers, results and stream.  Shared contexts driven from different host
+ * threads run their kernels concurrently.  parent must be a context that
+ * loaded them itself; while shared contexts exist neither side may call
+ * rpa_set_gvectors / rpa_set_symmetry / rpa_load_basis (RPA_ESTATE) and
+ * rpa_destroy(parent) fails with RPA_ESTATE. */
+int rpa_create_shared(rpa_ctx** out, rpa_ctx* parent);
+
+/* Request loop with continuous batching.  A server owns nslots shared contexts
+ * of parent and one worker thread each.  Submitted requests wait in a FIFO
+ * queue; the head starts as soon as a worker is free and its device footprint
+ * (about NGloc^2 x frequency rows complex values for S0, chi0 and, for W, the
+ * Dyson buffers, plus the vertex rows) fits in mem_bytes next to the requests
+ * already running; a request larger than mem_bytes runs alone.  Requests that
+ * arrive while others run start without waiting for them to finish and their
+ * kernels overlap on the GPU. */
+typedef struct rpa_server rpa_server;
+enum { RPA_REQ_CHI0 = 0, RPA_REQ_W = 1 };
+typedef struct rpa_request {
+  int kind;        /* RPA_REQ_CHI0: S0 (+ Qeff) and chi0 by KK; RPA_REQ_W: also the
+                      Dyson solve, W and eps^-1_{11} (loss function) */
+  int kk_variant;  /* RPA_KK_* */
+  int ntot;        /* FBZ points and their maps, as rpa_kmap */
+  const double* ktot;
+  const int *K1, *R1, *K2, *R2, *iG0;
+  double q[3];     /* as rpa_set_q */
+  int nlf;
+  const int* ilf;
+  const int* parG;
+  rpa_chi0_args args;
+  double c0, eps;  /* as rpa_dyson (RPA_REQ_W) */
+  double* S0_out;  /* host outputs as rpa_chi0 / rpa_kk / rpa_dyson; NULL = not wanted */
+  double* Qeff_out;
+  double* chi0_out;
+  double* WT_out;
+  double* head_out;
+} rpa_request;
+/* Every array a request points to must stay valid until rpa_server_wait
+ * returns for it. */
+int rpa_server_create(rpa_server** out, rpa_ctx* parent, int nslots, double mem_bytes);
+int rpa_server_submit(rpa_server* srv, const rpa_request* req, long long* id);
+/* Blocks until request id is done; returns its status.  times3 (may be NULL):
+ * [0] latency from submission to completion, [1] time in the queue,
+ * [2] service time, seconds. */
+int rpa_server_wait(rpa_server* srv, long long id, double* times3);
+/* Message of the last failed request returned by rpa_server_wait. */
+const char* rpa_server_last_error(const rpa_server* srv);
+/* Finishes the queued requests, stops the workers, destroys the contexts. */
+int rpa_server_destroy(rpa_server* srv);
+
 #ifdef __cplusplus
 }
 #endif

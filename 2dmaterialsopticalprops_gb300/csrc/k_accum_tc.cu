@@ -51,6 +51,9 @@ struct AccTcCtx {
   float scaleB;         // power of two folded into M2
   float inv_scale;      // 1 / (scaleA scaleB)
   float inv_src;        // 1 / (scale of the pre-split A-side tile)
+  int nht;              // 96-row tiles of the local fields
+  long long a_chunk, a_tile;  // A-side source: bytes per chunk and per tile
+  int a_lo;             // A-side source: offset of the lo rows
   int n_rows;           // rows of M / M2 (n_inter rounded up to a multiple of 32, zero padded)
   int seg;              // chunks accumulated in one TMEM segment before it is read back
 };
@@ -460,14 +463,14 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
 }
 
-template <int NIO, bool CPLX, bool TWO>
+template <int NIO, bool CPLX, bool SEPA>
 struct WsCfg {
   static constexpr uint32_t A_BYTES = TC_GA * 128;                  // one 16-bit A tile
   static constexpr uint32_t BROWS = CPLX ? 2 * TC_GB : TC_GB;       // [B1; B2] or B1
   static constexpr uint32_t BHALF = BROWS * 128;                    // hi (or lo) rows of B
   static constexpr uint32_t BSRC = 2 * BHALF;                       // hi, then lo
   static constexpr uint32_t ASRC = 2 * TC_TILE;                     // separate A-side tiles (M2 != M)
-  static constexpr uint32_t REC_OFF = BSRC + (TWO ? ASRC : 0);
+  static constexpr uint32_t REC_OFF = BSRC + (SEPA ? ASRC : 0);
   static constexpr uint32_t DATA = (REC_OFF + TC_TT * sizeof(Trans) + 1023) / 1024 * 1024;
   static constexpr uint32_t FORMED = NIO * 2 * A_BYTES;             // (Ah, Al) x NIO
   static constexpr int S0 = (int)((232448 - 2 * FORMED - 1024 - 3072) / DATA);
@@ -475,15 +478,17 @@ struct WsCfg {
   static constexpr size_t SMEM = (size_t)S * DATA + 2 * FORMED + 1024;
 };
 
-template <int NIO, bool CPLX, bool TWO>
+template <int NIO, bool CPLX, bool SEPA>
 __global__ void __launch_bounds__(WS_THREADS, 1)
     k_accum_ws(AccTcCtx A, const unsigned char* __restrict__ tiles, const unsigned char* __restrict__ tilesA) {
-  using Cfg = WsCfg<NIO, CPLX, TWO>;
+  using Cfg = WsCfg<NIO, CPLX, SEPA>;
   constexpr int S = Cfg::S;
   constexpr uint32_t DATA = Cfg::DATA, FORMED = Cfg::FORMED, A_BYTES = Cfg::A_BYTES;
-  constexpr uint32_t DCOLS = 192, NCOL = 512;
+  constexpr uint32_t DCOLS = (CPLX ? 2 : 1) * NIO * TC_GB;  // accumulator columns per TMEM buffer
+  constexpr int CW = DCOLS / 3;                                // columns per formation thread
+  constexpr uint32_t NCOL = 2 * DCOLS <= 256 ? 256 : 512;
   static_assert(S >= 2, "shared-memory ring too shallow");
-  static_assert((CPLX ? 2 * NIO : NIO) * TC_GB == (int)DCOLS, "accumulator layout");
+  static_assert(CW % 32 == 0, "accumulator layout");
 
   extern __shared__ unsigned char smraw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
@@ -496,7 +501,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int r0 = blockIdx.x * NIO;
-  const int nrowA = A.nlf;  // every local field sits in the one G tile
+  const int gi = blockIdx.y, gj = blockIdx.z;  // G tile (A rows), G' tile (B rows), 96 local fields each
+  const int nrowA = min(TC_GB, A.nlf - gi * TC_GB);
   const size_t np = (size_t)A.nlf * A.nlf;
 
   if (warp == 0) {
@@ -546,7 +552,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
     asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(WS_REG_PROD));
     if (warp == WS_SIMT_WARPS + 2 && lane == 0) {
       // ---------------- loads: a stage is refilled as soon as it is released ----------------
-      constexpr uint32_t bytes = Cfg::BSRC + (TWO ? Cfg::ASRC : 0) + TC_TT * sizeof(Trans);
+      constexpr uint32_t bytes = Cfg::BSRC + (SEPA ? Cfg::ASRC : 0) + TC_TT * sizeof(Trans);
       int loaded = 0;
       for (; loaded < nchunks && ok; ++loaded) {
         if (loaded >= S) ok = ws_wait(&dfree[loaded % S], ((loaded / S) - 1) & 1, &abort_flag);
@@ -555,8 +561,12 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
         uint64_t* b = &dfull[loaded % S];
         tc::mbar_arrive_expect_tx(b, bytes);
         const int pc = phys(loaded);
-        tc::bulk_g2s(st, tiles + (size_t)(chunk0 + pc) * Cfg::BSRC, Cfg::BSRC, b);
-        if (TWO) tc::bulk_g2s(st + Cfg::BSRC, tilesA + (size_t)(chunk0 + pc) * Cfg::ASRC, Cfg::ASRC, b);
+        tc::bulk_g2s(st, tiles + ((size_t)(chunk0 + pc) * A.nht + gj) * Cfg::BSRC, Cfg::BSRC, b);
+        if (SEPA) {
+          const unsigned char* as = tilesA + (size_t)(chunk0 + pc) * A.a_chunk + (size_t)gi * A.a_tile;
+          tc::bulk_g2s(st + Cfg::BSRC, as, TC_TILE, b);
+          tc::bulk_g2s(st + Cfg::BSRC + TC_TILE, as + A.a_lo, TC_TILE, b);
+        }
         tc::bulk_g2s(st + Cfg::REC_OFF, A.rec + ta + (size_t)pc * TC_TT, TC_TT * sizeof(Trans), b);
       }
       if (!ok) {
@@ -646,17 +656,18 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
   } else {
     // ---------------- read-back, weights, A formation ----------------
     asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(WS_REG_SIMT));
-    // accumulator slice: TMEM lane quadrant wq, columns cg * 64 .. cg * 64 + 63
+    // accumulator slice: TMEM lane quadrant wq, columns cg * CW .. cg * CW + CW - 1
     const int wq = warp & 3, cg = warp >> 2;
-    const int grow = wq * 32 + lane;  // G
-    float acc[64];
+    const int grow = wq * 32 + lane;       // row of the G tile
+    const int gG = gi * TC_GB + grow;      // G
+    float acc[CW];
 #pragma unroll
-    for (int i = 0; i < 64; ++i) acc[i] = 0.f;
+    for (int i = 0; i < CW; ++i) acc[i] = 0.f;
     int consumed = 0;
     auto consume = [&](int buf) {
-      const uint32_t a0 = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)(buf * DCOLS + cg * 64);
+      const uint32_t a0 = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)(buf * DCOLS + cg * CW);
 #pragma unroll
-      for (int p = 0; p < 2; ++p) {
+      for (int p = 0; p < CW / 32; ++p) {
         float v[32];
         tc::tmem_ld32(a0 + 32 * p, v);
         tc::tmem_ld_wait();
@@ -667,18 +678,18 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
     // column col of the accumulator = (part, G'): part = Re / Im (complex) or
     // the frequency row of the pair (real)
     auto flush = [&]() {
-      if (grow < A.nlf) {
+      if (grow < TC_GB && gG < A.nlf) {
         const int ncomp = CPLX ? 2 : 1;
 #pragma unroll
-        for (int j0 = 0; j0 < 64; j0 += 4) {
+        for (int j0 = 0; j0 < CW; j0 += 4) {
           float2* dst[4];
           float2 old[4];
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            const int col = cg * 64 + j0 + j, part = col / TC_GB, gp = col - part * TC_GB;
+            const int col = cg * CW + j0 + j, part = col / TC_GB, gp = gj * TC_GB + col - part * TC_GB;
             const int io = CPLX ? r0 : r0 + part, comp = CPLX ? part : 0;
             dst[j] = (gp < A.nlf && io < A.nw)
-                         ? A.Sdf + ((size_t)io * np + (size_t)grow + (size_t)A.nlf * gp) * ncomp + comp
+                         ? A.Sdf + ((size_t)io * np + (size_t)gG + (size_t)A.nlf * gp) * ncomp + comp
                          : nullptr;
             if (dst[j]) old[j] = *dst[j];
           }
@@ -688,7 +699,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
         }
       }
 #pragma unroll
-      for (int j = 0; j < 64; ++j) acc[j] = 0.f;
+      for (int j = 0; j < CW; ++j) acc[j] = 0.f;
     };
     for (int c = 0; c < nchunks; ++c) {
       ok = ws_wait(&dfull[c % S], (c / S) & 1, &abort_flag);
@@ -711,8 +722,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
       if (!ok) break;
       // A tiles: A = w * (hi + lo) of the staged vertex tile (B1 rows, or the
       // separate A-side tile), re-split
-      const unsigned char* srch = st + (TWO ? Cfg::BSRC : 0);
-      const unsigned char* srcl = srch + (TWO ? TC_TILE : Cfg::BHALF);
+      const unsigned char* srch = st + (SEPA ? Cfg::BSRC : 0);
+      const unsigned char* srcl = srch + (SEPA ? TC_TILE : Cfg::BHALF);
 #pragma unroll 2
       for (int e = tid; e < nrowA * 8; e += WS_SIMT) {
         const int row = e >> 3, ch = e & 7;
@@ -770,26 +781,29 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
   if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
 }
 
-// Pre-split B operand of the warp-specialised kernel, per chunk: the hi rows,
-// then the lo rows; rows 0-95 = [Re b | Im b] (B1), rows 96-191 = [-Im b | Re b]
-// (B2, complex S0 only), b = scale * M(G'), rows >= nlf zero.
+// Pre-split B operand of the warp-specialised kernel, per chunk and 96-row
+// tile of G': the hi rows, then the lo rows; rows 0-95 = [Re b | Im b] (B1),
+// rows 96-191 = [-Im b | Re b] (B2, complex S0 only), b = scale * M(G'),
+// rows with G' >= nlf zero.
 template <bool CPLX>
-__global__ void k_presplit_ws(const float2* __restrict__ M, int nlf, int nchunks, float scale,
+__global__ void k_presplit_ws(const float2* __restrict__ M, int nlf, int nchunks, int nht, float scale,
                               unsigned char* __restrict__ tiles) {
   constexpr uint32_t BROWS = CPLX ? 2 * TC_GB : TC_GB, BHALF = BROWS * 128;
-  const long long ntask = (long long)nchunks * TC_GB * 4;
+  const long long ntask = (long long)nchunks * nht * TC_GB * 4;
   for (long long task = blockIdx.x * (long long)blockDim.x + threadIdx.x; task < ntask;
        task += (long long)gridDim.x * blockDim.x) {
-    const int ch = (int)(task / (TC_GB * 4)), rem = (int)(task % (TC_GB * 4));
-    const int row = rem % TC_GB, grp = rem / TC_GB;
+    const long long cht = task / (TC_GB * 4);
+    const int rem = (int)(task % (TC_GB * 4));
+    const int ch = (int)(cht / nht), ht = (int)(cht % nht);
+    const int row = rem % TC_GB, grp = rem / TC_GB, g = ht * TC_GB + row;
     float re[8], im[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      float2 m = row < nlf ? M[((size_t)ch * TC_TT + grp * 8 + q) * nlf + row] : make_float2(0.f, 0.f);
+      float2 m = g < nlf ? M[((size_t)ch * TC_TT + grp * 8 + q) * nlf + g] : make_float2(0.f, 0.f);
       re[q] = m.x * scale;
       im[q] = m.y * scale;
     }
-    unsigned char* t = tiles + (size_t)ch * 2 * BHALF;
+    unsigned char* t = tiles + (size_t)cht * 2 * BHALF;
     uint4 rh, rl, ih, il;
     split8<true>(re, rh, rl);
     split8<true>(im, ih, il);
@@ -836,20 +850,21 @@ static int launch_tc(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char*
   return RPA_OK;
 }
 
-template <int NIO, bool CPLX, bool TWO>
+template <int NIO, bool CPLX, bool SEPA>
 static int launch_ws(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char* tiles, const unsigned char* tilesA) {
-  using Cfg = WsCfg<NIO, CPLX, TWO>;
-  auto kern = k_accum_ws<NIO, CPLX, TWO>;
+  using Cfg = WsCfg<NIO, CPLX, SEPA>;
+  auto kern = k_accum_ws<NIO, CPLX, SEPA>;
   RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM));
-  kern<<<(nw + NIO - 1) / NIO, WS_THREADS, Cfg::SMEM, c->stream>>>(A, tiles, tilesA);
+  dim3 grid((nw + NIO - 1) / NIO, A.nht, A.nht);
+  kern<<<grid, WS_THREADS, Cfg::SMEM, c->stream>>>(A, tiles, tilesA);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
   return RPA_OK;
 }
 
 template <bool CPLX>
-static int launch_presplit_ws(rpa_ctx* c, const float2* M, int nchunks, float scale, unsigned char* tiles) {
-  k_presplit_ws<CPLX><<<4096, 256, 0, c->stream>>>(M, c->nlf, nchunks, scale, tiles);
+static int launch_presplit_ws(rpa_ctx* c, const float2* M, int nchunks, int nht, float scale, unsigned char* tiles) {
+  k_presplit_ws<CPLX><<<4096, 256, 0, c->stream>>>(M, c->nlf, nchunks, nht, scale, tiles);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
   return RPA_OK;
@@ -896,26 +911,36 @@ int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const fl
   const int nch = A.n_rows / TC_TT + 1;  // one spare chunk for the last prefetch
   const int nht = (c->nlf + TC_GB - 1) / TC_GB;
   const bool two = Mf2 != Mf;
-  if (f16 && c->nlf <= TC_GB && A.seg == 1) {
-    // warp-specialised kernel: the A side reads the B1 rows when M2 = M, else
-    // its own pre-split copy
-    const size_t tbytes = (size_t)nch * (cplx ? 4 : 2) * TC_TILE;
-    RPA_TRY(ensure(c, c->d_tiles, tbytes));
+  if (f16 && A.seg == 1) {
+    // warp-specialised kernel on 96-row tiles of G and G'.  The A side reads
+    // the B1 rows of the same stage when there is one tile and M2 = M, else
+    // its own pre-split source tile (the B tiles of tile gi, or a pre-split
+    // copy of M for the yz / zy pair).
+    const size_t bsrc = (size_t)(cplx ? 4 : 2) * TC_TILE;
+    RPA_TRY(ensure(c, c->d_tiles, (size_t)nch * nht * bsrc));
     unsigned char* tiles = c->d_tiles.as<unsigned char>();
-    RPA_TRY(cplx ? launch_presplit_ws<true>(c, Mf2, nch, A.scaleB, tiles)
-                 : launch_presplit_ws<false>(c, Mf2, nch, A.scaleB, tiles));
+    RPA_TRY(cplx ? launch_presplit_ws<true>(c, Mf2, nch, nht, A.scaleB, tiles)
+                 : launch_presplit_ws<false>(c, Mf2, nch, nht, A.scaleB, tiles));
     const unsigned char* tilesA = tiles;
+    A.nht = nht;
     A.inv_src = 1.0f / A.scaleB;
+    A.a_chunk = (long long)nht * bsrc;
+    A.a_tile = (long long)bsrc;
+    A.a_lo = (cplx ? 2 : 1) * TC_TILE;
     if (two) {
       const double amS = (double)amaxM * 1.5;
       const float sM = amS > 0 ? (float)(16384.0 / pow2_floor(amS)) : 1.0f;
-      RPA_TRY(ensure(c, c->d_tilesA, (size_t)nch * 2 * TC_TILE));
+      RPA_TRY(ensure(c, c->d_tilesA, (size_t)nch * nht * 2 * TC_TILE));
       RPA_TRY(launch_presplit<true, false>(c, Mf, nch, sM, c->d_tilesA.as<unsigned char>()));
       tilesA = c->d_tilesA.as<unsigned char>();
       A.inv_src = 1.0f / sM;
+      A.a_chunk = (long long)nht * 2 * TC_TILE;
+      A.a_tile = 2 * TC_TILE;
+      A.a_lo = TC_TILE;
     }
-    if (cplx) return two ? launch_ws<1, true, true>(c, A, P.nw, tiles, tilesA) : launch_ws<1, true, false>(c, A, P.nw, tiles, tilesA);
-    return launch_ws<2, false, false>(c, A, P.nw, tiles, tilesA);
+    const bool sepa = two || nht > 1;
+    if (cplx) return sepa ? launch_ws<1, true, true>(c, A, P.nw, tiles, tilesA) : launch_ws<1, true, false>(c, A, P.nw, tiles, tilesA);
+    return sepa ? launch_ws<1, false, true>(c, A, P.nw, tiles, tilesA) : launch_ws<2, false, false>(c, A, P.nw, tiles, tilesA);
   }
   const size_t tbytes = (size_t)nch * nht * (cplx ? 4 : 2) * TC_TILE;
   RPA_TRY(ensure(c, c->d_tiles, tbytes));

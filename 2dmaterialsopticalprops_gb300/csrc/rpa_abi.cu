@@ -276,17 +276,21 @@ int rpa_create(rpa_ctx** out, const rpa_opts* opts) {
 // A context on the parent's device that shares the parent's G list, symmetry
 // and basis on the device (no copy) and owns its own k map, q, per-call buffers,
 // results and stream, so that several q-points run at once on one resident basis.
-int rpa_create_shared(rpa_ctx** out, rpa_ctx* parent) {
+int rpa_create_shared(rpa_ctx** out, rpa_ctx* parent, int precision) {
   if (!out || !parent) return fail(nullptr, RPA_EINVAL, "rpa_create_shared: NULL argument");
   *out = nullptr;
   if (parent->parent) return fail(parent, RPA_EINVAL, "rpa_create_shared: parent is itself a shared context");
   if (parent->nks == 0 || parent->ng == 0)
     return fail(parent, RPA_ESTATE, "rpa_create_shared: parent has no G vectors or basis loaded");
+  if (precision != -1 && precision != RPA_PREC_FP64 && precision != RPA_PREC_MIXED)
+    return fail(parent, RPA_EINVAL, "rpa_create_shared: unknown precision %d", precision);
+  if (precision == RPA_PREC_MIXED && parent->precision != RPA_PREC_MIXED)
+    return fail(parent, RPA_ESTATE, "rpa_create_shared: the mixed path needs a parent created with RPA_PREC_MIXED");
   cudaError_t e = cudaSetDevice(parent->device);
   if (e != cudaSuccess) return fail(parent, RPA_ECUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
   rpa_ctx* c = new rpa_ctx();
   c->device = parent->device;
-  c->precision = parent->precision;
+  c->precision = precision == -1 ? parent->precision : precision;
   c->verbose = parent->verbose;
   c->split_f16 = parent->split_f16;
   c->tc_seg = parent->tc_seg;

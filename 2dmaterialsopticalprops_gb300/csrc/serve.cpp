@@ -135,7 +135,7 @@ int rpa_server_create(rpa_server** out, rpa_ctx* parent, int nslots, double mem_
   s->nbnd = info[1];
   for (int i = 0; i < nslots; ++i) {
     rpa_ctx* c = nullptr;
-    const int rc = rpa_create_shared(&c, parent);
+    const int rc = rpa_create_shared(&c, parent, -1);
     if (rc != RPA_OK) {
       for (rpa_ctx* d : s->slots) rpa_destroy(d);
       delete s;

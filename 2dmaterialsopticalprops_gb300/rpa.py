@@ -94,7 +94,7 @@ def load_library(path: str = LIB_PATH):
     L.rpa_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.rpa_synchronize.argtypes = [vp]
     L.rpa_basis_info.argtypes = [vp, vp]
-    L.rpa_create_shared.argtypes = [C.POINTER(vp), vp]
+    L.rpa_create_shared.argtypes = [C.POINTER(vp), vp, ip]
     L.rpa_server_create.argtypes = [C.POINTER(vp), vp, ip, dp]
     L.rpa_server_submit.argtypes = [vp, C.POINTER(RpaRequest), C.POINTER(C.c_longlong)]
     L.rpa_server_wait.argtypes = [vp, C.c_longlong, vp]
@@ -290,16 +290,18 @@ class Context:
         self._chk(self.L.rpa_synchronize(self.h))
 
 
-def shared_context(parent: Context) -> Context:
+def shared_context(parent: Context, precision: int | None = None) -> Context:
     """A Context that uses parent's resident G list, symmetry and basis
-    (rpa_create_shared) with its own q, buffers and stream."""
+    (rpa_create_shared) with its own q, buffers and stream; precision
+    defaults to the parent's."""
     c = Context.__new__(Context)
     c.L = parent.L
     c.h = C.c_void_p()
-    rc = c.L.rpa_create_shared(C.byref(c.h), parent.h)
+    prec = -1 if precision is None else precision
+    rc = c.L.rpa_create_shared(C.byref(c.h), parent.h, prec)
     if rc != RPA_OK:
         raise RpaError(rc, c.L.rpa_last_error(parent.h).decode())
-    c.precision, c.nlf, c.no, c.mode = parent.precision, 0, 0, None
+    c.precision, c.nlf, c.no, c.mode = parent.precision if precision is None else precision, 0, 0, None
     c.sys = getattr(parent, "sys", None)
     return c
 

@@ -363,22 +363,22 @@ def build(cfg: SynthConfig, coeff_only=None, coeff_out: np.ndarray | None = None
     return sysd
 
 
-def q_kmap(s: System, steps: int) -> dict:
-    """K+Q bookkeeping of the commensurate q = steps * b1 / nk (Gamma-M) on the
-    Gamma-centred grid of a system built with q_steps: the basis is unchanged,
-    only K2 and iG0 move.  Returns rpa_kmap / rpa_set_q inputs."""
+def q_kmap(s: System, steps: int, steps2: int = 0) -> dict:
+    """K+Q bookkeeping of the commensurate q = (steps b1 + steps2 b2) / nk on
+    the Gamma-centred grid of a system built with q_steps: the basis is
+    unchanged, only K2 and iG0 move.  Returns rpa_kmap / rpa_set_q inputs."""
     nk = s.cfg.nk
     if s.cfg.q_steps is None:
         raise ValueError("q_kmap needs a system on a commensurate grid (q_steps)")
     b = s.KC.T
     ii, jj = np.meshgrid(np.arange(nk), np.arange(nk), indexing="ij")
     ii, jj = ii.ravel(), jj.ravel()
-    i2 = (ii + steps) % nk
-    g0 = (ii + steps) // nk
+    i2, j2 = (ii + steps) % nk, (jj + steps2) % nk
+    g1, g2 = (ii + steps) // nk, (jj + steps2) // nk
     mil_index = {tuple(m): i + 1 for i, m in enumerate(s.miller.tolist())}
-    return dict(q=steps * b[0] / nk, ktot=s.ktot, K1=s.K1, R1=s.R1, R2=s.R2,
-                K2=(i2 * nk + jj + 1).astype(np.int32),
-                iG0=np.array([mil_index[(int(g), 0, 0)] for g in g0], dtype=np.int32))
+    return dict(q=(steps * b[0] + steps2 * b[1]) / nk, ktot=s.ktot, K1=s.K1, R1=s.R1, R2=s.R2,
+                K2=(i2 * nk + j2 + 1).astype(np.int32),
+                iG0=np.array([mil_index[(int(a), int(c), 0)] for a, c in zip(g1, g2)], dtype=np.int32))
 
 
 def local_fields(s: System, q: np.ndarray, gcut2: float, lf: str = "xyz", nmax: int | None = None):

@@ -273,6 +273,90 @@ def serving_run(n_req: int = 32, rate: float = 200.0, nslots: int = 4, mem_gb: f
             "nw_range": [int(min(r[1][1] for r in reqs)), int(max(r[1][1] for r in reqs))]}
 
 
+def dispersion_path(nk: int, n_q: int):
+    """n_q commensurate q-points along Gamma-M-K of the nk x nk grid, as
+    (steps along b1, steps along b2): Gamma-M is (s, 0), s = 1..nk/2, M-K is
+    (nk/2 - j, 2j), j = 1..nk/6; n_q of them evenly spaced along the path."""
+    pts = [(s_, 0) for s_ in range(1, nk // 2 + 1)] + [(nk // 2 - j, 2 * j) for j in range(1, nk // 6 + 1)]
+    idx = np.unique(np.round(np.linspace(0, len(pts) - 1, n_q)).astype(int))
+    return [pts[i] for i in idx]
+
+
+def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, fp64_sample=(0, 31, 63), no: int = 701,
+                   eta_ev: float = 0.05):
+    """64-q loss-function dispersion (W and Im eps^-1 per q) on the resident
+    grid120 basis: NGloc rising from 31 to 151 along the path, nw = 701 on
+    0-30 eV, eta = 50 meV.  All q-points are submitted at once to a server of
+    shared mixed-path contexts; a sample of q-points also runs on the plain
+    FP64 GPU path for the speed ratio and the Im eps^-1 errors."""
+    rpa, synth = pkg("rpa"), pkg("synth")
+    own = parent is None
+    if own:
+        parent = rpa.Context(precision=rpa.PREC_MIXED)
+        parent.load_system(s)
+    path = dispersion_path(s.cfg.nk, n_q)
+    n_q = len(path)
+    domega = s.domega * (s.no - 1) / (no - 1)
+    eta = eta_ev / 27.211386245988
+    reqs, info = [], []
+    for i, (a, b) in enumerate(path):
+        km = synth.q_kmap(s, a, b)
+        nlf = 31 + int(round(120 * i / max(n_q - 1, 1)))
+        ilf, par = synth.local_fields(s, km["q"], 1e9, lf="xyz", nmax=nlf)
+        args = dict(no=no, domega=domega, eta=eta, Vcell=s.Vcell, Gcar=s.Gcar, nocc=s.nocc)
+        reqs.append(dict(kind=rpa.REQ_W, kmap=km, ilf=ilf, parG=par, args=args, mode=rpa.MODE_CHARGE,
+                         kk_variant=rpa.KK_SLOSS_REAL, c0=s.c0, eps=s.cfg.eps))
+        info.append((float(np.linalg.norm(km["q"])), int(ilf.size)))
+    srv = rpa.Server(parent, nslots=nslots, mem_bytes=80e9)
+    srv.wait(srv.submit(**reqs[-1]))  # warm-up at the largest NGloc
+    t0 = time.perf_counter()
+    ids = [srv.submit(**r) for r in reqs]
+    res = [srv.wait(i) for i in ids]
+    t_mixed = time.perf_counter() - t0
+    srv.close()
+    # FP64 GPU sample: the same requests, one at a time on an FP64 shared context
+    c64 = rpa.shared_context(parent, rpa.PREC_FP64)
+    t64, tmix_one, errs = 0.0, 0.0, []
+    cm = rpa.shared_context(parent)
+    for qi in fp64_sample:
+        r = reqs[qi]
+        outs = []
+        for c in (cm, c64):
+            km = r["kmap"]
+            t = time.perf_counter()
+            c.kmap(km["ktot"], km["K1"], km["R1"], km["K2"], km["R2"], km["iG0"])
+            c.set_q(km["q"], r["ilf"], r["parG"])
+            c.chi0(rpa.MODE_CHARGE, want=False, **r["args"])
+            c.kk(rpa.KK_SLOSS_REAL, want=False)
+            _, _, head = c.dyson(r["c0"], r["eps"], want_wt=False)
+            dt = time.perf_counter() - t
+            if c is c64:
+                t64 += dt
+            else:
+                tmix_one += dt
+            outs.append(head)
+        d = np.abs(outs[0].imag - outs[1].imag)
+        errs.append({"q_index": qi, "q_2pi_over_a": info[qi][0], "ngloc": info[qi][1],
+                     "max_rel_Im_epsinv": float(d.max() / np.abs(outs[1].imag).max()),
+                     "rms_rel_Im_epsinv": float(np.sqrt((d ** 2).mean()) / np.sqrt((outs[1].imag ** 2).mean()))})
+    c64.close()
+    cm.close()
+    if own:
+        parent.close()
+    return {"workload": f"{n_q} q-points along Gamma-M-K (|q| {info[0][0]:.4f}-{info[-1][0]:.3f} 2pi/a) on the "
+                        f"grid120 basis; loss chain per q (S0, KK, FP64 Dyson, W, Im eps^-1), NGloc 31-151 rising "
+                        f"along the path, nw={no}, eta={eta_ev * 1000:.0f} meV; mixed path: all q submitted at once "
+                        f"to {nslots} shared contexts",
+            "n_q": n_q, "mixed_s": t_mixed, "value": n_q / t_mixed, "unit": "q-spectra/s",
+            "mean_service_s": float(np.mean([x[1][2] for x in res])),
+            "fp64_sample": {"q_indices": list(fp64_sample), "fp64_s": t64, "mixed_s_one_at_a_time": tmix_one,
+                            "fp64_q_spectra_s_est": len(fp64_sample) / t64,
+                            "mixed_over_fp64_same_q": t64 / tmix_one,
+                            "mixed_batched_over_fp64": (n_q / t_mixed) / (len(fp64_sample) / t64),
+                            "note": "FP64 rate from the sampled q-points (NGloc 31, 91, 151), not all 64"},
+            "errors_vs_fp64_gpu": errs}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -286,6 +370,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop (serving) measurement")
+    ap.add_argument("--dispersion", action="store_true",
+                    help="also run the 64-q loss-function dispersion on the resident basis (adds ~2 min)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -461,9 +547,11 @@ def main():
         cpu = {"value": 1.0 / tq, "unit": "q-spectra/s", "cores": cores, "kind": "port", "sample": sample,
                "parts_s": {k: round(v, 3) for k, v in parts.items()}}
 
-    serving = None
+    serving = disp = None
     if rank == 0 and not args.no_serve and args.precision == "mixed":
         serving = serving_run()
+    if rank == 0 and args.dispersion and args.precision == "mixed":
+        disp = dispersion_run(ctx, s)
 
     if rank == 0:
         cfgd = workload_desc(s, args.config)
@@ -476,7 +564,7 @@ def main():
                 "data": "synthetic (seeded QE-layout Bloch basis)", "config": cfgd, "clocks": clocks,
                 "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "stage_ms_per_step": {k: round(v, 3) for k, v in sm.items()},
-                "fp64_gpu": fp64, "serving": serving,
+                "fp64_gpu": fp64, "serving": serving, "dispersion": disp,
                 "vertex_tflops": (work["vertex_flops"] / (sm["vertices"] / 1e3) / 1e12) if sm["vertices"] else None}
         print(json.dumps(line), flush=True)
     if ctx is not None:

@@ -230,11 +230,13 @@ int rpa_basis_info(const rpa_ctx* ctx, int* out4);
 /* A context on parent's device that uses parent's G list, symmetry and basis
  * on the device without copying them, and has its own k map, q, per-call
  * buffers, results and stream.  Shared contexts driven from different host
- * threads run their kernels concurrently.  parent must be a context that
- * loaded them itself; while shared contexts exist neither side may call
- * rpa_set_gvectors / rpa_set_symmetry / rpa_load_basis (RPA_ESTATE) and
+ * threads run their kernels concurrently.  precision: RPA_PREC_FP64,
+ * RPA_PREC_MIXED (needs a parent created with RPA_PREC_MIXED, which holds the
+ * split coefficient copies) or -1 for the parent's.  parent must be a context
+ * that loaded the basis itself; while shared contexts exist neither side may
+ * call rpa_set_gvectors / rpa_set_symmetry / rpa_load_basis (RPA_ESTATE) and
  * rpa_destroy(parent) fails with RPA_ESTATE. */
-int rpa_create_shared(rpa_ctx** out, rpa_ctx* parent);
+int rpa_create_shared(rpa_ctx** out, rpa_ctx* parent, int precision);
 
 /* Request loop with continuous batching.  A server owns nslots shared contexts
  * of parent and one worker thread each.  Submitted requests wait in a FIFO

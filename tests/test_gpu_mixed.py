@@ -46,7 +46,7 @@ def test_mixed_multi_tile_nlf131(synth, rpa, orc):
     s = synth.build(synth.config_small(npw=200, nlf=131, lf="xyz", no=21))
     ctx = rpa.Context(precision=rpa.PREC_MIXED)
     ctx.load_system(s)
-    for pol in ("xx",):
+    for pol in ("xx", "yz"):
         S, _ = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, pol))
         So, _ = orc.optabs_s0(orc.Bound(s, pol=pol))
         assert rel(S, So) < TOL

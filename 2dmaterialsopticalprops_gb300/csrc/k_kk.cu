@@ -16,6 +16,8 @@
 
 namespace rpa {
 
+constexpr double KK_PI = 3.141592653589793238462643383279502884;
+
 // Kernel matrix K[(no-1) x nw] for the given variant (row-major).
 void kk_matrix(int variant, int no, double domega, std::vector<double>& K, int* nw_out) {
   if (variant == RPA_KK_SLOSS_REAL) {
@@ -95,12 +97,13 @@ void kk_matrix(int variant, int no, double domega, std::vector<double>& K, int* 
   }
 }
 
-// out[io0][p] = sum_r K[io0][r] S[r][col] with the -i pi S(row(io0)) epilogue.
+// out[io0][p] = sum_r K[io0][r] S[r][col] with the -i pi S(row(io0)) epilogue
+// (scaled by pi_fac / pi: 1 for the KK transforms, 0 for a bare product).
 // S is viewed as [nw][ncols] doubles (ncols = np for real S, 2 np for complex).
 template <bool CPLX>
 __global__ void __launch_bounds__(256) k_kk_fp64(const double* __restrict__ K, const double* __restrict__ S,
                                                  double2* __restrict__ out, int nrow, int nw, int np,
-                                                 int pi_row0) {
+                                                 int pi_row0, double pi_fac) {
   constexpr int BM = 32, BN = 64, BK = 16;
   __shared__ double Ks[BK][BM + 1];
   __shared__ double Ss[BK][BN];
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(256) k_kk_fp64(const double* __restrict__ K, c
     }
     __syncthreads();
   }
-  const double pi = 3.141592653589793238462643383279502884;
+  const double pi = pi_fac;
 #pragma unroll
   for (int i = 0; i < 2; ++i) {
     int r = m0 + ty * 2 + i;
@@ -241,6 +244,21 @@ __global__ void __launch_bounds__(256) k_kk_f32(const float* __restrict__ K, con
   }
 }
 
+// out[nrow][np] = K[nrow][nw] S_real[nw][np] (FP64), plus -i pi S(row r) when
+// pi_epilogue; K comes from the host and is staged in buf.
+int kk_apply_real_fp64(rpa_ctx* c, DevBuf& buf, const std::vector<double>& K, int nrow, int nw, const double* S,
+                       double2* out, int np, bool pi_epilogue) {
+  RPA_TRY(ensure(c, buf, sizeof(double) * K.size()));
+  RPA_CUDA(c, cudaMemcpyAsync(buf.p, K.data(), sizeof(double) * K.size(), cudaMemcpyHostToDevice, c->stream));
+  dim3 grid((np + 63) / 64, (nrow + 31) / 32);
+  k_kk_fp64<false><<<grid, 256, 0, c->stream>>>(buf.as<double>(), S, out, nrow, nw, np, 0,
+                                                pi_epilogue ? KK_PI : 0.0);
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  RPA_CUDA(c, cudaStreamSynchronize(c->stream));  // the host copy of K goes out of scope
+  return RPA_OK;
+}
+
 int kk_run(rpa_ctx* c, int variant, int no, double domega) {
   std::vector<double> K;
   int nw = 0;
@@ -272,10 +290,10 @@ int kk_run(rpa_ctx* c, int variant, int no, double domega) {
   }
   if (cplx)
     k_kk_fp64<true><<<grid, 256, 0, c->stream>>>(c->d_kk.as<double>(), c->d_S.as<double>(),
-                                                 c->d_chi0.as<double2>(), nrow, nw, np, pi_row0);
+                                                 c->d_chi0.as<double2>(), nrow, nw, np, pi_row0, KK_PI);
   else
     k_kk_fp64<false><<<grid, 256, 0, c->stream>>>(c->d_kk.as<double>(), c->d_S.as<double>(),
-                                                  c->d_chi0.as<double2>(), nrow, nw, np, pi_row0);
+                                                  c->d_chi0.as<double2>(), nrow, nw, np, pi_row0, KK_PI);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
   return RPA_OK;

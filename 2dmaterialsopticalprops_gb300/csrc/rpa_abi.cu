@@ -489,7 +489,7 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
   cudaEventRecord(c->ev[7], c->stream);
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
   c->stage_ms[5] = elapsed(c, 6, 7);
-  c->have_S = c->have_chi0 = false;
+  c->have_S = c->have_chi0 = c->have_W = false;
   return RPA_OK;
 }
 
@@ -517,7 +517,7 @@ int rpa_kmap(rpa_ctx* c, int ntot, const double* ktot, const int* K1, const int*
   RPA_TRY(ensure(c, c->d_ktot, sizeof(double) * 3 * (size_t)ntot));
   RPA_CUDA(c, cudaMemcpy(c->d_kmap.p, c->h_kmap.data(), sizeof(int) * 5 * (size_t)ntot, cudaMemcpyHostToDevice));
   RPA_CUDA(c, cudaMemcpy(c->d_ktot.p, ktot, sizeof(double) * 3 * (size_t)ntot, cudaMemcpyHostToDevice));
-  c->have_S = c->have_chi0 = false;
+  c->have_S = c->have_chi0 = c->have_W = false;
   return RPA_OK;
 }
 
@@ -551,7 +551,7 @@ int rpa_set_q(rpa_ctx* c, const double* q, int nlf, const int* ilf, const int* p
   RPA_CUDA(c, cudaMemcpy(c->d_lf_miller.p, lm.data(), sizeof(int) * lm.size(), cudaMemcpyHostToDevice));
   RPA_CUDA(c, cudaMemcpy(c->d_Glf.p, gl.data(), sizeof(double) * gl.size(), cudaMemcpyHostToDevice));
   c->have_q = true;
-  c->have_S = c->have_chi0 = false;
+  c->have_S = c->have_chi0 = c->have_W = false;
   return RPA_OK;
 }
 
@@ -746,6 +746,7 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
   c->last_Gcar = a->Gcar;
   c->have_S = true;
   c->have_chi0 = false;
+  c->have_W = false;
   // results to the host, in the Fortran layouts
   double t_io = 0;
   if (S0_out || Qeff_out) {
@@ -781,6 +782,7 @@ int rpa_kk(rpa_ctx* c, int variant, double* chi0_out) {
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
   c->stage_ms[3] = elapsed(c, 0, 1);
   c->have_chi0 = true;
+  c->have_W = false;
   if (chi0_out) {
     const int nwo = c->last_no - 1, np = c->nlf * c->nlf;
     RPA_TRY(ensure(c, c->d_tmp, sizeof(double2) * (size_t)nwo * np));
@@ -846,6 +848,7 @@ int rpa_dyson(rpa_ctx* c, double c0, double eps, double* WT_out, double* epsinv_
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
   c->stage_ms[5] = elapsed(c, 6, 7);
   if (nsing) return fail(c, RPA_ESINGULAR, "singular matrix in gjel at %d frequencies", nsing);
+  c->have_W = true;
   if (nzero && c->verbose) fprintf(stderr, "rpa_dyson: singular matrix in gjel (zero pivot) at %d frequencies\n", nzero);
   return RPA_OK;
 }

@@ -94,7 +94,7 @@ struct rpa_ctx {
   // results
   int last_mode = -1, last_no = 0, last_nw = 0;
   double last_domega = 0.0, last_Gcar = 0.0;
-  bool have_S = false, have_chi0 = false;
+  bool have_S = false, have_chi0 = false, have_W = false;
   rpa::DevBuf d_S, d_Sdf, d_Q, d_chi0, d_kk, d_kkf, d_V, d_eps, d_WT, d_flags, d_tmp;
   double stage_ms[6] = {0, 0, 0, 0, 0, 0};
   long long launches = 0;  // kernels launched by this context
@@ -131,6 +131,8 @@ struct Chi0Plan {
 };
 
 int build_gfast(rpa_ctx* c, int ik, int nsum_legacy, int* out);
+int kk_apply_real_fp64(rpa_ctx* c, DevBuf& buf, const std::vector<double>& K, int nrow, int nw, const double* S,
+                       double2* out, int np, bool pi_epilogue);
 
 // device layout transposes between [w][p] (library) and (w fastest) Fortran
 void launch_transpose_wp_to_fortran(const double* src, double* dst, int nw, int np, int ncomp,

@@ -26,7 +26,7 @@ EXPORTS = ["rpa_create", "rpa_destroy", "rpa_last_error", "rpa_set_gvectors", "r
            "rpa_load_basis", "rpa_kmap", "rpa_set_q", "rpa_chi0", "rpa_kk", "rpa_dyson", "rpa_gfast",
            "rpa_init_igk", "rpa_kk_matrix", "rpa_stage_times", "rpa_chi0_stats", "rpa_dyson_noalloc", "rpa_selftest", "rpa_launch_count", "rpa_get_stream", "rpa_synchronize",
            "rpa_basis_info", "rpa_create_shared", "rpa_server_create", "rpa_server_submit", "rpa_server_wait",
-           "rpa_server_last_error", "rpa_server_destroy"]
+           "rpa_server_last_error", "rpa_server_destroy", "rpa_pi", "rpa_kk_w"]
 
 
 class RpaOpts(C.Structure):
@@ -94,6 +94,8 @@ def load_library(path: str = LIB_PATH):
     L.rpa_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.rpa_synchronize.argtypes = [vp]
     L.rpa_basis_info.argtypes = [vp, vp]
+    L.rpa_pi.argtypes = [vp, dp, dp, vp, vp, vp]
+    L.rpa_kk_w.argtypes = [vp, vp, vp, vp]
     L.rpa_create_shared.argtypes = [C.POINTER(vp), vp, ip]
     L.rpa_server_create.argtypes = [C.POINTER(vp), vp, ip, dp]
     L.rpa_server_submit.argtypes = [vp, C.POINTER(RpaRequest), C.POINTER(C.c_longlong)]
@@ -257,6 +259,24 @@ class Context:
         rc = self.L.rpa_dyson(self.h, c0, eps, _p(WT), _p(Ei), _p(head))
         self._chk(rc)
         return WT, Ei, head
+
+    def pi(self, eta_intra: float, c0: float, want_full: bool = False):
+        """Optabs calc = 2 assembly: (Pi_11 spectrum, sigma[2, no-1] inter/intra, full Pi or None)."""
+        nwo = self.no - 1
+        p11 = np.zeros(nwo, dtype=np.complex128)
+        full = np.zeros((self.nlf, self.nlf, nwo), dtype=np.complex128) if want_full else None
+        sig_c = np.zeros(2 * nwo)
+        self._chk(self.L.rpa_pi(self.h, eta_intra, c0, _p(p11), _p(sig_c), _p(full)))
+        return p11, sig_c.reshape(nwo, 2).T.copy(), full
+
+    def kk_w(self, want_gamma: bool = True):
+        """KK transform of W and its self-check: (Gamma+, Gamma-, check5)."""
+        nwo = self.no - 1
+        gp = np.zeros((self.nlf, self.nlf, nwo), dtype=np.complex128) if want_gamma else None
+        gm = np.zeros((self.nlf, self.nlf, nwo), dtype=np.complex128) if want_gamma else None
+        chk = np.zeros(5)
+        self._chk(self.L.rpa_kk_w(self.h, _p(gp), _p(gm), _p(chk)))
+        return gp, gm, chk
 
     def gfast(self, ik1: int, ngd: int = 0) -> np.ndarray:
         s = self.sys

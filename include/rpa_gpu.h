@@ -191,6 +191,32 @@ int rpa_kk_matrix(int variant, int no, double domega, double* K);
 int rpa_dyson_noalloc(const double* chi0, const double* V, int n, int nwo, double* WT, double* head,
                       void* stream, int* n_singular);
 
+/* Replaces: the calc = 2 assembly of Optabs (Optabs.f90:575-614) on the chi0
+ * and Qeff of the last Optabs rpa_chi0 + rpa_kk:
+ *   Pi(io) = chi0(io) + Pi_dia + Qeff oi / (oi + i eta_intra),
+ *   Pi_dia = -Re chi0(io = 1), oi = (io-1) domega, io = 1..no-1.
+ *   pi11_out  : host, complex (no-1): Pi_tot(1,1), the spectrum the driver writes
+ *   sigma_out : host, real (2, no-1): [inter, intra] conductivity in units of
+ *               2 pi e^2 / h, Re(-i c0 Pi / oi), 0 at io = 1 (not written there);
+ *               the interband term is Pi_tot(1,1) as the driver reads it after its
+ *               (iG, jG) loop: with the intraband term when Nlf > 1, without it
+ *               when Nlf = 1; the intraband term is Qeff(1,1) oi / (oi + i eta_intra)
+ *   Pi_out    : host, complex Pi(no-1, Nlf, Nlf), or NULL
+ * eta_intra in Hartree, c0 in bohr (namelist values). */
+int rpa_pi(rpa_ctx* ctx, double eta_intra, double c0, double* pi11_out, double* sigma_out, double* Pi_out);
+
+/* Replaces: the Kramers-Kronig transform of the screened interaction and its
+ * self-check in Sloss (Sloss.f90:486-534 with genW1W2 :1062-1171 and
+ * writeKramKron_Qi :1603-1641), on the W of the last rpa_dyson:
+ *   S_W(io) = -Im WT(io) / pi for io < no, S_W(no) = S0(no) of the chi0 (the
+ *   driver does not overwrite that row); W1, W2 as genW1W2;
+ *   gamma_p_out : host, complex (no-1, Nlf, Nlf): Gamma+ = (W1, Im WT), or NULL
+ *   gamma_m_out : host, complex (no-1, Nlf, Nlf): Gamma- = (-W2, 0), or NULL
+ *   check5      : host, [0] KKS = int (WindKK - Wind)^2, [1] SKK = int Wind^2,
+ *                 [2] 100 |KKS / SKK| (percent), [3] real Gamma+(o=0,1,1),
+ *                 [4] real[WT(o=0,1,1) - V(1,1)] / 2, or NULL. */
+int rpa_kk_w(rpa_ctx* ctx, double* gamma_p_out, double* gamma_m_out, double* check5);
+
 /* Timing of the stages of the last rpa_chi0/rpa_kk/rpa_dyson calls (ms, CUDA
  * events on the context stream): [0] pairs+sort, [1] vertices,
  * [2] accumulation, [3] KK, [4] Dyson, [5] host<->device copies. */

@@ -224,3 +224,128 @@ def dyson(chi0: np.ndarray, V: np.ndarray, fast_wt: bool = True, nthreads: int =
 def fortran_mat(a_np: np.ndarray) -> np.ndarray:
     """numpy (j,i) reversed-index array -> the matrix with [i,j] indexing."""
     return a_np.T
+
+
+# ---------------------------------------------------------------------------
+# Consumers right after the hot path, restated in Python (small sizes only).
+# Arrays use the layout of the other outputs here: (Nlf, Nlf, frequency).
+
+def pi_assembly(chi0: np.ndarray, Qeff: np.ndarray, domega: float, eta_intra: float, c0: float):
+    """Optabs calc = 2 (Optabs.f90:575-614), loop for loop: returns
+    (Pi_tot(1,1) per io = 1..no-1, sigma (2, no-1) [inter, intra], Pi per io).
+    Pi_inter is read inside the (iG, jG) loop, as the driver does, so it holds
+    Pi_tot(1,1) with the intraband term once the loop has passed (1,1)."""
+    nlf, _, nwo = chi0.shape
+    Pi_dia = np.zeros((nlf, nlf), dtype=np.complex128)
+    Pi_tot = np.zeros((nlf, nlf), dtype=np.complex128)
+    pi11 = np.zeros(nwo, dtype=np.complex128)
+    sigma = np.zeros((2, nwo))
+    full = np.zeros((nlf, nlf, nwo), dtype=np.complex128)
+    for io in range(1, nwo + 1):
+        oi = (io - 1) * domega
+        Pi_inter = Pi_intra = 0j
+        for iG in range(nlf):
+            for jG in range(nlf):
+                re, im = chi0[iG, jG, io - 1].real, chi0[iG, jG, io - 1].imag
+                if io == 1:
+                    Pi_dia[iG, jG] = -complex(re, 0.0)
+                Pi_tot[iG, jG] = complex(re, im)
+                Pi_tot[iG, jG] = Pi_tot[iG, jG] + Pi_dia[iG, jG]
+                Pi_inter = Pi_tot[0, 0]
+                Pi_intra = Qeff[0, 0] * oi / (oi + 1j * eta_intra)
+                Pi_tot[iG, jG] = Pi_tot[iG, jG] + Qeff[iG, jG] * oi / (oi + 1j * eta_intra)
+        pi11[io - 1] = Pi_tot[0, 0]
+        full[:, :, io - 1] = Pi_tot
+        if io > 1:
+            sigma[0, io - 1] = (-1j * c0 * Pi_inter / oi).real
+            sigma[1, io - 1] = (-1j * c0 * Pi_intra / oi).real
+    return pi11, sigma, full
+
+
+def _w1w2(io: int, no: int, oi: float, domega: float, S: np.ndarray):
+    """genW1W2 (Sloss.f90:1062-1171) for all (iG, jG) at once; S[..., jo-1]."""
+    W1 = np.zeros(S.shape[:2])
+    W2 = np.zeros(S.shape[:2])
+    if io == 1:
+        for jo in range(2, no + 1):
+            oj = (jo - 1) * domega
+            fact = domega / oj
+            if jo == 2:
+                fact = 3.0 / 2.0
+            elif jo == no:
+                fact = 0.5 * domega / oj
+            W1 = W1 - fact * S[..., jo - 1]
+        return W1, -W1
+    for jo in range(1, no + 1):
+        oj = (jo - 1) * domega
+        if io == 2:
+            if jo != io:
+                fact = domega / (oi - oj)
+            elif jo == 1:
+                fact = 1.0
+            elif jo == 2:
+                fact = 0.0
+            elif jo == 3:
+                fact = -3.0 / 2.0
+            elif jo == no:
+                fact = 0.5 * domega / (oi - oj)
+        elif io == no - 1:
+            if jo != io:
+                fact = domega / (oi - oj)
+            elif jo == 1:
+                fact = 0.5 * domega / (oi - oj)
+            elif jo == no - 2:
+                fact = 3.0 / 2.0
+            elif jo == no - 1:
+                fact = 0.0
+            elif jo == no:
+                fact = -1.0
+        else:
+            if jo != io:
+                fact = domega / (oi - oj)
+            elif jo == 1:
+                fact = 0.5 * domega / (oi - oj)
+            elif jo == io - 1:
+                fact = 3.0 / 2.0
+            elif jo == io:
+                fact = 0.0
+            elif jo == io + 1:
+                fact = -3.0 / 2.0
+            elif jo == no:
+                fact = 0.5 * domega / (oi - oj)
+        W1 = W1 + fact * S[..., jo - 1]
+        fact = domega / (oi + oj)
+        if jo == 1 or jo == no:
+            fact = 0.5 * domega / (oi + oj)
+        W2 = W2 + fact * S[..., jo - 1]
+    return W1, W2
+
+
+def kk_w(WT: np.ndarray, S0_chi: np.ndarray, V11: float, domega: float):
+    """KK transform of W and its self-check (Sloss.f90:486-534): returns
+    (Gamma+, Gamma-, [KKS, SKK, 100|KKS/SKK|, Re Gamma(o=0,1,1),
+    Re(WT(o=0,1,1) - V(1,1))/2]).  S0_chi: the chi0 spectral function
+    (Nlf, Nlf, no); its last row stays in the transform, as in the driver."""
+    nlf, _, nwo = WT.shape
+    no = nwo + 1
+    S = S0_chi.copy()
+    S[..., :no - 1] = -(1.0 / np.pi) * WT.imag
+    Gp = np.zeros_like(WT)
+    Gm = np.zeros_like(WT)
+    KKS = SKK = 0.0
+    G0 = 0j
+    for io in range(1, no):
+        oi = (io - 1) * domega
+        W1, W2 = _w1w2(io, no, oi, domega, S)
+        ImW = -np.pi * S[..., io - 1]
+        Gp[..., io - 1] = W1 + 1j * ImW
+        Gm[..., io - 1] = -W2 + 0j
+        W2KK = W2[0, 0]
+        if io == 1:
+            G0 = Gp[0, 0, 0]
+        Wind = (WT[0, 0, io - 1] - V11).real
+        WindKK = Gp[0, 0, io - 1].real - W2KK
+        fact = 0.5 * domega if (io == 1 or io == no - 1) else domega
+        KKS += fact * (WindKK - Wind) ** 2
+        SKK += fact * Wind * Wind
+    return Gp, Gm, np.array([KKS, SKK, 100.0 * abs(KKS / SKK), G0.real, (WT[0, 0, 0] - V11).real / 2.0])

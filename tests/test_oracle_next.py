@@ -1,0 +1,55 @@
+"""Oracle restatements of the consumers after the hot path (CPU only): the
+Optabs calc = 2 assembly (Pi, conductivity) and the KK transform of W with
+its self-check, checked against closed forms."""
+import numpy as np
+
+
+def test_w1w2_single_spike(orc):
+    no, d = 11, 0.1
+    S = np.zeros((1, 1, no))
+    S[0, 0, 4] = 1.0  # a spike at oj = 4 d
+    W1, W2 = orc._w1w2(1, no, 0.0, d, S)
+    assert np.isclose(W1[0, 0], -d / (4 * d)) and np.isclose(W2[0, 0], -W1[0, 0])
+    for io in (2, 3, 7, no - 1):
+        oi = (io - 1) * d
+        W1, W2 = orc._w1w2(io, no, oi, d, S)
+        assert np.isclose(W1[0, 0], d / (oi - 4 * d))
+        assert np.isclose(W2[0, 0], d / (oi + 4 * d))
+    # the row io never contributes to W1 at io (the else-if chain sets fact = 0)
+    W1, _ = orc._w1w2(5, no, 4 * d, d, S)
+    assert W1[0, 0] == 0.0
+
+
+def test_kk_w_of_a_consistent_pair_is_small(orc):
+    # W - V = a pole pair: Re and Im are a KK pair, so the self-check error is
+    # a discretisation error only
+    no, d, e0, g = 801, 0.01, 2.0, 0.2
+    o = np.arange(no - 1) * d
+    w = 1.0 / (o - e0 + 1j * g) - 1.0 / (o + e0 + 1j * g)
+    V11 = 0.7
+    WT = (w + V11).reshape(1, 1, -1)
+    S0 = np.zeros((1, 1, no))
+    S0[0, 0, -1] = -(1.0 / np.pi) * w[-1].imag
+    Gp, Gm, chk = orc.kk_w(WT, S0, V11, d)
+    assert chk[2] < 1.0  # percent
+    assert np.isclose(chk[4], (WT[0, 0, 0] - V11).real / 2)
+    np.testing.assert_allclose(Gp[0, 0].imag, WT[0, 0].imag)
+    assert np.all(Gm.imag == 0)
+
+
+def test_pi_assembly_matches_the_closed_form(orc):
+    rng = np.random.default_rng(3)
+    for nlf in (1, 4):
+        nwo, d, eta, c0 = 30, 0.02, 0.05, 37.8
+        chi0 = rng.standard_normal((nlf, nlf, nwo)) + 1j * rng.standard_normal((nlf, nlf, nwo))
+        Q = rng.standard_normal((nlf, nlf)) + 1j * rng.standard_normal((nlf, nlf))
+        pi11, sig, full = orc.pi_assembly(chi0, Q, d, eta, c0)
+        oi = np.arange(nwo) * d
+        intra = Q[..., None] * oi / (oi + 1j * eta)
+        Pi = chi0 - chi0[..., :1].real + intra
+        np.testing.assert_allclose(full, Pi, rtol=1e-13, atol=1e-13)
+        np.testing.assert_allclose(pi11, Pi[0, 0], rtol=1e-13, atol=1e-13)
+        inter = Pi[0, 0] if nlf > 1 else Pi[0, 0] - intra[0, 0]
+        np.testing.assert_allclose(sig[0, 1:], c0 * inter.imag[1:] / oi[1:], rtol=1e-12)
+        np.testing.assert_allclose(sig[1, 1:], c0 * intra[0, 0].imag[1:] / oi[1:], rtol=1e-12)
+        assert sig[0, 0] == 0 and sig[1, 0] == 0

@@ -441,9 +441,27 @@ static int launch_vtc_nb(rpa_ctx* c, const VtxTcCtx& V, int nk, int NB) {
   return launch_vtc<32, CURRENT>(c, V, nk);
 }
 
+// One launch per pair of band windows [m0 + i mwin, ...) x [n0 + j nwin, ...).
+template <bool CURRENT>
+static int launch_windows(rpa_ctx* c, VtxTcCtx V, int nk, int m0, int mcount, int mwin, int n0, int ncount,
+                          int nwin) {
+  for (int mb = 0; mb < mcount; mb += mwin) {
+    for (int nb = 0; nb < ncount; nb += nwin) {
+      V.m0 = m0 + mb;
+      V.mcount = std::min(mwin, mcount - mb);
+      V.n0 = n0 + nb;
+      V.ncount = std::min(nwin, ncount - nb);
+      V.gpt = 128 / V.mcount;
+      const int NB = V.ncount <= 8 ? 8 : (V.ncount <= 16 ? 16 : 32);
+      RPA_TRY(launch_vtc_nb<CURRENT>(c, V, nk, NB));
+    }
+  }
+  return RPA_OK;
+}
+
 // Mixed-path vertices of the FBZ k-points [k0, k0+nk) on the tensor cores.
-// Leaves *used false when the band windows or the plane-wave count do not fit
-// the tiles (the caller then uses the CUDA-core kernel).
+// Leaves *used false when the plane-wave count does not fit the int16 Gfast
+// positions (the caller then uses the CUDA-core kernel).
 int vertices_tc(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans, const int* pos_of, float2* Mf,
                 float2* Mf2, unsigned* amax, bool* used) {
   *used = false;
@@ -456,8 +474,11 @@ int vertices_tc(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
   } else {
     m0 = P.nocc, mcount = c->nbnd - P.nocc, n0 = 0, ncount = P.nocc;
   }
-  if (mcount < 1 || mcount > 32 || ncount > 32 || c->npwx > 32767) return RPA_OK;
-  const int NB = ncount <= 8 ? 8 : (ncount <= 16 ? 16 : 32);
+  if (mcount < 1 || ncount < 1 || c->npwx > 32767) return RPA_OK;
+  // band windows of at most 32 on each side, one launch per pair of windows
+  // (transitions outside a launch's windows are skipped by it)
+  const int nmw = (mcount + 31) / 32, nnw = (ncount + 31) / 32;
+  const int mwin = (mcount + nmw - 1) / nmw, nwin = (ncount + nnw - 1) / nnw;
   // Gfast map of the chunk (int16 positions), shared by the chains of one q-point
   int nsum_max = 0;
   for (int i = 0; i < nk; ++i) {
@@ -498,8 +519,6 @@ int vertices_tc(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
   V.legacy = c->legacy ? 1 : 0;
   V.nsum_legacy = P.nsum_legacy;
   V.nsum_max = nsum_max;
-  V.m0 = m0, V.mcount = mcount, V.n0 = n0, V.ncount = ncount;
-  V.gpt = 128 / mcount;
   V.q0 = c->q[0];
   V.q1 = c->q[1];
   V.q2 = c->q[2];
@@ -512,7 +531,7 @@ int vertices_tc(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
     V.M = Mf;
     V.amax = amax;
     *used = true;
-    return launch_vtc_nb<false>(c, V, nk, NB);
+    return launch_windows<false>(c, V, nk, m0, mcount, mwin, n0, ncount, nwin);
   }
   // current vertices: |C| <= 1 (orthonormal bands), |b(i)| <= Gcar max|G|
   double gmax = 0.0;
@@ -542,7 +561,7 @@ int vertices_tc(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
     k_vtx_btab<<<2048, 256, 0, c->stream>>>(V, nk, c->d_vbt.as<float>());
     RPA_CUDA(c, cudaGetLastError());
     ++c->launches;
-    RPA_TRY(launch_vtc_nb<true>(c, V, nk, NB));
+    RPA_TRY(launch_windows<true>(c, V, nk, m0, mcount, mwin, n0, ncount, nwin));
   }
   *used = true;
   return RPA_OK;

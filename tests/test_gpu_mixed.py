@@ -80,3 +80,20 @@ def test_bf16_split_variant_runs(synth, rpa, orc):
     S, _ = ctx.chi0(rpa.MODE_CHARGE, **rpa.sloss_args(s))
     assert rel(S, orc.sloss_s0(orc.Bound(s))) < 1e-4
     ctx.close()
+
+
+@pytest.mark.parametrize("nbnd,nocc", [(80, 13), (40, 20)])
+def test_mixed_band_windows_over_32(synth, rpa, orc, nbnd, nocc):
+    """More than 32 bands on a side of the vertex GEMM: the tensor-core vertex
+    kernel runs once per pair of band windows (80 bands / 13 occupied: 3
+    windows of empty bands for the charge vertex; 40 bands: 2 x 2 windows for
+    the current vertex)."""
+    s = synth.build(synth.config_small(nbnd=nbnd, nocc=nocc, npw=160, nlf=9, no=31))
+    ctx = rpa.Context(precision=rpa.PREC_MIXED)
+    ctx.load_system(s)
+    S, _ = ctx.chi0(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+    assert rel(S, orc.sloss_s0(orc.Bound(s))) < TOL
+    Sc, _ = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, "zz"))
+    Sco, _ = orc.optabs_s0(orc.Bound(s, pol="zz"))
+    assert rel(Sc, Sco) < TOL
+    ctx.close()

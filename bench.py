@@ -357,6 +357,72 @@ def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, fp64_sample=(0, 31
             "errors_vs_fp64_gpu": errs}
 
 
+def c5_config(nk: int):
+    """Large screened interaction: MoS2-like cell stand-in (the synthetic
+    hexagonal cell), 80 bands (13 occupied), ~4000 coefficients, NGloc = 301,
+    nw = 701 on 0-50 eV, eta = 50 meV."""
+    return pkg("synth").config_grid120(nk=nk, nbnd=80, nocc=13, npw=4000, nlf=301, lf="xyz", no=701,
+                                       omax_ev=50.0, eta_ev=0.05)
+
+
+def c5_run(n_q: int = 16, nk_full: int = 96, nk_check: int = 24, q_check=(1, 8)):
+    """W(q, w) for 16 q-points at full size on the mixed path (timed), and the
+    mixed-vs-FP64 comparison (time ratio, per-q max / RMS error of Im W) on
+    the same workload with a 24x24 k-grid."""
+    rpa, synth = pkg("rpa"), pkg("synth")
+
+    def w_chain(c, s, steps):
+        km = synth.q_kmap(s, steps)
+        c.kmap(km["ktot"], km["K1"], km["R1"], km["K2"], km["R2"], km["iG0"])
+        c.set_q(km["q"], s.ilf, s.parG)
+        c.chi0(rpa.MODE_CHARGE, want=False, **rpa.sloss_args(s))
+        c.kk(rpa.KK_SLOSS_REAL, want=False)
+        WT, _, head = c.dyson(s.c0, s.cfg.eps, want_wt=True)
+        return WT, head
+
+    # mixed vs FP64 on the 24x24 grid
+    s = synth.build(c5_config(nk_check))
+    cm = rpa.Context(precision=rpa.PREC_MIXED)
+    cm.load_system(s)
+    c64 = rpa.shared_context(cm, rpa.PREC_FP64)
+    errs, tm, t64 = [], 0.0, 0.0
+    for st in q_check:
+        t = time.perf_counter()
+        Wm, hm = w_chain(cm, s, st)
+        tm += time.perf_counter() - t
+        t = time.perf_counter()
+        W6, h6 = w_chain(c64, s, st)
+        t64 += time.perf_counter() - t
+        d = np.abs(Wm.imag - W6.imag)
+        errs.append({"q_steps": st, "max_rel_Im_W": float(d.max() / np.abs(W6.imag).max()),
+                     "rms_rel_Im_W": float(np.sqrt((d ** 2).mean()) / np.sqrt((W6.imag ** 2).mean())),
+                     "max_rel_Im_epsinv": float(np.abs(hm.imag - h6.imag).max() / np.abs(h6.imag).max())})
+    c64.close()
+    cm.close()
+    del s
+    # full size, mixed path
+    t0 = time.perf_counter()
+    s = synth.build(c5_config(nk_full))
+    cm = rpa.Context(precision=rpa.PREC_MIXED)
+    cm.load_system(s)
+    t_setup = time.perf_counter() - t0
+    steps = list(range(1, n_q + 1))
+    w_chain(cm, s, steps[0])  # warm-up (buffers reach their sizes)
+    t = time.perf_counter()
+    for st in steps:
+        w_chain(cm, s, st)
+    t_full = time.perf_counter() - t
+    st_times = cm.stage_times()
+    cm.close()
+    return {"workload": f"large W: {nk_full}x{nk_full} k-grid, 80 bands (13 occ), ~4000 coefficients, "
+                        f"NGloc=301, nw=701 on 0-50 eV, eta=50 meV, {n_q} q-points (1..{n_q} grid steps along "
+                        f"Gamma-M); loss chain per q (S0, KK, FP64 Dyson, W)",
+            "n_q": n_q, "mixed_s": t_full, "value": n_q / t_full, "unit": "q-spectra/s", "setup_s": t_setup,
+            "last_q_stage_ms": st_times,
+            "check": {"grid": f"{nk_check}x{nk_check}", "mixed_s": tm, "fp64_s": t64, "mixed_over_fp64": t64 / tm,
+                      "errors_vs_fp64_gpu": errs}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -370,6 +436,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop (serving) measurement")
+    ap.add_argument("--c5", action="store_true",
+                    help="also run the large-W workload (96x96, 80 bands, 4000 coefficients, NGloc 301; adds minutes)")
     ap.add_argument("--dispersion", action="store_true",
                     help="also run the 64-q loss-function dispersion on the resident basis (adds ~2 min)")
     args = ap.parse_args()
@@ -552,6 +620,12 @@ def main():
         serving = serving_run()
     if rank == 0 and args.dispersion and args.precision == "mixed":
         disp = dispersion_run(ctx, s)
+    c5 = None
+    if rank == 0 and args.c5 and args.precision == "mixed":
+        if ctx is not None:
+            ctx.close()
+            ctx = None
+        c5 = c5_run()
 
     if rank == 0:
         cfgd = workload_desc(s, args.config)
@@ -564,7 +638,7 @@ def main():
                 "data": "synthetic (seeded QE-layout Bloch basis)", "config": cfgd, "clocks": clocks,
                 "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "stage_ms_per_step": {k: round(v, 3) for k, v in sm.items()},
-                "fp64_gpu": fp64, "serving": serving, "dispersion": disp,
+                "fp64_gpu": fp64, "serving": serving, "dispersion": disp, "c5": c5,
                 "vertex_tflops": (work["vertex_flops"] / (sm["vertices"] / 1e3) / 1e12) if sm["vertices"] else None}
         print(json.dumps(line), flush=True)
     if ctx is not None:

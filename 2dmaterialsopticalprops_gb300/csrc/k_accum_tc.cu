@@ -459,10 +459,6 @@ __device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile
   return false;
 }
 
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
-}
-
 template <int NIO, bool CPLX, bool SEPA>
 struct WsCfg {
   static constexpr uint32_t A_BYTES = TC_GA * 128;                  // one 16-bit A tile
@@ -647,8 +643,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
         }
         __syncwarp();
         if (lane == 0) {
-          mbar_arrive(&wready[c & 1]);
-          mbar_arrive(&dfree[c % S]);
+          tc::mbar_arrive(&wready[c & 1]);
+          tc::mbar_arrive(&dfree[c % S]);
         }
       }
       if (!ok) abort_flag = 1;
@@ -715,7 +711,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
         consume(sg & 1);
         tc::tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&tfree[sg & 1]);
+        if (lane == 0) tc::mbar_arrive(&tfree[sg & 1]);
         if (++consumed % TC_FLUSH == 0) flush();
       }
       if (ok) ok = __all_sync(0xffffffffu, ws_wait(&wready[c & 1], (c >> 1) & 1, &abort_flag));
@@ -755,8 +751,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
       tc::fence_async_smem();
       __syncwarp();
       if (lane == 0) {
-        mbar_arrive(&formed[c & 1]);
-        mbar_arrive(&dfree[c % S]);
+        tc::mbar_arrive(&formed[c & 1]);
+        tc::mbar_arrive(&dfree[c % S]);
       }
     }
     // drain: read back the segments the loop did not reach

@@ -510,6 +510,36 @@ int build_gmap(rpa_ctx* c, int k0, int nk, int nsum_max, int16_t* gmap, int nsum
   return RPA_OK;
 }
 
+// Inverse maps of the FBZ k-points [k0, k0+nk): ginv[k_local][G][p] = the K1
+// plane wave i with Gfast(G, i) = p (a basis position of K2), -1 where none.
+// Gfast(G, .) is injective (distinct G_i give distinct G''), so each p is
+// written at most once.
+__global__ void k_ginv(MapCtx C, int k0, int nk, int nsum_max, int nsum1_max, int16_t* __restrict__ ginv) {
+  const size_t per_k = (size_t)C.nlf * nsum1_max;
+  const size_t n = (size_t)nk * per_k;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int kl = (int)(e / per_k);
+    const size_t r = e % per_k;
+    const int g = (int)(r / nsum1_max), i = (int)(r % nsum1_max);
+    const int* km = C.kmap + 5 * (k0 + kl);
+    if (i >= C.npw[km[0]]) continue;
+    const int p = gfast_pos(C, km, g, i);
+    if (p >= 0 && p < nsum_max) ginv[((size_t)kl * C.nlf + g) * nsum_max + p] = (int16_t)i;
+  }
+}
+
+int build_ginv(rpa_ctx* c, int k0, int nk, int nsum_max, int16_t* ginv) {
+  if (c->legacy) return fail(c, RPA_EINVAL, "inverse Gfast map: needs the igk map of the basis");
+  MapCtx C = make_map_ctx(c);
+  int nsum1_max = 0;
+  for (int i = 0; i < nk; ++i) nsum1_max = std::max(nsum1_max, c->h_npw[c->h_kmap[5 * (size_t)(k0 + i)]]);
+  RPA_CUDA(c, cudaMemsetAsync(ginv, 0xff, sizeof(int16_t) * (size_t)nk * c->nlf * nsum_max, c->stream));
+  k_ginv<<<4096, 256, 0, c->stream>>>(C, k0, nk, nsum_max, nsum1_max, ginv);
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  return RPA_OK;
+}
+
 // Gfast map of one FBZ k-point in the reference's convention (1-based basis
 // positions, NG2+1 when absent), for the index-map parity checks.
 __global__ void k_gfast(MapCtx C, int ik, int nsum, int* out) {

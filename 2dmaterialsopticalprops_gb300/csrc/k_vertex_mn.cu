@@ -1,0 +1,761 @@
+// k_vertex_mn.cu -- plane-wave vertices on the tcgen05 tensor cores with both
+// operands MN-major (mixed path, default vertex kernel).
+//
+// Same vertices as k_vertex.cu (genMnmK1K2, Sloss.f90:883-952; genStrujniVrhovi,
+// Optabs.f90:1354-1472), per FBZ k-point as a GEMM over plane waves:
+//     D((G,a), b) = sum_i x_a(G,i) conj(y_b(i))
+// x: the gathered side, coefficients of bands a at basis positions map(G,i);
+// y: the sequential side, coefficients of bands b at plane wave i.
+//   Optabs, and Sloss with more occupied than empty bands: x = C2[m] of K2 at
+//     Gfast(G,i), y = C1[n] of K1, i over the plane waves of K1  -> M = D.
+//   Sloss with fewer occupied bands (the usual case): x = C1[n] of K1 at the
+//     inverse map (the K1 plane wave that Gfast sends to plane wave p of K2),
+//     y = C2[m] of K2, p over the plane waves of K2 -> M = conj(D).  The inverse
+//     exists because Gfast(G, .) is injective (G'' is an affine bijection of the
+//     K1 plane wave); gathering the occupied side moves nocc instead of
+//     nbnd - nocc bands per gathered plane wave.
+// The coefficients live as four fp16 planes per plane wave, [re_hi, im_hi,
+// re_lo, im_lo][bands] (x 2^14), so a gathered plane wave is one contiguous run
+// of bands.  The MMA operands are MN-major: a K row of the X tile holds 128
+// (G, band) rows, 8 bands per 16-byte chunk, so each gathered (G, plane wave,
+// plane) lands with 16-byte cp.async copies and no transposition.  K order in a
+// chunk of 32 plane waves: rows 0-31 real parts, 32-63 imaginary parts.  Then
+//     Re D = X . Y                          (all 64 K rows)
+//     Im D = X[Re] . (-Y[Im]) + X[Im] . Y[Re]
+// both from the same Y tile: the Im block reads the other half of Y's K rows,
+// negated by the instruction descriptor.  The current factor separates,
+// f(G,i) = a(G) + b(i): warps 0-3 form the b(i) c block of Y (extra columns)
+// from the c block they copied, and a(G) multiplies the c block at read-back:
+// M = a(G) D[c] + D[b c].  Each local-field tile sweeps the plane waves in the
+// opposite direction of the previous one, so the coefficient rows read last
+// are read again first while they are still in L2.
+// Three products per chunk, Xh Yl + Xl Yh + Xh Yh, into a fresh TMEM
+// accumulator (two, ping-pong) that the worker warps add to FP32 registers.
+// Warp roles: 16 worker warps gather chunk t + S - 1 into the ring of S
+// shared-memory stages and read back chunk t - 1 from TMEM; warp 16 issues
+// the MMAs.  Every wait is bounded and ends in an error status.
+
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "rpa_internal.cuh"
+#include "tc05.cuh"
+
+namespace rpa {
+
+int build_gmap(rpa_ctx* c, int k0, int nk, int nsum_max, int16_t* gmap, int nsum_legacy);
+int build_ginv(rpa_ctx* c, int k0, int nk, int nsum_max, int16_t* ginv);
+
+struct VtxMnCtx {
+  const int* kmap;
+  const double* ktot;
+  const double* Glf;
+  const int* npw;
+  const __half* planes;   // [kibz][npwx][4][nbp]
+  const float* btab;      // [k_local][nsum_max]: b(i) sB / 2^14 (current vertices)
+  const int16_t* map;     // [k_local][nlf][nsum_max]: gathered-side position of (G, i), -1 none
+  const Trans* trans;
+  const long long* offsets;
+  const int* pos_of;
+  float2* M;
+  unsigned* amax;
+  int* status;
+  int k0, nlf, npwx, nbp, nsum_max, legacy, nsum_legacy;
+  int swap;               // 1: x = bands n of K1 (inverse map), y = bands m of K2
+  int xs, xb, xo0, xo1;   // gathered window: first band, rows per G (multiple of 8), owned bands
+  int ys, yo0, yo1;       // sequential window: first band (multiple of 8), owned bands
+  int gpt;                // local fields per 128-row tile
+  int comp;
+  double q0, q1, q2, Gcar;
+  float a_scale, out_scale;
+};
+
+constexpr int VM_WORKERS = 512;                 // 16 worker warps
+constexpr int VM_THREADS = VM_WORKERS + 32;     // + the MMA warp
+constexpr int VM_I = 32;                        // plane waves per chunk (K = 64)
+constexpr uint32_t VM_SPINS = 1u << 16;         // suspending polls: about 1.3 s at most
+constexpr int VM_SMEM_MAX = 232448 - 1024;      // dynamic shared memory left beside the static part
+constexpr int VM_SMAX = 6;
+
+template <int NBY, bool CURRENT>
+struct VmCfg {
+  static constexpr int NY = CURRENT ? 2 : 1;
+  static constexpr int NYN = NY * NBY;                   // MMA N
+  static constexpr int NYA = (NYN + 63) / 64;            // 64-wide atoms along N
+  static constexpr uint32_t XH = 64 * 128 * 2;           // one half (hi or lo) of X
+  static constexpr uint32_t YH = (uint32_t)NYA * 8192;   // one half of Y
+  static constexpr uint32_t B_OFF = 2 * XH + 2 * YH;       // b(i) of the chunk, one copy per forming warp
+  static constexpr uint32_t STAGE = (B_OFF + (CURRENT ? 512u : 0u) + 1023u) / 1024u * 1024u;
+  static constexpr uint32_t PTAB = 32 * NBY * 2;         // int16 [32][NBY]
+  static constexpr int S0 = (int)((VM_SMEM_MAX - 1024 - (int)PTAB) / (int)STAGE);
+  static constexpr int S = S0 > VM_SMAX ? VM_SMAX : S0;
+  static constexpr uint32_t BUFC = 2 * NYN;              // Re block + Im block
+  static constexpr uint32_t NCOL = 4 * NYN <= 32 ? 32 : 4 * NYN <= 64 ? 64 : 4 * NYN <= 128 ? 128
+                                                       : 4 * NYN <= 256 ? 256 : 512;
+  static constexpr int CW = NBY / 4;                     // columns per thread per block
+  static constexpr size_t SMEM = (size_t)S * STAGE + PTAB + 1024;
+  static_assert(NBY % 16 == 0 && NYN <= 128, "window too wide");
+  static_assert(S >= 3, "shared-memory ring too shallow");
+};
+
+__device__ __forceinline__ void cp16z(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp4(uint32_t dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ uint4 lds16(uint32_t a) {
+  uint4 v;
+  asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ void sts16(uint32_t a, uint4 v) {
+  asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+               : "memory");
+}
+__device__ __forceinline__ float lds_f32(uint32_t a) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory");
+}
+
+// CW consecutive TMEM columns of this thread's lane
+template <int CW>
+__device__ __forceinline__ void tmem_ld_n(uint32_t addr, float* v) {
+  if constexpr (CW >= 16) {
+    tc::tmem_ld16(addr, v);
+    if constexpr (CW > 16) tmem_ld_n<CW - 16>(addr + 16, v + 16);
+  } else if constexpr (CW >= 8) {
+    tc::tmem_ld8(addr, v);
+    if constexpr (CW > 8) tmem_ld_n<CW - 8>(addr + 8, v + 8);
+  } else {
+    static_assert(CW == 4, "columns per thread");
+    tc::tmem_ld4(addr, v);
+  }
+}
+
+// One CTA per FBZ k-point of the launch.
+template <int NBY, bool CURRENT>
+__global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
+  using Cfg = VmCfg<NBY, CURRENT>;
+  constexpr int S = Cfg::S, NYN = Cfg::NYN, NYA = Cfg::NYA, CW = Cfg::CW;
+  constexpr uint32_t XH = Cfg::XH, YH = Cfg::YH, STAGE = Cfg::STAGE;
+
+  extern __shared__ unsigned char smraw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+  const uint32_t sbase = tc::smem_u32(base);
+  int16_t* ptab = reinterpret_cast<int16_t*>(base + (size_t)S * STAGE);  // [a][b]: local transition, -1 none
+  __shared__ uint64_t full[VM_SMAX], done[2], tfree[2];
+  __shared__ uint32_t tslot;
+  __shared__ volatile int abort_flag;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int kl = blockIdx.x, ik = V.k0 + kl;
+  const long long t0 = V.offsets[kl], t1 = V.offsets[kl + 1];
+  if (t1 == t0) return;
+  const int* km = V.kmap + 5 * ik;
+  const int K1 = km[0], K2 = km[2];
+  const int kX = V.swap ? K1 : K2, kY = V.swap ? K2 : K1;
+  const int nsum = V.legacy ? V.nsum_legacy : V.npw[kY];
+  const int nchunk = (nsum + VM_I - 1) / VM_I;
+  const int GPT = V.gpt, XB = V.xb;
+  const int ngt = (V.nlf + GPT - 1) / GPT;
+  const int total = ngt * nchunk;
+
+  if (warp == 0) {
+    tc::tmem_alloc(&tslot, Cfg::NCOL);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) tc::mbar_init(&full[s], VM_WORKERS / 32);
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&done[b], 1);
+      tc::mbar_init(&tfree[b], VM_WORKERS / 32);
+    }
+    abort_flag = 0;
+    tc::fence_mbar_init();
+  }
+  for (int e = tid; e < XB * NBY; e += VM_THREADS) ptab[e] = -1;
+  __syncthreads();
+  for (long long t = t0 + tid; t < t1; t += VM_THREADS) {
+    const int nm = V.trans[t].nm;
+    const int n = nm & 0xffff, m = nm >> 16;
+    const int xa = V.swap ? n : m, yb = V.swap ? m : n;
+    if (xa >= V.xo0 && xa < V.xo1 && yb >= V.yo0 && yb < V.yo1)
+      ptab[(xa - V.xs) * NBY + (yb - V.ys)] = (int16_t)(t - t0);
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t taddr = tslot;
+
+  if (warp == VM_WORKERS / 32) {
+    // ---------------------------------------------------------------- MMA warp
+    if (lane == 0) {
+      const uint32_t id_p = tc::idesc_f16_mn(128, NYN, false), id_n = tc::idesc_f16_mn(128, NYN, true);
+      // descriptors of stage 0; a chunk adds its byte offsets / 16 to the start-address field
+      const uint64_t dx0 = tc::desc_sw128_mn(sbase, 1024u, 2048u);
+      const uint64_t dy0 = tc::desc_sw128_mn(sbase + 2 * XH, 1024u, NYA * 1024u);
+      int last = -1;
+      int s = 0, ph = 0;
+      for (int t = 0; t < total; ++t) {
+        if (abort_flag) break;
+        if (!tc::mbar_wait(&full[s], (uint32_t)ph, VM_SPINS) ||
+            (t >= 2 && !tc::mbar_wait(&tfree[t & 1], (uint32_t)(((t - 2) >> 1) & 1), VM_SPINS))) {
+          atomicExch(V.status, 1);
+          abort_flag = 1;
+          break;
+        }
+        tc::tc_fence_after();
+        const uint64_t so = (uint64_t)(((uint32_t)s * STAGE) >> 4);
+        const uint64_t dx = dx0 + so, dy = dy0 + so;
+        const uint32_t dre = taddr + (uint32_t)((t & 1) * Cfg::BUFC), dim = dre + NYN;
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {  // Xh Yl, Xl Yh, Xh Yh
+          const uint64_t xa = dx + (p == 1 ? XH >> 4 : 0u), yb = dy + (p == 0 ? YH >> 4 : 0u);
+#pragma unroll
+          for (int ks = 0; ks < 4; ++ks) {
+            const uint32_t acc = (p > 0 || ks > 0) ? 1u : 0u;
+            const uint64_t da = xa + (uint64_t)(ks * 256);
+            const uint32_t kb = ks < 2 ? 4 + 2 * ks : 2 * (ks - 2);
+            tc::mma_bf16(dre, da, yb + (uint64_t)(ks * 2 * NYA * 64), id_p, acc);
+            tc::mma_bf16(dim, da, yb + (uint64_t)(kb * NYA * 64), ks < 2 ? id_n : id_p, acc);
+          }
+        }
+        tc::mma_commit(&done[t & 1]);
+        last = t;
+        if (++s == S) s = 0, ph ^= 1;
+      }
+      if (last >= 0) tc::mbar_wait(&done[last & 1], (uint32_t)((last >> 1) & 1), VM_SPINS);
+    }
+  } else {
+    // ------------------------------------------------------------- worker warps
+    // X copies of this thread: plane wave xpw of the chunk, rows 8 xj .. 8 xj + 7,
+    // the four planes (u = 0..3 -> half u / 2, K rows (u % 2) 32 + xpw)
+    const int xpw = tid >> 4, xj = tid & 15;
+    const int xrow = 8 * xj, xg = xrow / XB, xb0 = xrow - xg * XB;
+    const bool xok = xg < GPT && V.xs + xb0 < V.nbp;
+    const uint32_t xoff = (uint32_t)(xpw >> 3) * 2048u + (uint32_t)(xj >> 3) * 1024u + (uint32_t)(xpw & 7) * 128u +
+                          ((uint32_t)((xj & 7) ^ (xpw & 7)) << 4);
+    const size_t pstride = (size_t)4 * V.nbp;  // halves per plane wave
+    const __half* xsrc = V.planes + (size_t)kX * V.npwx * pstride + V.xs + xb0;
+    const int16_t* mp = V.map + (size_t)kl * V.nlf * V.nsum_max + xpw;
+    // Y copies (charge): e = tid + VM_WORKERS v over 2 halves x 64 K rows x NYN / 8 chunks
+    constexpr int YCH = NYN / 8, YE = CURRENT ? 0 : 128 * YCH, YV = (YE + VM_WORKERS - 1) / VM_WORKERS + (CURRENT ? 1 : 0);
+    // ysrc: plane * nbp + band (bits 0-15), plane wave of the chunk (bits 16-20),
+    // zero fill (bit 22); -1: no copy
+    uint32_t ydst[YV];
+    int ysrc[YV];
+#pragma unroll
+    for (int v = 0; v < YV; ++v) {
+      const int e = tid + VM_WORKERS * v;
+      ysrc[v] = -1;
+      ydst[v] = 0;
+      if (e < YE) {
+        const int line = e / YCH, j = e - line * YCH;
+        const int half = line >> 6, kk = line & 63, part = kk >> 5, pw = kk & 31;
+        const int col = 8 * j, u = 2 * half + part;
+        const int band = V.ys + col;
+        ydst[v] = 2 * XH + (uint32_t)half * YH + (uint32_t)(kk >> 3) * (NYA * 1024u) + (uint32_t)(col >> 6) * 1024u +
+                  (uint32_t)(kk & 7) * 128u + ((uint32_t)(((col >> 3) & 7) ^ (kk & 7)) << 4);
+        ysrc[v] = (band < V.nbp ? u * V.nbp + band : (1 << 22)) | (pw << 16);
+      }
+    }
+    const __half* ysrc_c = V.planes + (size_t)kY * V.npwx * pstride;
+    // current vertices: forming thread tid < 128, tasks f = tid + 128 r (r < FR) =
+    // (8-band chunk f / 32 of the c block, plane wave f % 32 = lane): copies the
+    // four planes of the c block, then writes the b(i) c block beside them
+    constexpr int FR = CURRENT ? (NBY * 4 + 127) / 128 : 1;
+    const bool former = CURRENT && tid < 128;
+    uint32_t fco[FR], fbo[FR];  // Re-hi offsets (within the stage) of the c and b c chunks; Im: + 4 NYA 1024, lo: + YH
+    int fsrc[FR];               // plane-row offset (halves) of the c chunk, -1: beyond the tasks, -2: zero fill
+#pragma unroll
+    for (int r = 0; r < FR; ++r) {
+      const int f = tid + 128 * r, j = f >> 5, pw = f & 31;
+      const int col = 8 * j, colb = NBY + col;
+      fco[r] = 2 * XH + (uint32_t)(pw >> 3) * (NYA * 1024u) + (uint32_t)(col >> 6) * 1024u + (uint32_t)(pw & 7) * 128u +
+               ((uint32_t)(((col >> 3) & 7) ^ (pw & 7)) << 4);
+      fbo[r] = 2 * XH + (uint32_t)(pw >> 3) * (NYA * 1024u) + (uint32_t)(colb >> 6) * 1024u + (uint32_t)(pw & 7) * 128u +
+               ((uint32_t)(((colb >> 3) & 7) ^ (pw & 7)) << 4);
+      fsrc[r] = (!former || f >= NBY * 4) ? -1 : (V.ys + col < V.nbp ? V.ys + col : -2);
+    }
+    const float* bsrc = CURRENT ? V.btab + (size_t)kl * V.nsum_max + lane : nullptr;
+    const uint32_t fb_off = Cfg::B_OFF + (uint32_t)warp * 128u + (uint32_t)lane * 4u;
+
+    // b(i) c chunks of the chunk in a stage, from this thread's own c copies
+    auto form = [&](int stage) {
+      if constexpr (CURRENT) {
+        if (!former) return;
+        const uint32_t st = sbase + (uint32_t)stage * STAGE;
+        const float b = lds_f32(st + fb_off);
+#pragma unroll
+        for (int r = 0; r < FR; ++r) {
+          if (fsrc[r] == -1) continue;
+          const uint32_t ci = 4 * NYA * 1024u;
+          uint4 rh = lds16(st + fco[r]), ih = lds16(st + fco[r] + ci);
+          uint4 rl = lds16(st + fco[r] + YH), il = lds16(st + fco[r] + YH + ci);
+          uint32_t* prh = &rh.x;
+          uint32_t* pih = &ih.x;
+          uint32_t* prl = &rl.x;
+          uint32_t* pil = &il.x;
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&prh[e]));
+            const float2 c = __half22float2(*reinterpret_cast<const __half2*>(&pih[e]));
+            const float2 al = __half22float2(*reinterpret_cast<const __half2*>(&prl[e]));
+            const float2 cl = __half22float2(*reinterpret_cast<const __half2*>(&pil[e]));
+            uint32_t ohr = 0, ohi = 0, olr = 0, oli = 0;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const float re = ((h ? a.y : a.x) + (h ? al.y : al.x)) * b;
+              const float im = ((h ? c.y : c.x) + (h ? cl.y : cl.x)) * b;
+              const __half2 hh = __floats2half2_rn(re, im);
+              const float2 hf = __half22float2(hh);
+              const __half2 ll = __floats2half2_rn(re - hf.x, im - hf.y);
+              const __half2_raw hr = hh, lr = ll;
+              ohr |= (uint32_t)hr.x << (16 * h);
+              ohi |= (uint32_t)hr.y << (16 * h);
+              olr |= (uint32_t)lr.x << (16 * h);
+              oli |= (uint32_t)lr.y << (16 * h);
+            }
+            prh[e] = ohr;
+            pih[e] = ohi;
+            prl[e] = olr;
+            pil[e] = oli;
+          }
+          sts16(st + fbo[r], rh);
+          sts16(st + fbo[r] + ci, ih);
+          sts16(st + fbo[r] + YH, rl);
+          sts16(st + fbo[r] + YH + ci, il);
+        }
+      }
+    };
+
+    struct Cur {
+      int gt, c;
+    };
+    auto advance = [&](Cur& u) {
+      if (++u.c == nchunk) u.c = 0, ++u.gt;
+    };
+    // plane-wave chunk swept at position c of tile gt (alternating direction)
+    auto chunk_of = [&](Cur u) { return (u.gt & 1) ? nchunk - 1 - u.c : u.c; };
+    auto load_pos = [&](Cur u) -> int {
+      const int G = u.gt * GPT + xg;
+      if (u.gt >= ngt || !xok || G >= V.nlf) return -1;
+      return (int)mp[(size_t)G * V.nsum_max + chunk_of(u) * VM_I];
+    };
+    auto issue = [&](Cur u, int stage, int pos) {
+      if (u.gt < ngt) {
+        const uint32_t st = sbase + (uint32_t)stage * STAGE;
+        const __half* src = xsrc + (size_t)(pos >= 0 ? pos : 0) * pstride;
+        const uint32_t sz = pos >= 0 ? 16u : 0u;
+#pragma unroll
+        for (int u4 = 0; u4 < 4; ++u4)
+          cp16z(st + xoff + (uint32_t)(u4 >> 1) * XH + (uint32_t)(u4 & 1) * 8192u, src + u4 * V.nbp, sz);
+        const int i0 = chunk_of(u) * VM_I;
+        if constexpr (CURRENT) {
+          if (former) {
+            const int i = i0 + lane;
+#pragma unroll
+            for (int r = 0; r < FR; ++r) {
+              if (fsrc[r] == -1) continue;
+              const bool ok = fsrc[r] >= 0 && i < nsum;
+              const __half* src = ok ? ysrc_c + (size_t)i * pstride + fsrc[r] : ysrc_c;
+              const uint32_t sz = ok ? 16u : 0u;
+              cp16z(st + fco[r], src, sz);
+              cp16z(st + fco[r] + 4 * NYA * 1024u, src + V.nbp, sz);
+              cp16z(st + fco[r] + YH, src + 2 * V.nbp, sz);
+              cp16z(st + fco[r] + YH + 4 * NYA * 1024u, src + 3 * V.nbp, sz);
+            }
+            cp4(st + fb_off, bsrc + i0);
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < YV; ++v) {
+          if (CURRENT || ysrc[v] < 0) continue;
+          const int i = i0 + ((ysrc[v] >> 16) & 31);
+          const bool ok = !(ysrc[v] & (1 << 22)) && i < nsum;
+          const int so = ysrc[v] & 0xffff;
+          cp16z(st + ydst[v], ok ? ysrc_c + (size_t)i * pstride + so : ysrc_c, ok ? 16u : 0u);
+        }
+      }
+      cp_commit();
+    };
+
+    // accumulator slice: TMEM lane quadrant wq, columns cg CW .. cg CW + CW - 1 of each block
+    const int wq = warp & 3, cg = warp >> 2;
+    const int row_t = wq * 32 + lane;
+    const int eg = row_t / XB, ea = row_t - eg * XB;
+    float accR[CW], accI[CW];
+#pragma unroll
+    for (int j = 0; j < CW; ++j) accR[j] = accI[j] = 0.f;
+    float fa = 0.f;
+    auto set_afac = [&](int gt) {
+      const int G = gt * GPT + eg;
+      fa = 0.f;
+      if (CURRENT && eg < GPT && G < V.nlf) {
+        const double* kv = V.ktot + 3 * ik;
+        const double* gl = V.Glf + 3 * G;
+        const int mu = V.comp;
+        const double qmu = mu == 0 ? V.q0 : (mu == 1 ? V.q1 : V.q2);
+        fa = (float)(0.5 * V.Gcar * (qmu + 2.0 * kv[mu] + gl[mu])) * V.a_scale;
+      }
+    };
+    auto consume = [&](int t) -> bool {
+      if (!tc::mbar_wait(&done[t & 1], (uint32_t)((t >> 1) & 1), VM_SPINS)) {
+        atomicExch(V.status, 1);
+        abort_flag = 1;
+        return false;
+      }
+      tc::tc_fence_after();
+      const uint32_t ad = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)((t & 1) * Cfg::BUFC + cg * CW);
+      {
+        float v[CW];
+        tmem_ld_n<CW>(ad, v);
+        if constexpr (CURRENT) {
+          float w[CW];
+          tmem_ld_n<CW>(ad + NBY, w);
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < CW; ++j) accR[j] += fmaf(fa, v[j], w[j]);
+        } else {
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < CW; ++j) accR[j] += v[j];
+        }
+      }
+      {
+        float v[CW];
+        tmem_ld_n<CW>(ad + NYN, v);
+        if constexpr (CURRENT) {
+          float w[CW];
+          tmem_ld_n<CW>(ad + NYN + NBY, w);
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < CW; ++j) accI[j] += fmaf(fa, v[j], w[j]);
+        } else {
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < CW; ++j) accI[j] += v[j];
+        }
+      }
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&tfree[t & 1]);
+      return true;
+    };
+    float amx = 0.f;
+    const float isign = V.swap ? -V.out_scale : V.out_scale;
+    auto write_out = [&](int gt) {
+      const int G = gt * GPT + eg;
+      if (eg < GPT && G < V.nlf) {
+#pragma unroll
+        for (int j = 0; j < CW; ++j) {
+          const int lt = ptab[ea * NBY + cg * CW + j];
+          if (lt >= 0) {
+            const int r = V.pos_of[t0 + lt];
+            const float re = accR[j] * V.out_scale, im = accI[j] * isign;
+            V.M[(size_t)r * V.nlf + G] = make_float2(re, im);
+            amx = fmaxf(amx, fmaxf(fabsf(re), fabsf(im)));
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < CW; ++j) accR[j] = accI[j] = 0.f;
+    };
+
+    // prologue: chunks 0 .. S-2 in flight.  The Gfast positions of a chunk are
+    // loaded two chunks ahead into one of two registers that alternate by
+    // chunk parity (the loop below is unrolled by two), so a pending load is
+    // never copied between registers.
+    Cur ui = {0, 0}, ug = {0, 0};
+    int pA = load_pos(ug);
+    advance(ug);
+    int pB = load_pos(ug);
+    advance(ug);
+    auto issue_with = [&](int stage, int& R) {
+      issue(ui, stage, R);
+      advance(ui);
+      R = load_pos(ug);
+      advance(ug);
+    };
+#pragma unroll
+    for (int s = 0; s < S - 1; ++s) issue_with(s, (s & 1) ? pB : pA);
+    cp_wait<S - 2>();
+    form(0);
+    tc::fence_async_smem();
+    __syncwarp();
+    if (lane == 0) tc::mbar_arrive(&full[0]);
+    set_afac(0);
+    Cur uc = {0, 0};   // chunk read back next
+    int si = S - 1;    // stage of the next chunk to issue
+    int sf = 1 % S;    // stage of chunk j + 1
+    bool fail = false;
+    auto body = [&](int j, int& R) -> bool {
+      if (j >= 1) {
+        if (!consume(j - 1)) return false;
+        if (uc.c == nchunk - 1) {
+          write_out(uc.gt);
+          set_afac(uc.gt + 1);
+        }
+        advance(uc);
+      }
+      issue_with(si, R);
+      si = si + 1 == S ? 0 : si + 1;
+      cp_wait<S - 2>();
+      if (j + 1 < total) form(sf);
+      tc::fence_async_smem();
+      __syncwarp();
+      if (lane == 0 && j + 1 < total) tc::mbar_arrive(&full[sf]);
+      sf = sf + 1 == S ? 0 : sf + 1;
+      return !abort_flag;
+    };
+    // chunk j + S - 1 is issued at step j: its positions are in pA for even
+    // j + S - 1, pB for odd
+    int& R0 = ((S - 1) & 1) ? pB : pA;
+    int& R1 = ((S - 1) & 1) ? pA : pB;
+    for (int j = 0; j < total; j += 2) {
+      if (!body(j, R0) || (j + 1 < total && !body(j + 1, R1))) {
+        fail = true;
+        break;
+      }
+    }
+    if (!fail && consume(total - 1)) write_out(ngt - 1);
+    cp_wait<0>();
+    for (int o = 16; o > 0; o >>= 1) amx = fmaxf(amx, __shfl_xor_sync(0xffffffffu, amx, o));
+    if (lane == 0) atomicMax(V.amax, __float_as_uint(amx));
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, Cfg::NCOL);
+}
+
+// b(i) = Gcar (R1 G1_i)_mu sB / 2^14 of every FBZ k-point of the launch, zero
+// beyond nsum: btab[k_local][i].
+struct BtabCtx {
+  const int* kmap;
+  const double* G;
+  const double* Rcart;
+  const int* gidx;
+  const int* npw;
+  float* btab;
+  int k0, nk, npwx, nsum_max, legacy, nsum_legacy, comp;
+  double Gcar;
+  float sB;
+};
+
+__global__ void k_vtx_btab_mn(BtabCtx Y) {
+  const size_t n = (size_t)Y.nk * Y.nsum_max;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % Y.nsum_max), kl = (int)(e / Y.nsum_max);
+    const int* km = Y.kmap + 5 * (Y.k0 + kl);
+    const int K1 = km[0];
+    const int nsum = Y.legacy ? Y.nsum_legacy : Y.npw[K1];
+    float b = 0.f;
+    if (i < nsum) {
+      const double* R = Y.Rcart + 9 * km[1] + 3 * Y.comp;
+      const double* g1 = Y.G + 3 * Y.gidx[(size_t)K1 * Y.npwx + i];
+      b = (float)(Y.Gcar * (R[0] * g1[0] + R[1] * g1[1] + R[2] * g1[2])) * Y.sB * (1.0f / 16384.0f);
+    }
+    Y.btab[e] = b;
+  }
+}
+
+template <int NBY, bool CURRENT>
+static int launch_vmn(rpa_ctx* c, const VtxMnCtx& V, int nk) {
+  using Cfg = VmCfg<NBY, CURRENT>;
+  auto kern = k_vertex_mn<NBY, CURRENT>;
+  RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM));
+  kern<<<nk, VM_THREADS, Cfg::SMEM, c->stream>>>(V);
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  return RPA_OK;
+}
+
+template <bool CURRENT>
+static int launch_vmn_nby(rpa_ctx* c, const VtxMnCtx& V, int nk, int nby) {
+  switch (nby) {
+    case 16: return launch_vmn<16, CURRENT>(c, V, nk);
+    case 32: return launch_vmn<32, CURRENT>(c, V, nk);
+    case 48: return launch_vmn<48, CURRENT>(c, V, nk);
+    case 64: return launch_vmn<64, CURRENT>(c, V, nk);
+    default: break;
+  }
+  if constexpr (!CURRENT) {
+    if (nby == 80) return launch_vmn<80, false>(c, V, nk);
+    if (nby == 96) return launch_vmn<96, false>(c, V, nk);
+  }
+  return fail(c, RPA_EINVAL, "vertices: no kernel for a %d-band window", nby);
+}
+
+// One launch per pair of band windows: gathered bands [x0, x1) in windows of
+// 32 starting on multiples of 8, sequential bands [y0, y1) in windows of at most
+// ymax (multiples of 16 wide, starting on a multiple of 8).
+template <bool CURRENT>
+static int launch_windows_mn(rpa_ctx* c, VtxMnCtx V, int nk, int x0, int x1, int y0, int y1, int ymax) {
+  const int ys0 = y0 & ~7, span = y1 - ys0;
+  const int nyw = (span + ymax - 1) / ymax;
+  const int W = ((span + nyw - 1) / nyw + 15) / 16 * 16;
+  for (int ws = x0 & ~7; ws < x1; ws += 32) {
+    V.xs = ws;
+    V.xo0 = std::max(x0, ws);
+    V.xo1 = std::min(x1, ws + 32);
+    V.xb = (V.xo1 - ws + 7) / 8 * 8;
+    V.gpt = 128 / V.xb;
+    for (int w = 0; w < nyw; ++w) {
+      V.ys = ys0 + w * W;
+      V.yo0 = std::max(y0, V.ys);
+      V.yo1 = std::min(y1, V.ys + W);
+      if (V.yo1 <= V.yo0) continue;
+      RPA_TRY(launch_vmn_nby<CURRENT>(c, V, nk, W));
+    }
+  }
+  return RPA_OK;
+}
+
+static double pow2_floor_m(double x) { return std::ldexp(1.0, (int)std::floor(std::log2(x))); }
+
+// Mixed-path vertices of the FBZ k-points [k0, k0+nk) with MN-major operands.
+// Leaves *used false when the plane-wave count does not fit the int16 map
+// positions or the band count the int16 pair table (the caller then uses the
+// CUDA-core kernel).
+int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans, const int* pos_of, float2* Mf,
+                float2* Mf2, unsigned* amax, bool* used) {
+  *used = false;
+  if (n_trans == 0) return RPA_OK;
+  if (c->npwx > 32767 || c->nbnd > 181 || c->d_cpl.p == nullptr) return RPA_OK;
+  const bool current = P.mode == RPA_MODE_CURRENT;
+  const bool two = current && (P.pol == RPA_POL_YZ || P.pol == RPA_POL_ZY);
+  const bool swap = !current && !c->legacy && P.nocc < c->nbnd - P.nocc;
+  int x0, x1, y0, y1;
+  if (current) {
+    x0 = 0, x1 = c->nbnd, y0 = 0, y1 = c->nbnd;
+  } else if (swap) {
+    x0 = 0, x1 = P.nocc, y0 = P.nocc, y1 = c->nbnd;
+  } else {
+    x0 = P.nocc, x1 = c->nbnd, y0 = 0, y1 = P.nocc;
+  }
+  if (x1 <= x0 || y1 <= y0) return RPA_OK;
+  // sequential side: plane waves of K1 (K2 when swapped)
+  int nsum_max = 0;
+  for (int i = 0; i < nk; ++i) {
+    const int* km = &c->h_kmap[5 * (size_t)(k0 + i)];
+    nsum_max = std::max(nsum_max, c->legacy ? P.nsum_legacy : c->h_npw[swap ? km[2] : km[0]]);
+  }
+  nsum_max = (nsum_max + VM_I - 1) / VM_I * VM_I;
+  const int16_t* map;
+  if (swap) {
+    const size_t gbytes = (size_t)nk * c->nlf * nsum_max * sizeof(int16_t);
+    if (!(c->ginv_valid && c->ginv_k0 == k0 && c->ginv_nk == nk && c->ginv_nsum == nsum_max)) {
+      RPA_TRY(ensure(c, c->d_ginv, gbytes));
+      RPA_TRY(build_ginv(c, k0, nk, nsum_max, c->d_ginv.as<int16_t>()));
+      c->ginv_valid = true;
+      c->ginv_k0 = k0;
+      c->ginv_nk = nk;
+      c->ginv_nsum = nsum_max;
+    }
+    map = c->d_ginv.as<int16_t>();
+  } else {
+    const size_t gbytes = (size_t)nk * c->nlf * nsum_max * sizeof(int16_t);
+    if (!(c->gmap_valid && c->gmap_k0 == k0 && c->gmap_nk == nk && c->gmap_nsum == nsum_max &&
+          c->gmap_legacy_n == P.nsum_legacy)) {
+      RPA_TRY(ensure(c, c->d_gmap, gbytes));
+      RPA_TRY(build_gmap(c, k0, nk, nsum_max, c->d_gmap.as<int16_t>(), P.nsum_legacy));
+      c->gmap_valid = true;
+      c->gmap_k0 = k0;
+      c->gmap_nk = nk;
+      c->gmap_nsum = nsum_max;
+      c->gmap_legacy_n = P.nsum_legacy;
+    }
+    map = c->d_gmap.as<int16_t>();
+  }
+  VtxMnCtx V;
+  V.kmap = c->d_kmap.as<int>();
+  V.ktot = c->d_ktot.as<double>();
+  V.Glf = c->d_Glf.as<double>();
+  V.npw = c->d_npw.as<int>();
+  V.planes = c->d_cpl.as<__half>();
+  V.btab = nullptr;
+  V.map = map;
+  V.trans = c->d_trans.as<Trans>();
+  V.offsets = c->d_offsets.as<long long>();
+  V.pos_of = pos_of;
+  V.status = c->d_flags.as<int>() + 3;
+  V.k0 = k0;
+  V.nlf = c->nlf;
+  V.npwx = c->npwx;
+  V.nbp = c->nbp;
+  V.nsum_max = nsum_max;
+  V.legacy = c->legacy ? 1 : 0;
+  V.nsum_legacy = P.nsum_legacy;
+  V.swap = swap ? 1 : 0;
+  V.q0 = c->q[0];
+  V.q1 = c->q[1];
+  V.q2 = c->q[2];
+  V.Gcar = P.Gcar;
+  if (!current) {
+    V.comp = 0;
+    V.a_scale = 0.0f;
+    V.out_scale = (float)(1.0 / (16384.0 * 16384.0));
+    V.M = Mf;
+    V.amax = amax;
+    *used = true;
+    return launch_windows_mn<false>(c, V, nk, x0, x1, y0, y1, 96);
+  }
+  // current vertices: |C| <= 1 (orthonormal bands), |b(i)| <= Gcar max|G|
+  double gmax = 0.0;
+  for (size_t g = 0; g < c->h_G.size() / 3; ++g) {
+    const double* v = &c->h_G[3 * g];
+    gmax = std::max(gmax, std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+  }
+  const double bmax = std::max(P.Gcar * gmax, 1e-30);
+  const float sB = (float)(16384.0 / pow2_floor_m(bmax * 1.5));
+  V.a_scale = sB / 16384.0f;
+  V.out_scale = (float)(1.0 / (16384.0 * (double)sB));
+  int comps[2];
+  switch (P.pol) {
+    case RPA_POL_XX: comps[0] = comps[1] = 0; break;
+    case RPA_POL_YY: comps[0] = comps[1] = 1; break;
+    case RPA_POL_ZZ: comps[0] = comps[1] = 2; break;
+    case RPA_POL_YZ: comps[0] = 1; comps[1] = 2; break;
+    default: comps[0] = 2; comps[1] = 1; break;
+  }
+  RPA_TRY(ensure(c, c->d_vbt, sizeof(float) * (size_t)nk * nsum_max));
+  V.btab = c->d_vbt.as<float>();
+  BtabCtx Y;
+  Y.kmap = V.kmap;
+  Y.G = c->d_G.as<double>();
+  Y.Rcart = c->d_Rcart.as<double>();
+  Y.gidx = c->d_gidx.as<int>();
+  Y.npw = V.npw;
+  Y.btab = c->d_vbt.as<float>();
+  Y.k0 = k0;
+  Y.nk = nk;
+  Y.npwx = c->npwx;
+  Y.nsum_max = nsum_max;
+  Y.legacy = V.legacy;
+  Y.nsum_legacy = P.nsum_legacy;
+  Y.Gcar = P.Gcar;
+  Y.sB = sB;
+  // the yz / zy pair: one pass per Cartesian component
+  for (int a = 0; a < (two ? 2 : 1); ++a) {
+    V.comp = Y.comp = comps[a];
+    V.M = a == 0 ? Mf : Mf2;
+    V.amax = amax + a;
+    k_vtx_btab_mn<<<2048, 256, 0, c->stream>>>(Y);
+    RPA_CUDA(c, cudaGetLastError());
+    ++c->launches;
+    RPA_TRY(launch_windows_mn<true>(c, V, nk, x0, x1, y0, y1, 64));
+  }
+  *used = true;
+  return RPA_OK;
+}
+
+}  // namespace rpa

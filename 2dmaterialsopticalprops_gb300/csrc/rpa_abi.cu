@@ -31,6 +31,8 @@ int qeff_f32(rpa_ctx* c, int n_inter, int n_trans, const float2* Mf, const float
 int cmax_of(rpa_ctx* c, int n_inter, double* cmax);
 int vertices_f32(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, long long n_trans, const int* pos_of,
                  float2* Mf, float2* Mf2, unsigned* amax);
+int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans, const int* pos_of, float2* Mf,
+                float2* Mf2, unsigned* amax, bool* used);
 int vertices_tc(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans, const int* pos_of, float2* Mf,
                 float2* Mf2, unsigned* amax, bool* used);
 int qeff_fp64(rpa_ctx* c, const Chi0Plan& P, int n_inter, int n_trans);
@@ -100,6 +102,33 @@ __global__ void k_to_f32(const double2* __restrict__ src, float2* __restrict__ d
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     double2 v = src[e];
     dst[e] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+// Coefficients scaled by 2^14 and split into fp16 hi + lo halves (as
+// k_to_split16), stored as four planes per plane wave, [re_hi, im_hi, re_lo,
+// im_lo][nbp bands], zero beyond nbnd: a run of bands of one plane wave is
+// contiguous for the MN-major vertex operands.
+__global__ void k_to_planes16(const double2* __restrict__ src, __half* __restrict__ dst, size_t nrows, int nbnd,
+                              int nbp) {
+  const size_t n = nrows * nbp;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t row = e / nbp;
+    const int b = (int)(e % nbp);
+    float re = 0.f, im = 0.f;
+    if (b < nbnd) {
+      const double2 v = src[row * nbnd + b];
+      re = (float)v.x * 16384.0f;
+      im = (float)v.y * 16384.0f;
+    }
+    const __half2 hi = __floats2half2_rn(re, im);
+    const float2 h = __half22float2(hi);
+    const __half2 lo = __floats2half2_rn(re - h.x, im - h.y);
+    __half* d = dst + row * 4 * nbp + b;
+    d[0] = __low2half(hi);
+    d[nbp] = __high2half(hi);
+    d[2 * nbp] = __low2half(lo);
+    d[3 * nbp] = __high2half(lo);
   }
 }
 
@@ -261,7 +290,7 @@ int rpa_create(rpa_ctx** out, const rpa_opts* opts) {
   c->verbose = opts ? opts->verbose : 0;
   c->split_f16 = opts ? opts->split == 0 : true;
   c->tc_seg = (opts && opts->reserved[0] > 0) ? opts->reserved[0] : 1;
-  c->vertex_tc = !(opts && opts->reserved[1] == 1);
+  c->vertex_kind = (opts && (opts->reserved[1] == 1 || opts->reserved[1] == 2)) ? opts->reserved[1] : 0;
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete c;
@@ -294,7 +323,8 @@ int rpa_create_shared(rpa_ctx** out, rpa_ctx* parent, int precision) {
   c->verbose = parent->verbose;
   c->split_f16 = parent->split_f16;
   c->tc_seg = parent->tc_seg;
-  c->vertex_tc = parent->vertex_tc;
+  c->vertex_kind = parent->vertex_kind;
+  c->nbp = parent->nbp;
   c->ng = parent->ng;
   c->h_miller = parent->h_miller;
   c->h_G = parent->h_G;
@@ -313,10 +343,10 @@ int rpa_create_shared(rpa_ctx** out, rpa_ctx* parent, int precision) {
   c->h_npw = parent->h_npw;
   c->h_E = parent->h_E;
   DevBuf* mine[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
-                    &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_coeffs, &c->d_E};
+                    &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_coeffs, &c->d_cpl, &c->d_E};
   const DevBuf* theirs[] = {&parent->d_miller, &parent->d_G, &parent->d_box, &parent->d_Rc, &parent->d_RIc,
                             &parent->d_Rcart, &parent->d_npw, &parent->d_gidx, &parent->d_inv, &parent->d_coeff,
-                            &parent->d_coeff32, &parent->d_coeffs, &parent->d_E};
+                            &parent->d_coeff32, &parent->d_coeffs, &parent->d_cpl, &parent->d_E};
   for (size_t i = 0; i < sizeof(mine) / sizeof(mine[0]); ++i) *mine[i] = *theirs[i];
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -338,14 +368,14 @@ int rpa_destroy(rpa_ctx* c) {
   if (c->parent) {
     // borrowed from the parent: not ours to free
     DevBuf* borrowed[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
-                          &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_coeffs, &c->d_E};
+                          &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_coeffs, &c->d_cpl, &c->d_E};
     for (DevBuf* b : borrowed) *b = DevBuf();
     --c->parent->children;
   }
   DevBuf* bufs[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
-                    &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_coeffs, &c->d_E, &c->d_kmap, &c->d_ktot, &c->d_lf_miller,
+                    &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_coeffs, &c->d_cpl, &c->d_E, &c->d_kmap, &c->d_ktot, &c->d_lf_miller,
                     &c->d_Glf, &c->d_occ, &c->d_counts, &c->d_offsets, &c->d_trans, &c->d_keys, &c->d_keys_alt,
-                    &c->d_vals, &c->d_vals_alt, &c->d_sorted, &c->d_M, &c->d_M2, &c->d_Mf, &c->d_Mf2, &c->d_tiles, &c->d_tilesA, &c->d_gmap, &c->d_vbt, &c->d_cub, &c->d_wmax,
+                    &c->d_vals, &c->d_vals_alt, &c->d_sorted, &c->d_M, &c->d_M2, &c->d_Mf, &c->d_Mf2, &c->d_tiles, &c->d_tilesA, &c->d_gmap, &c->d_ginv, &c->d_vbt, &c->d_cub, &c->d_wmax,
                     &c->d_ntrans, &c->d_S, &c->d_Sdf, &c->d_Q, &c->d_chi0, &c->d_kk, &c->d_kkf, &c->d_V, &c->d_eps, &c->d_WT,
                     &c->d_flags, &c->d_tmp};
   for (DevBuf* b : bufs) release(*b);
@@ -359,7 +389,7 @@ int rpa_destroy(rpa_ctx* c) {
 const char* rpa_last_error(const rpa_ctx* c) { return c ? c->err.c_str() : g_create_err.c_str(); }
 
 int rpa_set_gvectors(rpa_ctx* c, int ng, const int* miller, const double* G, const double* KC) {
-  if (c) c->gmap_valid = false;
+  if (c) c->gmap_valid = c->ginv_valid = false;
   if (c && (c->parent || c->children > 0))
     return fail(c, RPA_ESTATE, "rpa_set_gvectors: the G list and basis are shared between contexts");
   if (!c || ng <= 0 || !miller || !G || !KC) return fail(c, RPA_EINVAL, "rpa_set_gvectors: bad arguments");
@@ -400,7 +430,7 @@ int rpa_set_gvectors(rpa_ctx* c, int ng, const int* miller, const double* G, con
 }
 
 int rpa_set_symmetry(rpa_ctx* c, int nsym, const double* R, const double* RI) {
-  if (c) c->gmap_valid = false;
+  if (c) c->gmap_valid = c->ginv_valid = false;
   if (c && (c->parent || c->children > 0))
     return fail(c, RPA_ESTATE, "rpa_set_symmetry: the G list and basis are shared between contexts");
   if (!c || nsym < 1 || nsym > 48 || !R || !RI) return fail(c, RPA_EINVAL, "rpa_set_symmetry: bad arguments");
@@ -416,7 +446,7 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
                    const double* E) {
   if (c && (c->parent || c->children > 0))
     return fail(c, RPA_ESTATE, "rpa_load_basis: the G list and basis are shared between contexts");
-  if (c) c->gmap_valid = false;
+  if (c) c->gmap_valid = c->ginv_valid = false;
   if (!c || nks <= 0 || nbnd <= 0 || npwx <= 0 || !npw || !coeff || !E)
     return fail(c, RPA_EINVAL, "rpa_load_basis: bad arguments");
   if (c->ng == 0) return fail(c, RPA_ESTATE, "rpa_load_basis: call rpa_set_gvectors first");
@@ -481,10 +511,18 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
     k_to_f32<<<2048, 256, 0, c->stream>>>(c->d_coeff.as<double2>(), c->d_coeff32.as<float2>(), per_k * nks);
     RPA_CUDA(c, cudaGetLastError());
     ++c->launches;
-    RPA_TRY(ensure(c, c->d_coeffs, sizeof(uint2) * per_k * nks));
-    k_to_split16<<<2048, 256, 0, c->stream>>>(c->d_coeff.as<double2>(), c->d_coeffs.as<uint2>(), per_k * nks);
+    c->nbp = (nbnd + 7) / 8 * 8;
+    RPA_TRY(ensure(c, c->d_cpl, sizeof(__half) * (size_t)nks * npwx * 4 * c->nbp));
+    k_to_planes16<<<2048, 256, 0, c->stream>>>(c->d_coeff.as<double2>(), c->d_cpl.as<__half>(), (size_t)nks * npwx,
+                                               nbnd, c->nbp);
     RPA_CUDA(c, cudaGetLastError());
     ++c->launches;
+    if (c->vertex_kind == 2) {
+      RPA_TRY(ensure(c, c->d_coeffs, sizeof(uint2) * per_k * nks));
+      k_to_split16<<<2048, 256, 0, c->stream>>>(c->d_coeff.as<double2>(), c->d_coeffs.as<uint2>(), per_k * nks);
+      RPA_CUDA(c, cudaGetLastError());
+      ++c->launches;
+    }
   }
   cudaEventRecord(c->ev[7], c->stream);
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -495,7 +533,7 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
 
 int rpa_kmap(rpa_ctx* c, int ntot, const double* ktot, const int* K1, const int* R1, const int* K2, const int* R2,
              const int* iG0) {
-  if (c) c->gmap_valid = false;
+  if (c) c->gmap_valid = c->ginv_valid = false;
   if (!c || ntot <= 0 || !ktot || !K1 || !R1 || !K2 || !R2 || !iG0)
     return fail(c, RPA_EINVAL, "rpa_kmap: bad arguments");
   if (c->nks == 0) return fail(c, RPA_ESTATE, "rpa_kmap: call rpa_load_basis first");
@@ -522,7 +560,7 @@ int rpa_kmap(rpa_ctx* c, int ntot, const double* ktot, const int* K1, const int*
 }
 
 int rpa_set_q(rpa_ctx* c, const double* q, int nlf, const int* ilf, const int* parG) {
-  if (c) c->gmap_valid = false;
+  if (c) c->gmap_valid = c->ginv_valid = false;
   if (!c || !q || nlf <= 0 || !ilf) return fail(c, RPA_EINVAL, "rpa_set_q: bad arguments");
   if (nlf > 1000) return fail(c, RPA_EINVAL, "Nlf = %d exceeds the gjel limit NMAX = 1000", nlf);
   if (c->ng == 0) return fail(c, RPA_ESTATE, "rpa_set_q: call rpa_set_gvectors first");
@@ -690,7 +728,10 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
       RPA_CUDA(c, cudaMemsetAsync(c->d_ntrans.p, 0, 32, c->stream));
       cudaEventRecord(c->ev[2], c->stream);
       bool used_tc = false;
-      if (c->vertex_tc) RPA_TRY(vertices_tc(c, P, k0, nk, tot, pos_of, Mf, Mf2, c->d_ntrans.as<unsigned>(), &used_tc));
+      if (c->vertex_kind == 0)
+        RPA_TRY(vertices_mn(c, P, k0, nk, tot, pos_of, Mf, Mf2, c->d_ntrans.as<unsigned>(), &used_tc));
+      else if (c->vertex_kind == 2)
+        RPA_TRY(vertices_tc(c, P, k0, nk, tot, pos_of, Mf, Mf2, c->d_ntrans.as<unsigned>(), &used_tc));
       if (!used_tc) RPA_TRY(vertices_f32(c, P, k0, nk, maxp, tot, pos_of, Mf, Mf2, c->d_ntrans.as<unsigned>()));
       cudaEventRecord(c->ev[3], c->stream);
       double cmax = 0.0;

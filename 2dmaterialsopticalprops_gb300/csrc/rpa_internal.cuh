@@ -43,7 +43,7 @@ struct rpa_ctx {
   int verbose = 0;
   bool split_f16 = true;  // mixed path: fp16 (scaled) or bf16 hi/lo operands
   int tc_seg = 1;         // mixed path: chunks per TMEM accumulation segment
-  bool vertex_tc = true;  // mixed path: vertices on the tensor cores (else FP32 CUDA cores)
+  int vertex_kind = 0;    // mixed-path vertices: 0 tensor cores (MN-major), 1 FP32 CUDA cores, 2 tensor cores (K-major)
   cudaStream_t stream = nullptr;
   std::string err;
   // a context made by rpa_create_shared borrows the G list, symmetry and basis
@@ -70,7 +70,8 @@ struct rpa_ctx {
   bool legacy = false;
   std::vector<int> h_npw;
   std::vector<double> h_E;        // [k][b]
-  rpa::DevBuf d_npw, d_gidx, d_inv, d_coeff, d_coeff32, d_coeffs, d_E;
+  int nbp = 0;                    // bands rounded up to 8 (coefficient planes)
+  rpa::DevBuf d_npw, d_gidx, d_inv, d_coeff, d_coeff32, d_coeffs, d_cpl, d_E;
 
   // k map
   int ntot = 0;
@@ -87,10 +88,13 @@ struct rpa_ctx {
 
   // per-call scratch
   rpa::DevBuf d_occ, d_counts, d_offsets, d_trans, d_keys, d_keys_alt, d_vals, d_vals_alt, d_sorted,
-      d_M, d_M2, d_Mf, d_Mf2, d_tiles, d_tilesA, d_gmap, d_vbt, d_cub, d_wmax, d_ntrans;
+      d_M, d_M2, d_Mf, d_Mf2, d_tiles, d_tilesA, d_gmap, d_ginv, d_vbt, d_cub, d_wmax, d_ntrans;
   // cached Gfast map (int16) of the last k-chunk, valid until the basis, k map or q change
   bool gmap_valid = false;
   int gmap_k0 = 0, gmap_nk = 0, gmap_nsum = 0, gmap_legacy_n = 0;
+  // cached inverse map (gathered K1 plane wave of each K2 plane wave), same validity
+  bool ginv_valid = false;
+  int ginv_k0 = 0, ginv_nk = 0, ginv_nsum = 0;
   // results
   int last_mode = -1, last_no = 0, last_nw = 0;
   double last_domega = 0.0, last_Gcar = 0.0;

@@ -161,6 +161,34 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t smem_addr) {
   return d;
 }
 
+// Shared-memory matrix descriptor, MN-major operand in the 128-byte swizzle
+// layout: atoms of 8 K rows x 128 bytes (64 elements along M or N), the 16-byte
+// chunks of K row k at chunk position c ^ (k % 8); lbo = bytes between atoms
+// along M/N, sbo = bytes between groups of 8 K rows; atoms 1024-byte aligned.
+__device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t smem_addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((smem_addr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D f32, A and B f16, both MN-major; negb
+// negates B.
+__host__ __device__ constexpr uint32_t idesc_f16_mn(int M, int N, bool negb) {
+  return (1u << 4)                        // D format: f32
+         | (negb ? (1u << 14) : 0u)       // negate B
+         | (1u << 15) | (1u << 16)        // A and B MN-major
+         | ((uint32_t)(N >> 3) << 17)     // N / 8
+         | ((uint32_t)(M >> 4) << 24);    // M / 16
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // Instruction descriptor, kind::f16: D f32, A and B bf16 (or f16), both K-major.
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, bool f16 = false) {
   return (1u << 4)                        // D format: f32

@@ -157,12 +157,14 @@ class Context:
     """One rpa_ctx: resident basis + per-q state, Fortran-layout I/O."""
 
     def __init__(self, device: int = 0, precision: int = PREC_FP64, verbose: int = 0, split: int = 0,
-                 tc_seg: int = 0, vertex_simt: bool = False):
+                 tc_seg: int = 0, vertex_simt: bool = False, vertex_kmajor: bool = False):
         self.L = load_library()
         self.h = C.c_void_p()
         opts = RpaOpts(device=device, precision=precision, verbose=verbose, split=split)
         opts.reserved[0] = tc_seg
-        opts.reserved[1] = 1 if vertex_simt else 0
+        # mixed-path vertices: MN-major tensor-core kernel (default), FP32 CUDA cores,
+        # or the K-major tensor-core kernel
+        opts.reserved[1] = 1 if vertex_simt else (2 if vertex_kmajor else 0)
         rc = self.L.rpa_create(C.byref(self.h), C.byref(opts))
         if rc != RPA_OK:
             raise RpaError(rc, self.L.rpa_last_error(None).decode())

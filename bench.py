@@ -48,6 +48,8 @@ def config_of(name: str, q_steps: int):
         return synth.config_grid120(q_steps=q_steps)
     if name == "grid60":  # the grid120 workload on a 60x60 k-grid (profiling-size case)
         return synth.config_grid120(nk=60, q_steps=q_steps)
+    if name == "grid40":  # the grid120 workload on a 40x40 k-grid (1.2 GB basis: ncu-capture size)
+        return synth.config_grid120(nk=40, q_steps=q_steps)
     if name == "grid24":
         return synth.config_grid24()
     if name == "small":

@@ -52,8 +52,9 @@ typedef struct rpa_opts {
                      scaling (default, ~2^-22 per operand), 1 = bf16 hi/lo (~2^-16) */
   int reserved[4]; /* reserved[0]: mixed path, chunks of 32 transitions summed in one
                       TMEM accumulator before read-back (0 -> 1); keep 0.
-                      reserved[1] = 1: mixed-path vertices on FP32 CUDA cores
-                      instead of the tensor cores */
+                      reserved[1]: mixed-path vertex kernel, 0 = tensor cores with
+                      MN-major operands (default), 1 = FP32 CUDA cores, 2 = tensor
+                      cores with K-major operands (transposing 4-byte gathers) */
 } rpa_opts;
 
 /* Arguments of one chi0 accumulation (the namelist values the drivers use).

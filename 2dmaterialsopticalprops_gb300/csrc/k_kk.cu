@@ -260,12 +260,29 @@ int kk_apply_real_fp64(rpa_ctx* c, DevBuf& buf, const std::vector<double>& K, in
 }
 
 int kk_run(rpa_ctx* c, int variant, int no, double domega) {
-  std::vector<double> K;
-  int nw = 0;
-  kk_matrix(variant, no, domega, K, &nw);
+  // the fixed kernel depends on (variant, no, domega) only: built on the host and
+  // copied once, then reused by every transform with the same grid
+  const bool cached = c->kk_key_variant == variant && c->kk_key_no == no && c->kk_key_domega == domega;
+  const int nw = variant == RPA_KK_OPTABS_COMPLEX ? 2 * no + 1 : no;
   const int nrow = no - 1, np = c->nlf * c->nlf;
-  RPA_TRY(ensure(c, c->d_kk, sizeof(double) * K.size()));
-  RPA_CUDA(c, cudaMemcpyAsync(c->d_kk.p, K.data(), sizeof(double) * K.size(), cudaMemcpyHostToDevice, c->stream));
+  if (!cached) {
+    std::vector<double> K;
+    int nwk = 0;
+    kk_matrix(variant, no, domega, K, &nwk);
+    c->kk_key_variant = -1;
+    RPA_TRY(ensure(c, c->d_kk, sizeof(double) * K.size()));
+    RPA_CUDA(c, cudaMemcpyAsync(c->d_kk.p, K.data(), sizeof(double) * K.size(), cudaMemcpyHostToDevice, c->stream));
+    if (c->precision == RPA_PREC_MIXED) {
+      std::vector<float> Kf(K.begin(), K.end());
+      RPA_TRY(ensure(c, c->d_kkf, sizeof(float) * Kf.size()));
+      RPA_CUDA(c, cudaMemcpyAsync(c->d_kkf.p, Kf.data(), sizeof(float) * Kf.size(), cudaMemcpyHostToDevice,
+                                  c->stream));
+    }
+    RPA_CUDA(c, cudaStreamSynchronize(c->stream));  // the host copies of K go out of scope
+    c->kk_key_variant = variant;
+    c->kk_key_no = no;
+    c->kk_key_domega = domega;
+  }
   RPA_TRY(ensure(c, c->d_chi0, sizeof(double2) * (size_t)nrow * np));
   const bool cplx = variant == RPA_KK_OPTABS_COMPLEX;
   const int ncols = cplx ? 2 * np : np;
@@ -273,9 +290,6 @@ int kk_run(rpa_ctx* c, int variant, int no, double domega) {
   // S row holding S0(io-1): Sloss row io-1 (io0), Optabs row (io-1)+no
   const int pi_row0 = cplx ? no : 0;
   if (c->precision == RPA_PREC_MIXED) {
-    std::vector<float> Kf(K.begin(), K.end());
-    RPA_TRY(ensure(c, c->d_kkf, sizeof(float) * Kf.size()));
-    RPA_CUDA(c, cudaMemcpyAsync(c->d_kkf.p, Kf.data(), sizeof(float) * Kf.size(), cudaMemcpyHostToDevice, c->stream));
     dim3 g2((ncols + 127) / 128, (nrow + 31) / 32);
     if (cplx)
       k_kk_f32<true><<<g2, 256, 0, c->stream>>>(c->d_kkf.as<float>(), c->d_S.as<double>(), c->d_chi0.as<double2>(),
@@ -285,7 +299,6 @@ int kk_run(rpa_ctx* c, int variant, int no, double domega) {
                                                  nrow, nw, np, pi_row0);
     RPA_CUDA(c, cudaGetLastError());
     ++c->launches;
-    RPA_CUDA(c, cudaStreamSynchronize(c->stream));  // the host copy of K goes out of scope
     return RPA_OK;
   }
   if (cplx)

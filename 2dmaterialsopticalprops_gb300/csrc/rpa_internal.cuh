@@ -99,6 +99,9 @@ struct rpa_ctx {
   int last_mode = -1, last_no = 0, last_nw = 0;
   double last_domega = 0.0, last_Gcar = 0.0;
   bool have_S = false, have_chi0 = false, have_W = false;
+  // fixed KK kernel on the device (d_kk, d_kkf): the (variant, no, domega) it was built for
+  int kk_key_variant = -1, kk_key_no = 0;
+  double kk_key_domega = 0.0;
   rpa::DevBuf d_S, d_Sdf, d_Q, d_chi0, d_kk, d_kkf, d_V, d_eps, d_WT, d_flags, d_tmp;
   double stage_ms[6] = {0, 0, 0, 0, 0, 0};
   long long launches = 0;  // kernels launched by this context

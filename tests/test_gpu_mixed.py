@@ -97,3 +97,39 @@ def test_mixed_band_windows_over_32(synth, rpa, orc, nbnd, nocc):
     Sco, _ = orc.optabs_s0(orc.Bound(s, pol="zz"))
     assert rel(Sc, Sco) < TOL
     ctx.close()
+
+
+def test_mixed_legacy_basis(synth, rpa, orc):
+    """A basis without an igk map (legacy drivers, NGd coefficients summed): the
+    charge vertices gather the empty bands through Gfast (no inverse map)."""
+    s = synth.build(synth.config_small(igk=False))
+    ctx = rpa.Context(precision=rpa.PREC_MIXED)
+    ctx.load_system(s)
+    S, _ = ctx.chi0(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+    assert rel(S, orc.sloss_s0(orc.Bound(s))) < TOL
+    Sc, Qc = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, "yz"))
+    Sco, Qco = orc.optabs_s0(orc.Bound(s, pol="yz"))
+    assert rel(Sc, Sco) < TOL
+    assert rel(Qc, Qco) < TOL
+    ctx.close()
+
+
+@pytest.mark.parametrize("kind", ["kmajor", "simt"])
+def test_vertex_kernels_agree(synth, rpa, orc, kind):
+    """The MN-major vertex kernel (default), the K-major tensor-core kernel and
+    the FP32 CUDA-core kernel give the same S0 to the mixed-path tolerance."""
+    s = synth.build(synth.config_small(nbnd=12, nocc=3, npw=120, nlf=11, no=31))
+    ref = rpa.Context(precision=rpa.PREC_MIXED)
+    alt = rpa.Context(precision=rpa.PREC_MIXED, vertex_kmajor=kind == "kmajor", vertex_simt=kind == "simt")
+    for c in (ref, alt):
+        c.load_system(s)
+    So = orc.sloss_s0(orc.Bound(s))
+    a, _ = ref.chi0(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+    b, _ = alt.chi0(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+    assert rel(a, So) < TOL and rel(b, So) < TOL
+    Sco, _ = orc.optabs_s0(orc.Bound(s, pol="xx"))
+    a, _ = ref.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, "xx"))
+    b, _ = alt.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, "xx"))
+    assert rel(a, Sco) < TOL and rel(b, Sco) < TOL
+    ref.close()
+    alt.close()

@@ -26,7 +26,8 @@ EXPORTS = ["rpa_create", "rpa_destroy", "rpa_last_error", "rpa_set_gvectors", "r
            "rpa_load_basis", "rpa_kmap", "rpa_set_q", "rpa_chi0", "rpa_kk", "rpa_dyson", "rpa_gfast",
            "rpa_init_igk", "rpa_kk_matrix", "rpa_stage_times", "rpa_chi0_stats", "rpa_dyson_noalloc", "rpa_selftest", "rpa_launch_count", "rpa_get_stream", "rpa_synchronize",
            "rpa_basis_info", "rpa_create_shared", "rpa_server_create", "rpa_server_submit", "rpa_server_wait",
-           "rpa_server_last_error", "rpa_server_destroy", "rpa_pi", "rpa_kk_w"]
+           "rpa_server_last_error", "rpa_server_destroy", "rpa_pi", "rpa_kk_w", "rpa_gen_fbz",
+           "rpa_find_k_ibz", "rpa_find_kq"]
 
 
 class RpaOpts(C.Structure):
@@ -96,6 +97,9 @@ def load_library(path: str = LIB_PATH):
     L.rpa_basis_info.argtypes = [vp, vp]
     L.rpa_pi.argtypes = [vp, dp, dp, vp, vp, vp]
     L.rpa_kk_w.argtypes = [vp, vp, vp, vp]
+    L.rpa_gen_fbz.argtypes = [vp, ip, vp, dp, ip, vp, vp]
+    L.rpa_find_k_ibz.argtypes = [vp, ip, vp, ip, vp, dp, vp, vp]
+    L.rpa_find_kq.argtypes = [vp, ip, vp, ip, vp, vp, dp, vp, vp, vp]
     L.rpa_create_shared.argtypes = [C.POINTER(vp), vp, ip]
     L.rpa_server_create.argtypes = [C.POINTER(vp), vp, ip, dp]
     L.rpa_server_submit.argtypes = [vp, C.POINTER(RpaRequest), C.POINTER(C.c_longlong)]
@@ -199,6 +203,35 @@ class Context:
         R = np.asfortranarray(R, dtype=np.float64)
         RI = np.asfortranarray(RI, dtype=np.float64)
         self._chk(self.L.rpa_set_symmetry(self.h, nsym, _p(R), _p(RI)))
+
+    # -- k-point bookkeeping (genFBZ, findKinIBZ, findKQinBZ) on the device -----
+    def gen_fbz(self, kI, eps: float = 1e-4, max_ntot: int | None = None) -> np.ndarray:
+        """FBZ points R_i kI_j (i outer) without eps-duplicates: (ntot, 3)."""
+        kI = np.ascontiguousarray(kI, dtype=np.float64)
+        cap = max_ntot or 48 * kI.shape[0]
+        out = np.zeros((cap, 3))
+        n = C.c_int()
+        self._chk(self.L.rpa_gen_fbz(self.h, kI.shape[0], _p(kI), eps, cap, C.byref(n), _p(out)))
+        return out[:n.value].copy()
+
+    def find_k_ibz(self, ktot, kI, eps: float = 1e-4):
+        """(R1, K1), 1-based, for every FBZ point."""
+        ktot = np.ascontiguousarray(ktot, dtype=np.float64)
+        kI = np.ascontiguousarray(kI, dtype=np.float64)
+        R1 = np.zeros(ktot.shape[0], dtype=np.int32)
+        K1 = np.zeros_like(R1)
+        self._chk(self.L.rpa_find_k_ibz(self.h, ktot.shape[0], _p(ktot), kI.shape[0], _p(kI), eps, _p(R1), _p(K1)))
+        return R1, K1
+
+    def find_kq(self, ktot, kI, q, eps: float = 1e-4):
+        """(iG0, R2, K2), 1-based, for every FBZ point k and k + q."""
+        ktot = np.ascontiguousarray(ktot, dtype=np.float64)
+        kI = np.ascontiguousarray(kI, dtype=np.float64)
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        n = ktot.shape[0]
+        iG0, R2, K2 = (np.zeros(n, dtype=np.int32) for _ in range(3))
+        self._chk(self.L.rpa_find_kq(self.h, n, _p(ktot), kI.shape[0], _p(kI), _p(q), eps, _p(iG0), _p(R2), _p(K2)))
+        return iG0, R2, K2
 
     def load_basis(self, npw, igk, coeff, E):
         """npw (nks,), igk (nks,npwx) 1-based or None, coeff (nks,nbnd,npwx) complex, E (nbnd,nks) Ha."""

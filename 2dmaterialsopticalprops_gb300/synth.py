@@ -397,6 +397,54 @@ def local_fields(s: System, q: np.ndarray, gcut2: float, lf: str = "xyz", nmax: 
     return ilf, parG
 
 
+# Point group and irreducible wedge ------------------------------------------
+def hex_symmetry():
+    """C6v of the hexagonal cell of hex_cell in Cartesian coordinates: the six
+    rotations about z, then the six rotation x mirror(y -> -y) products; the
+    identity first.  Returns (nsym, R, RI) as (48, 3, 3) arrays (Fortran
+    R(48,3,3) layout when passed with order='F')."""
+    h = math.sqrt(3.0) / 2.0
+    cs = [(1.0, 0.0), (0.5, h), (-0.5, h), (-1.0, 0.0), (-0.5, -h), (0.5, -h)]
+    ops = []
+    for c, s in cs:
+        ops.append(np.array([[c, -s, 0.0], [s, c, 0.0], [0.0, 0.0, 1.0]]))
+    for c, s in cs:
+        ops.append(np.array([[c, s, 0.0], [s, -c, 0.0], [0.0, 0.0, 1.0]]))
+    R = np.zeros((48, 3, 3))
+    RI = np.zeros((48, 3, 3))
+    for i, r in enumerate(ops):
+        R[i] = r
+        RI[i] = r.T  # orthogonal
+    return len(ops), R, RI
+
+
+def mp_ibz(KC: np.ndarray, nk: int, R: np.ndarray, nsym: int, tol: float = 1e-6) -> np.ndarray:
+    """IBZ of the Gamma-centred nk x nk grid: each grid point folded into the
+    Wigner-Seitz cell, kept unless a symmetry image of it (modulo G) is already
+    kept.  (n, 3) Cartesian, 2pi/a0 units."""
+    b = KC.T
+    Binv = np.linalg.inv(KC)
+    shifts = [i * b[0] + j * b[1] for i in (-1, 0, 1) for j in (-1, 0, 1)]
+    kept = []
+    for i in range(nk):
+        for j in range(nk):
+            k = (i * b[0] + j * b[1]) / nk
+            k = min((k - s for s in shifts), key=lambda v: (round(float(v @ v), 9), tuple(np.round(v, 9))))
+            seen = False
+            for r in R[:nsym]:
+                rk = r @ k
+                for kk in kept:
+                    d = Binv @ (rk - kk)
+                    if np.all(np.abs(d - np.round(d)) < tol):
+                        seen = True
+                        break
+                if seen:
+                    break
+            if not seen:
+                kept.append(k)
+    return np.array(kept)
+
+
 # Named workloads -------------------------------------------------------------
 def config_small(**kw) -> SynthConfig:
     """A few-second oracle case with the C1 shapes scaled down."""

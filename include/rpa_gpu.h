@@ -118,6 +118,30 @@ int rpa_load_basis(rpa_ctx* ctx, int nks, int nbnd, int npwx, const int* npw, co
 int rpa_kmap(rpa_ctx* ctx, int ntot, const double* ktot, const int* K1, const int* R1,
              const int* K2, const int* R2, const int* iG0);
 
+/* ---- k-point bookkeeping on the device --------------------------------------
+ * The drivers' O(Ntot^2) / O(NG Ntot Nsym NkI) host searches, with identical
+ * results (first-match order and eps tests of the reference loops).  They use
+ * the symmetry of rpa_set_symmetry (identity when never called) and, for
+ * rpa_find_kq, the G list of rpa_set_gvectors.  k-points are Cartesian, 2pi/a0
+ * units; kI(3,nki), ktot(3,ntot) column-major; index outputs are 1-based, as
+ * rpa_kmap takes them.
+ *
+ * Replaces: genFBZ (Chi_RPA/Optabs.f90:886-933; Sloss keeps its own copy).
+ * Writes the *ntot distinct points R_i kI_j (i outer) into ktot; RPA_EINVAL when
+ * more than max_ntot. */
+int rpa_gen_fbz(rpa_ctx* ctx, int nki, const double* kI, double eps, int max_ntot, int* ntot, double* ktot);
+
+/* Replaces: findKinIBZ (Chi_RPA/Optabs.f90:776-818) for every FBZ point.
+ * RPA_ENOTFOUND ("Can not find wave vector K= in I.B.Z.") when a point has no
+ * image. */
+int rpa_find_k_ibz(rpa_ctx* ctx, int ntot, const double* ktot, int nki, const double* kI, double eps, int* R1,
+                   int* K1);
+
+/* Replaces: findKQinBZ (Chi_RPA/Optabs.f90:820-884) for every FBZ point k and
+ * k + q.  RPA_ENOTFOUND when a K+Q has no (G, FBZ point, IBZ image) match. */
+int rpa_find_kq(rpa_ctx* ctx, int ntot, const double* ktot, int nki, const double* kI, const double* q, double eps,
+                int* iG0, int* R2, int* K2);
+
 /* Replaces: findMinQ + genGlf/genGlfandParity results (Optabs.f90:272,248;
  * Sloss.f90:295,258).
  *   q    : q(3), 2pi/a0 units (before the Gcar conversion)

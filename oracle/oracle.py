@@ -349,3 +349,90 @@ def kk_w(WT: np.ndarray, S0_chi: np.ndarray, V11: float, domega: float):
         KKS += fact * (WindKK - Wind) ** 2
         SKK += fact * Wind * Wind
     return Gp, Gm, np.array([KKS, SKK, 100.0 * abs(KKS / SKK), G0.real, (WT[0, 0, 0] - V11).real / 2.0])
+
+
+# ---------------------------------------------------------------------------
+# k-point bookkeeping of the drivers, loop for loop (pure Python; small grids).
+# R, RI: Fortran R(48,3,3) as numpy (48, 3, 3) [i, n, m]; k-points (n, 3).
+
+def gen_fbz(kI: np.ndarray, R: np.ndarray, nsym: int, eps: float) -> np.ndarray:
+    """genFBZ (Chi_RPA/Optabs.f90:886-933): k(:,jk) = R_i kI_ik for i outer, kept
+    when no earlier generated point lies within eps in all components."""
+    gen = []
+    ktot = []
+    for i in range(nsym):
+        for ik in range(kI.shape[0]):
+            k = [0.0, 0.0, 0.0]
+            for n in range(3):
+                s = 0.0
+                for m in range(3):
+                    s = s + float(R[i, n, m]) * float(kI[ik, m])
+                k[n] = s
+            dup = False
+            for lk in gen:
+                if abs(k[0] - lk[0]) <= eps and abs(k[1] - lk[1]) <= eps and abs(k[2] - lk[2]) <= eps:
+                    dup = True
+            gen.append(k)
+            if not dup:
+                ktot.append(k)
+    return np.array(ktot, dtype=np.float64)
+
+
+def _rot(RI, i, k):
+    r = RI[i]
+    return [float(r[n, 0]) * k[0] + float(r[n, 1]) * k[1] + float(r[n, 2]) * k[2] for n in range(3)]
+
+
+def _first_ibz(K, kI, eps):
+    for j in range(kI.shape[0]):
+        if abs(K[0] - kI[j, 0]) <= eps and abs(K[1] - kI[j, 1]) <= eps and abs(K[2] - kI[j, 2]) <= eps:
+            return j
+    return -1
+
+
+def find_k_ibz(ktot: np.ndarray, kI: np.ndarray, RI: np.ndarray, nsym: int, eps: float):
+    """findKinIBZ (Chi_RPA/Optabs.f90:776-818) for every FBZ point: (R1, K1)
+    1-based; 0 where the reference stops ('Can not find wave vector K')."""
+    nki = kI.shape[0]
+    R1 = np.zeros(ktot.shape[0], dtype=np.int32)
+    K1 = np.zeros_like(R1)
+    for ik in range(ktot.shape[0]):
+        if ik < nki:
+            R1[ik], K1[ik] = 1, ik + 1
+            continue
+        k = [float(x) for x in ktot[ik]]
+        for i in range(1, nsym):
+            j = _first_ibz(_rot(RI, i, k), kI, eps)
+            if j >= 0:
+                R1[ik], K1[ik] = i + 1, j + 1
+                break
+    return R1, K1
+
+
+def find_kq(ktot: np.ndarray, kI: np.ndarray, RI: np.ndarray, nsym: int, G: np.ndarray, q, eps: float):
+    """findKQinBZ (Chi_RPA/Optabs.f90:820-884) for every FBZ point k and k + q:
+    (iG0, R2, K2) 1-based; 0 where the reference stops.  The G loop is outer
+    and the FBZ loop inner, as in the reference (first match wins)."""
+    n = ktot.shape[0]
+    out = np.zeros((3, n), dtype=np.int32)
+    for ik in range(n):
+        KQ = [float(ktot[ik, d]) + float(q[d]) for d in range(3)]
+        done = False
+        for iG in range(G.shape[0]):
+            g = G[iG]
+            for jk in range(n):
+                kt = ktot[jk]
+                if (abs(KQ[0] - g[0] - kt[0]) <= eps and abs(KQ[1] - g[1] - kt[1]) <= eps
+                        and abs(KQ[2] - g[2] - kt[2]) <= eps):
+                    k = [float(x) for x in kt]
+                    for i in range(nsym):
+                        j = _first_ibz(_rot(RI, i, k), kI, eps)
+                        if j >= 0:
+                            out[:, ik] = (iG + 1, i + 1, j + 1)
+                            done = True
+                            break
+                    if done:
+                        break
+            if done:
+                break
+    return out[0], out[1], out[2]

@@ -51,3 +51,61 @@ def test_kk_of_w_and_self_check(synth, rpa, orc):
     assert abs(chk[3] - chko[3]) <= TOL_W * max(abs(chko[3]), 1e-300)
     assert abs(chk[4] - chko[4]) <= TOL_W * max(abs(chko[4]), 1e-300)
     ctx.close()
+
+
+def _hex(synth, nk):
+    a0, c0, V, KC = synth.hex_cell(2.46, 20.0)
+    nsym, R, RI = synth.hex_symmetry()
+    kI = synth.mp_ibz(KC, nk, R, nsym)
+    miller, G = synth.g_list(KC, 3.5 ** 2)
+    return KC, nsym, R, RI, kI, miller, G
+
+
+@pytest.mark.parametrize("nk", [6, 12])
+def test_kmap_on_the_device_equals_the_restated_search(synth, rpa, orc, nk):
+    """rpa_gen_fbz / rpa_find_k_ibz / rpa_find_kq against the oracle's
+    loop-for-loop genFBZ / findKinIBZ / findKQinBZ: identical points and
+    indices (C6v, hexagonal grid, q along Gamma-M, Gamma-K and off-axis)."""
+    KC, nsym, R, RI, kI, miller, G = _hex(synth, nk)
+    ctx = rpa.Context()
+    ctx.set_gvectors(miller, G, KC)
+    ctx.set_symmetry(nsym, R, RI)
+    ktot = ctx.gen_fbz(kI, 1e-4)
+    kto = orc.gen_fbz(kI, R, nsym, 1e-4)
+    assert ktot.shape == kto.shape and (ktot == kto).all()
+    R1, K1 = ctx.find_k_ibz(ktot, kI, 1e-4)
+    R1o, K1o = orc.find_k_ibz(kto, kI, RI, nsym, 1e-4)
+    assert (R1 == R1o).all() and (K1 == K1o).all()
+    b = KC.T
+    for q in (b[0] / nk, (b[0] + b[1]) / nk, (2 * b[0] + b[1]) / nk):
+        got = ctx.find_kq(ktot, kI, q, 1e-4)
+        ref = orc.find_kq(kto, kI, RI, nsym, G, q, 1e-4)
+        for a, r in zip(got, ref):
+            assert (a == r).all()
+    ctx.close()
+
+
+def test_kmap_on_the_device_reproduces_the_grid_bookkeeping(synth, rpa):
+    s = synth.build(synth.config_small(nk=6, q_steps=1))
+    ctx = rpa.Context()
+    ctx.set_gvectors(s.miller, s.G, s.KC)
+    assert (ctx.gen_fbz(s.ktot) == s.ktot).all()
+    for steps, steps2 in ((1, 0), (2, 1), (5, 3)):
+        km = synth.q_kmap(s, steps, steps2)
+        iG0, R2, K2 = ctx.find_kq(s.ktot, s.ktot, km["q"])
+        assert (K2 == km["K2"]).all() and (iG0 == km["iG0"]).all() and (R2 == 1).all()
+    ctx.close()
+
+
+def test_kmap_off_grid_q_is_not_found(synth, rpa):
+    """A q that is not a grid vector: the reference stops ('Can not find wave
+    vector K+Q'); the device search returns RPA_ENOTFOUND."""
+    KC, nsym, R, RI, kI, miller, G = _hex(synth, 6)
+    ctx = rpa.Context()
+    ctx.set_gvectors(miller, G, KC)
+    ctx.set_symmetry(nsym, R, RI)
+    ktot = ctx.gen_fbz(kI)
+    with pytest.raises(rpa.RpaError) as e:
+        ctx.find_kq(ktot, kI, 0.37 * KC.T[0] / 6)
+    assert e.value.code == rpa.RPA_ENOTFOUND
+    ctx.close()

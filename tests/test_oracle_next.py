@@ -53,3 +53,42 @@ def test_pi_assembly_matches_the_closed_form(orc):
         np.testing.assert_allclose(sig[0, 1:], c0 * inter.imag[1:] / oi[1:], rtol=1e-12)
         np.testing.assert_allclose(sig[1, 1:], c0 * intra[0, 0].imag[1:] / oi[1:], rtol=1e-12)
         assert sig[0, 0] == 0 and sig[1, 0] == 0
+
+
+def _hex(synth, nk):
+    a0, c0, V, KC = synth.hex_cell(2.46, 20.0)
+    nsym, R, RI = synth.hex_symmetry()
+    kI = synth.mp_ibz(KC, nk, R, nsym)
+    miller, G = synth.g_list(KC, 3.5 ** 2)
+    return KC, nsym, R, RI, kI, miller, G
+
+
+def test_kmap_oracle_on_a_symmetric_grid(synth, orc):
+    """genFBZ / findKinIBZ / findKQinBZ restatements on a hexagonal 9x9 grid
+    with C6v: the FBZ covers the grid (points on the Wigner-Seitz boundary
+    appear once per distinct image), every point and every K+Q is found."""
+    KC, nsym, R, RI, kI, miller, G = _hex(synth, 9)
+    ktot = orc.gen_fbz(kI, R, nsym, 1e-4)
+    assert ktot.shape[0] >= 81 and np.allclose(ktot[:kI.shape[0]], kI)
+    d = np.abs(ktot[:, None, :] - ktot[None, :, :]).max(axis=2)
+    assert (d[np.triu_indices(ktot.shape[0], 1)] > 1e-4).all()
+    R1, K1 = orc.find_k_ibz(ktot, kI, RI, nsym, 1e-4)
+    assert (R1 > 0).all() and (K1 > 0).all()
+    for ik in range(ktot.shape[0]):
+        assert np.allclose(RI[R1[ik] - 1] @ ktot[ik], kI[K1[ik] - 1], atol=1e-4)
+    q = KC.T[0] / 9
+    iG0, R2, K2 = orc.find_kq(ktot, kI, RI, nsym, G, q, 1e-4)
+    assert (iG0 > 0).all()
+    for ik in range(ktot.shape[0]):
+        # K+Q - G is an FBZ point whose image under RI_R2 is the IBZ point K2
+        assert np.allclose(RI[R2[ik] - 1] @ (ktot[ik] + q - G[iG0[ik] - 1]), kI[K2[ik] - 1], atol=1e-4)
+
+
+def test_kmap_oracle_reproduces_the_grid_bookkeeping(synth, orc):
+    """Identity symmetry on the Gamma-centred grid of the synthetic systems:
+    the restated search gives the K2 / iG0 that synth.q_kmap constructs."""
+    s = synth.build(synth.config_small(nk=6, q_steps=1))
+    for steps, steps2 in ((1, 0), (2, 1), (5, 3)):
+        km = synth.q_kmap(s, steps, steps2)
+        iG0, R2, K2 = orc.find_kq(s.ktot, s.ktot, s.RI, 1, s.G, km["q"], 1e-4)
+        assert (K2 == km["K2"]).all() and (iG0 == km["iG0"]).all() and (R2 == 1).all()

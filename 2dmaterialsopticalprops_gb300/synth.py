@@ -418,30 +418,27 @@ def hex_symmetry():
     return len(ops), R, RI
 
 
-def mp_ibz(KC: np.ndarray, nk: int, R: np.ndarray, nsym: int, tol: float = 1e-6) -> np.ndarray:
-    """IBZ of the Gamma-centred nk x nk grid: each grid point folded into the
-    Wigner-Seitz cell, kept unless a symmetry image of it (modulo G) is already
-    kept.  (n, 3) Cartesian, 2pi/a0 units."""
+def mp_ibz(KC: np.ndarray, nk: int, R: np.ndarray, nsym: int) -> np.ndarray:
+    """IBZ of the Gamma-centred nk x nk grid: grid points in order (i outer),
+    each kept unless a symmetry image of it is, modulo the reciprocal lattice,
+    an already kept point; kept points are folded into the Wigner-Seitz cell.
+    (n, 3) Cartesian, 2pi/a0 units.  The operations act on the grid indices as
+    integer matrices (crystal coordinates)."""
     b = KC.T
-    Binv = np.linalg.inv(KC)
+    Kinv = np.linalg.inv(KC)
+    Rc = [np.rint(Kinv @ R[s] @ KC).astype(np.int64) for s in range(nsym)]
+    seen = np.zeros((nk, nk), dtype=bool)
     shifts = [i * b[0] + j * b[1] for i in (-1, 0, 1) for j in (-1, 0, 1)]
     kept = []
     for i in range(nk):
         for j in range(nk):
+            if seen[i, j]:
+                continue
+            for r in Rc:
+                a, c = (r[0, 0] * i + r[0, 1] * j) % nk, (r[1, 0] * i + r[1, 1] * j) % nk
+                seen[a, c] = True
             k = (i * b[0] + j * b[1]) / nk
-            k = min((k - s for s in shifts), key=lambda v: (round(float(v @ v), 9), tuple(np.round(v, 9))))
-            seen = False
-            for r in R[:nsym]:
-                rk = r @ k
-                for kk in kept:
-                    d = Binv @ (rk - kk)
-                    if np.all(np.abs(d - np.round(d)) < tol):
-                        seen = True
-                        break
-                if seen:
-                    break
-            if not seen:
-                kept.append(k)
+            kept.append(min((k - s for s in shifts), key=lambda v: (round(float(v @ v), 9), tuple(np.round(v, 9)))))
     return np.array(kept)
 
 

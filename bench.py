@@ -367,6 +367,49 @@ def c5_config(nk: int):
                                        omax_ev=50.0, eta_ev=0.05)
 
 
+def kmap_run(nk: int = 120, oracle_sample: int = 24):
+    """The drivers' k-point bookkeeping for one q on a 120x120 hexagonal grid
+    with the C6v point group (12 operations; 1261 IBZ points): genFBZ,
+    findKinIBZ and findKQinBZ on the device (host-to-host wall time, 5 repeats,
+    best), and the oracle's loop-for-loop restatement (pure Python) on a
+    sample of FBZ points, scaled to the grid."""
+    rpa, synth = pkg("rpa"), pkg("synth")
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    a0, c0, V, KC = synth.hex_cell(2.46, 20.0)
+    nsym, R, RI = synth.hex_symmetry()
+    kI = synth.mp_ibz(KC, nk, R, nsym)
+    miller, G = synth.g_list(KC, 3.5 ** 2)
+    q = KC.T[0] / nk
+    ctx = rpa.Context()
+    ctx.set_gvectors(miller, G, KC)
+    ctx.set_symmetry(nsym, R, RI)
+    best = None
+    for _ in range(5):
+        t0 = time.perf_counter()
+        ktot = ctx.gen_fbz(kI)
+        t1 = time.perf_counter()
+        ctx.find_k_ibz(ktot, kI)
+        t2 = time.perf_counter()
+        ctx.find_kq(ktot, kI, q)
+        t3 = time.perf_counter()
+        tt = (1e3 * (t1 - t0), 1e3 * (t2 - t1), 1e3 * (t3 - t2))
+        best = tt if best is None or sum(tt) < sum(best) else best
+    ctx.close()
+    # CPU baseline: the oracle's findKQinBZ on a sample of FBZ points
+    rng = np.random.default_rng(5)
+    idx = np.sort(rng.choice(ktot.shape[0], size=oracle_sample, replace=False))
+    t0 = time.perf_counter()
+    orc.find_kq(ktot, kI, RI, nsym, G, q, 1e-4, points=idx)
+    t_kq = (time.perf_counter() - t0) / oracle_sample * ktot.shape[0]
+    return {"workload": f"{nk}x{nk} hexagonal grid, C6v (12 operations), {kI.shape[0]} IBZ points, "
+                        f"{ktot.shape[0]} FBZ points, {G.shape[0]} G vectors, q one grid step along Gamma-M",
+            "device_ms": {"gen_fbz": round(best[0], 2), "find_k_ibz": round(best[1], 2), "find_kq": round(best[2], 2)},
+            "cpu_baseline": {"find_kq_s": round(t_kq, 1), "kind": "port", "cores": 1,
+                             "sample": f"findKQinBZ restated loop for loop (pure Python) for {oracle_sample} of "
+                                       f"{ktot.shape[0]} FBZ points, scaled by the point count"}}
+
+
 def c5_run(n_q: int = 16, nk_full: int = 96, nk_check: int = 24, q_check=(1, 8)):
     """W(q, w) for 16 q-points at full size on the mixed path (timed), and the
     mixed-vs-FP64 comparison (time ratio, per-q max / RMS error of Im W) on
@@ -440,6 +483,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop (serving) measurement")
     ap.add_argument("--c5", action="store_true",
                     help="also run the large-W workload (96x96, 80 bands, 4000 coefficients, NGloc 301; adds minutes)")
+    ap.add_argument("--kmap", action="store_true",
+                    help="also time the k-point bookkeeping (genFBZ / findKinIBZ / findKQinBZ) on a 120x120 C6v grid")
     ap.add_argument("--dispersion", action="store_true",
                     help="also run the 64-q loss-function dispersion on the resident basis (adds ~2 min)")
     args = ap.parse_args()
@@ -622,6 +667,7 @@ def main():
         serving = serving_run()
     if rank == 0 and args.dispersion and args.precision == "mixed":
         disp = dispersion_run(ctx, s)
+    kmap = kmap_run() if rank == 0 and args.kmap else None
     c5 = None
     if rank == 0 and args.c5 and args.precision == "mixed":
         if ctx is not None:
@@ -640,7 +686,7 @@ def main():
                 "data": "synthetic (seeded QE-layout Bloch basis)", "config": cfgd, "clocks": clocks,
                 "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "stage_ms_per_step": {k: round(v, 3) for k, v in sm.items()},
-                "fp64_gpu": fp64, "serving": serving, "dispersion": disp, "c5": c5,
+                "fp64_gpu": fp64, "serving": serving, "dispersion": disp, "c5": c5, "kmap": kmap,
                 "vertex_tflops": (work["vertex_flops"] / (sm["vertices"] / 1e3) / 1e12) if sm["vertices"] else None}
         print(json.dumps(line), flush=True)
     if ctx is not None:

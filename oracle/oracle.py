@@ -409,13 +409,15 @@ def find_k_ibz(ktot: np.ndarray, kI: np.ndarray, RI: np.ndarray, nsym: int, eps:
     return R1, K1
 
 
-def find_kq(ktot: np.ndarray, kI: np.ndarray, RI: np.ndarray, nsym: int, G: np.ndarray, q, eps: float):
-    """findKQinBZ (Chi_RPA/Optabs.f90:820-884) for every FBZ point k and k + q:
-    (iG0, R2, K2) 1-based; 0 where the reference stops.  The G loop is outer
-    and the FBZ loop inner, as in the reference (first match wins)."""
+def find_kq(ktot: np.ndarray, kI: np.ndarray, RI: np.ndarray, nsym: int, G: np.ndarray, q, eps: float,
+            points=None):
+    """findKQinBZ (Chi_RPA/Optabs.f90:820-884) for every FBZ point k and k + q
+    (or for the FBZ indices in ``points``): (iG0, R2, K2) 1-based; 0 where the
+    reference stops.  The G loop is outer and the FBZ loop inner, as in the
+    reference (first match wins)."""
     n = ktot.shape[0]
     out = np.zeros((3, n), dtype=np.int32)
-    for ik in range(n):
+    for ik in (range(n) if points is None else points):
         KQ = [float(ktot[ik, d]) + float(q[d]) for d in range(3)]
         done = False
         for iG in range(G.shape[0]):

@@ -27,7 +27,8 @@ EXPORTS = ["rpa_create", "rpa_destroy", "rpa_last_error", "rpa_set_gvectors", "r
            "rpa_init_igk", "rpa_kk_matrix", "rpa_stage_times", "rpa_chi0_stats", "rpa_dyson_noalloc", "rpa_selftest", "rpa_launch_count", "rpa_get_stream", "rpa_synchronize",
            "rpa_basis_info", "rpa_create_shared", "rpa_server_create", "rpa_server_submit", "rpa_server_wait",
            "rpa_server_last_error", "rpa_server_destroy", "rpa_pi", "rpa_kk_w", "rpa_gen_fbz",
-           "rpa_find_k_ibz", "rpa_find_kq"]
+           "rpa_find_k_ibz", "rpa_find_kq", "rpa_qe_read_gvectors", "rpa_qe_wfc_info", "rpa_qe_read_wfc",
+           "rpa_write_corrfun", "rpa_read_corrfun", "rpa_write_wt"]
 
 
 class RpaOpts(C.Structure):
@@ -100,6 +101,13 @@ def load_library(path: str = LIB_PATH):
     L.rpa_gen_fbz.argtypes = [vp, ip, vp, dp, ip, vp, vp]
     L.rpa_find_k_ibz.argtypes = [vp, ip, vp, ip, vp, dp, vp, vp]
     L.rpa_find_kq.argtypes = [vp, ip, vp, ip, vp, vp, dp, vp, vp, vp]
+    cp = C.c_char_p
+    L.rpa_qe_read_gvectors.argtypes = [cp, vp, ip, vp, vp, vp, vp]
+    L.rpa_qe_wfc_info.argtypes = [cp, ip, vp, vp, vp, vp]
+    L.rpa_qe_read_wfc.argtypes = [cp, ip, ip, ip, vp, vp]
+    L.rpa_write_corrfun.argtypes = [cp, cp, ip, ip, dp, vp, vp]
+    L.rpa_read_corrfun.argtypes = [cp, cp, ip, ip, vp, vp]
+    L.rpa_write_wt.argtypes = [cp, ip, ip, dp, vp]
     L.rpa_create_shared.argtypes = [C.POINTER(vp), vp, ip]
     L.rpa_server_create.argtypes = [C.POINTER(vp), vp, ip, dp]
     L.rpa_server_submit.argtypes = [vp, C.POINTER(RpaRequest), C.POINTER(C.c_longlong)]
@@ -155,6 +163,68 @@ def selftest(which: int) -> float:
     if rc != RPA_OK:
         raise RpaError(rc, "rpa_selftest failed")
     return r.value
+
+
+# -- on-disk formats (host only) ------------------------------------------------
+def _io_chk(L, rc):
+    if rc != RPA_OK:
+        raise RpaError(rc, L.rpa_last_error(None).decode())
+
+
+def qe_read_gvectors(savedir: str, KC, max_ng: int = 1 << 22):
+    """charge-density.dat of a QE 6 save directory: (miller (ng,3), G (ng,3), parG (ng,))."""
+    L = load_library()
+    KC = np.asfortranarray(KC, dtype=np.float64)
+    mil = np.zeros((max_ng, 3), dtype=np.int32)
+    G = np.zeros((max_ng, 3))
+    par = np.zeros(max_ng, dtype=np.int32)
+    ng = C.c_int()
+    _io_chk(L, L.rpa_qe_read_gvectors(savedir.encode(), _p(KC), max_ng, C.byref(ng), _p(mil), _p(G), _p(par)))
+    n = ng.value
+    return mil[:n].copy(), G[:n].copy(), par[:n].copy()
+
+
+def qe_read_wfc(savedir: str, ik: int, npwx: int | None = None, nbnd: int | None = None):
+    """wfc<ik>.dat (1-based ik): (coeff (nbnd, npwx) complex, miller (igwx, 3), xk (3,))."""
+    L = load_library()
+    igwx, npol, nb = C.c_int(), C.c_int(), C.c_int()
+    xk = np.zeros(3)
+    _io_chk(L, L.rpa_qe_wfc_info(savedir.encode(), ik, C.byref(igwx), C.byref(npol), C.byref(nb), _p(xk)))
+    npwx = npwx or igwx.value
+    nbnd = nbnd or nb.value
+    coeff = np.zeros((nbnd, npwx), dtype=np.complex128)
+    mil = np.zeros((igwx.value, 3), dtype=np.int32)
+    _io_chk(L, L.rpa_qe_read_wfc(savedir.encode(), ik, npwx, nbnd, _p(coeff), _p(mil)))
+    return coeff, mil, xk
+
+
+def write_corrfun(path_s0: str, path_qeff: str | None, S0, Qeff, domega: float):
+    """S0 and Qeff as Context.chi0 returns them for MODE_CURRENT (their memory is
+    Fortran S0(-no:no,nlf,nlf) and Qeff(nlf,nlf))."""
+    L = load_library()
+    S0 = np.ascontiguousarray(S0, dtype=np.complex128)
+    nlf, no = S0.shape[0], (S0.shape[2] - 1) // 2
+    Qeff = None if Qeff is None else np.ascontiguousarray(Qeff, dtype=np.complex128)
+    _io_chk(L, L.rpa_write_corrfun(path_s0.encode(), None if path_qeff is None else path_qeff.encode(), no, nlf,
+                                   domega, _p(S0), _p(Qeff)))
+
+
+def read_corrfun(path_s0: str, path_qeff: str | None, no: int, nlf: int):
+    """The files of write_corrfun (or of the reference's calc = 1): (S0, Qeff)
+    in Context.chi0's layout; Qeff None without path_qeff."""
+    L = load_library()
+    S0 = np.zeros((nlf, nlf, 2 * no + 1), dtype=np.complex128)
+    Qeff = np.zeros((nlf, nlf), dtype=np.complex128) if path_qeff else None
+    _io_chk(L, L.rpa_read_corrfun(path_s0.encode(), None if path_qeff is None else path_qeff.encode(), no, nlf,
+                                  _p(S0), _p(Qeff)))
+    return S0, Qeff
+
+
+def write_wt(path: str, WT, domega: float):
+    """WT as Context.dyson returns it (memory = Fortran WT(nw,nlf,nlf))."""
+    L = load_library()
+    WT = np.ascontiguousarray(WT, dtype=np.complex128)
+    _io_chk(L, L.rpa_write_wt(path.encode(), WT.shape[2], WT.shape[0], domega, _p(WT)))
 
 
 class Context:

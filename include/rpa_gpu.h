@@ -142,6 +142,38 @@ int rpa_find_k_ibz(rpa_ctx* ctx, int ntot, const double* ktot, int nki, const do
 int rpa_find_kq(rpa_ctx* ctx, int ntot, const double* ktot, int nki, const double* kI, const double* q, double eps,
                 int* iG0, int* R2, int* K2);
 
+/* ---- On-disk formats (host only, no context; errors via rpa_last_error(NULL)) --
+ *
+ * Replaces: loadG (Modules/io_qe.f90:11-71).  Reads the Miller indices of
+ * <savedir>/charge-density.dat (QE 6 binary), G(:,iG) = KC mill(:,iG)
+ * (KC(3,3) column-major, 2pi/a0 units) and parG(iG) = mill(3,iG) (parG may be
+ * NULL).  miller(3,max_ng), G(3,max_ng) column-major. */
+int rpa_qe_read_gvectors(const char* savedir, const double* KC, int max_ng, int* ng, int* miller, double* G,
+                         int* parG);
+
+/* Header of <savedir>/wfc<ik>.dat: igwx, npol, nbnd and xk(3) (xk may be NULL). */
+int rpa_qe_wfc_info(const char* savedir, int ik, int* igwx, int* npol, int* nbnd, double* xk);
+
+/* Replaces: loadCs_full (Modules/io_qe.f90:124-166).  The first nbnd bands of
+ * <savedir>/wfc<ik>.dat into coeff(npwx, nbnd) complex(dp) column-major (zero
+ * beyond igwx), and the record of Miller indices into miller(3, igwx) (may be
+ * NULL).  npol must be 1. */
+int rpa_qe_read_wfc(const char* savedir, int ik, int npwx, int nbnd, double* coeff, int* miller);
+
+/* Replaces: the calc = 1 output of Optabs (Chi_RPA/Optabs.f90:482-508):
+ * S0(-no:no,nlf,nlf) and Qeff(nlf,nlf) complex(dp) column-major as text, one
+ * 'omega=' line per frequency and '(2F15.10)' per element (path_qeff / Qeff may
+ * be NULL). */
+int rpa_write_corrfun(const char* path_s0, const char* path_qeff, int no, int nlf, double domega, const double* S0,
+                      const double* Qeff);
+
+/* Replaces: the calc = 2 read-back (Chi_RPA/Optabs.f90:531-559) of those files. */
+int rpa_read_corrfun(const char* path_s0, const char* path_qeff, int no, int nlf, double* S0, double* Qeff);
+
+/* Replaces: writeWT_Qi (W/Sloss.f90:1572-1601).  The first frequency of
+ * WT(no_rows,nlf,nlf) complex(dp) column-major, '(10F15.5)'. */
+int rpa_write_wt(const char* path, int no_rows, int nlf, double domega, const double* WT);
+
 /* Replaces: findMinQ + genGlf/genGlfandParity results (Optabs.f90:272,248;
  * Sloss.f90:295,258).
  *   q    : q(3), 2pi/a0 units (before the Gcar conversion)

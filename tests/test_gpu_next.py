@@ -109,3 +109,27 @@ def test_kmap_off_grid_q_is_not_found(synth, rpa):
         ctx.find_kq(ktot, kI, 0.37 * KC.T[0] / 6)
     assert e.value.code == rpa.RPA_ENOTFOUND
     ctx.close()
+
+
+def test_corrfun_and_wt_files_from_the_device_path(synth, rpa, tmp_path):
+    """Optabs calc = 1 output written from the device S0 / Qeff and read back as
+    calc = 2 would (values rounded to the files' 10 decimals), and the Sloss
+    W_Qi file of the device WT."""
+    s = synth.build(synth.config_small())
+    ctx = rpa.Context()
+    ctx.load_system(s)
+    S, Q = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, "xx"))
+    p0, p1 = str(tmp_path / "Corrfun_xx"), str(tmp_path / "Qeff_xx")
+    rpa.write_corrfun(p0, p1, S, Q, s.domega)
+    Sr, Qr = rpa.read_corrfun(p0, p1, s.no, s.nlf)
+    for a, b in ((Sr, S), (Qr, Q)):
+        assert np.abs(a.real - b.real).max() <= 5.0001e-11 and np.abs(a.imag - b.imag).max() <= 5.0001e-11
+    ctx.chi0(rpa.MODE_CHARGE, want=False, **rpa.sloss_args(s))
+    ctx.kk(rpa.KK_SLOSS_REAL, want=False)
+    WT, _, _ = ctx.dyson(s.c0, s.cfg.eps)
+    rpa.write_wt(str(tmp_path / "W_Q1"), WT, s.domega)
+    vals = " ".join(open(tmp_path / "W_Q1").read().splitlines()[1:]).split()
+    got = np.array([float(v) for v in vals]).reshape(-1, 2)
+    ref = np.array([[WT[j, i, 0].real, WT[j, i, 0].imag] for i in range(s.nlf) for j in range(s.nlf)])
+    assert np.abs(got - ref).max() <= 5.0001e-6
+    ctx.close()

@@ -208,25 +208,39 @@ def cpu_sample(cfg_name: str, q_steps: int, budget_s: float):
 
 
 # ---------------------------------------------------------------------------
-def serving_run(n_req: int = 32, rate: float = 200.0, nslots: int = 4, mem_gb: float = 40.0, seed: int = 5):
-    """Request loop on a resident grid60 basis (mixed path): seeded Poisson
-    arrivals of W (loss-function) and chi0 (Optabs xx) requests with q of
-    1-15 grid steps along Gamma-M, NGloc 19-91 and nw 200-1000, served by
-    nslots shared contexts with continuous batching.  Latency = submission to
-    completion (server clock)."""
+# request mixes of the serving measurement: basis, q steps, NGloc, nw, local-field choice
+SERVE_MIXES = {
+    "grid60": dict(desc="grid60 basis resident (mixed path)", steps=(1, 16), nlf=(19, 92), no=(200, 1001), lf="z"),
+    # MoS2-like resident basis: 72x72, 40 bands (13 occupied), ~2500 coefficients;
+    # q ~ U(0.005, 0.5) 2pi/a as 1-31 grid steps along Gamma-M, NGloc 19-301, nw 200-2000
+    "c4": dict(desc="72x72 basis, 40 bands (13 occ), ~2500 coefficients resident (mixed path)", steps=(1, 32),
+               nlf=(19, 302), no=(200, 2001), lf="xyz"),
+}
+
+
+def serving_run(n_req: int = 32, rate: float = 200.0, nslots: int = 4, mem_gb: float = 40.0, seed: int = 5,
+                mix: str = "grid60"):
+    """Request loop on a resident basis (mixed path): seeded Poisson arrivals of
+    W (loss-function) and chi0 (Optabs xx) requests with the q, NGloc and nw
+    ranges of SERVE_MIXES[mix], served by nslots shared contexts with
+    continuous batching.  Latency = submission to completion (server clock)."""
     import threading
     rpa, synth = pkg("rpa"), pkg("synth")
-    s = synth.build(config_of("grid60", 1))
+    M = SERVE_MIXES[mix]
+    if mix == "c4":
+        s = synth.build(synth.config_grid120(nk=72, nbnd=40, nocc=13, npw=2500, nlf=19, no=1001, q_steps=1))
+    else:
+        s = synth.build(config_of("grid60", 1))
     parent = rpa.Context(precision=rpa.PREC_MIXED)
     parent.load_system(s)
     rng = np.random.default_rng(seed)
 
     def make(i):
-        steps = int(rng.integers(1, 16))
+        steps = int(rng.integers(*M["steps"]))
         km = synth.q_kmap(s, steps)
-        nlf = int(rng.integers(19, 92))
-        ilf, par = synth.local_fields(s, km["q"], 1e9, lf="z", nmax=nlf)
-        no = int(rng.integers(200, 1001))
+        nlf = int(rng.integers(*M["nlf"]))
+        ilf, par = synth.local_fields(s, km["q"], 1e9, lf=M["lf"], nmax=nlf)
+        no = int(rng.integers(*M["no"]))
         domega = s.domega * (s.no - 1) / (no - 1)
         if i % 2 == 0:
             args = dict(no=no, domega=domega, eta=s.eta, Vcell=s.Vcell, Gcar=s.Gcar, nocc=s.nocc)
@@ -265,9 +279,10 @@ def serving_run(n_req: int = 32, rate: float = 200.0, nslots: int = 4, mem_gb: f
     lat = np.array([r[0] for r in res])
     queue = np.array([r[1] for r in res])
     serv = np.array([r[2] for r in res])
-    return {"workload": f"grid60 basis resident (mixed path); {n_req} requests, Poisson arrivals at {rate:g}/s "
-                        f"(seed {seed}): W (loss) and chi0 (Optabs xx) alternating, q 1-15 grid steps along "
-                        f"Gamma-M, NGloc 19-91, nw 200-1000; {nslots} slots, {mem_gb:g} GB admission budget",
+    return {"workload": f"{M['desc']}; {n_req} requests, Poisson arrivals at {rate:g}/s "
+                        f"(seed {seed}): W (loss) and chi0 (Optabs xx) alternating, q {M['steps'][0]}-"
+                        f"{M['steps'][1] - 1} grid steps along Gamma-M, NGloc {M['nlf'][0]}-{M['nlf'][1] - 1}, "
+                        f"nw {M['no'][0]}-{M['no'][1] - 1}; {nslots} slots, {mem_gb:g} GB admission budget",
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
             "mean_queue_s": float(queue.mean()), "mean_service_s": float(serv.mean()),
             "throughput_req_s": n_req / (t_end - t0), "n_requests": n_req, "slots": nslots,
@@ -483,6 +498,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop (serving) measurement")
     ap.add_argument("--c5", action="store_true",
                     help="also run the large-W workload (96x96, 80 bands, 4000 coefficients, NGloc 301; adds minutes)")
+    ap.add_argument("--serve-c4", action="store_true",
+                    help="also run the request loop on the MoS2-like 72x72 / 40-band / 2500-coefficient basis")
     ap.add_argument("--kmap", action="store_true",
                     help="also time the k-point bookkeeping (genFBZ / findKinIBZ / findKQinBZ) on a 120x120 C6v grid")
     ap.add_argument("--dispersion", action="store_true",
@@ -668,6 +685,9 @@ def main():
     if rank == 0 and args.dispersion and args.precision == "mixed":
         disp = dispersion_run(ctx, s)
     kmap = kmap_run() if rank == 0 and args.kmap else None
+    serving_c4 = None
+    if rank == 0 and args.serve_c4 and args.precision == "mixed":
+        serving_c4 = serving_run(mem_gb=120.0, mix="c4")
     c5 = None
     if rank == 0 and args.c5 and args.precision == "mixed":
         if ctx is not None:
@@ -687,6 +707,7 @@ def main():
                 "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "stage_ms_per_step": {k: round(v, 3) for k, v in sm.items()},
                 "fp64_gpu": fp64, "serving": serving, "dispersion": disp, "c5": c5, "kmap": kmap,
+                "serving_c4": serving_c4,
                 "vertex_tflops": (work["vertex_flops"] / (sm["vertices"] / 1e3) / 1e12) if sm["vertices"] else None}
         print(json.dumps(line), flush=True)
     if ctx is not None:

@@ -19,14 +19,16 @@
 // of bands.  The MMA operands are MN-major: a K row of the X tile holds 128
 // (G, band) rows, 8 bands per 16-byte chunk, so each gathered (G, plane wave,
 // plane) lands with 16-byte cp.async copies and no transposition.  K order in a
-// chunk of 32 plane waves: rows 0-31 real parts, 32-63 imaginary parts.  Then
-//     Re D = X . Y                          (all 64 K rows)
-//     Im D = X[Re] . (-Y[Im]) + X[Im] . Y[Re]
-// both from the same Y tile: the Im block reads the other half of Y's K rows,
-// negated by the instruction descriptor.  The current factor separates,
-// f(G,i) = a(G) + b(i): warps 0-3 form the b(i) c block of Y (extra columns)
-// from the c block they copied, and a(G) multiplies the c block at read-back:
-// M = a(G) D[c] + D[b c].  Each local-field tile sweeps the plane waves in the
+// chunk of 32 plane waves: rows 0-31 real parts, 32-63 imaginary parts.  The Y
+// tile holds two column blocks, [y | y'] with y' = (-Im y rows 0-31, Re y rows
+// 32-63), so one MMA of N = 2 NYN per K step gives
+//     Re D = X . y  and  Im D = X . y' = X[Re] . (-Im y) + X[Im] . Re y
+// (wide MMAs: each one re-reads the 128-row X operand from shared memory, so
+// the fewer and wider the better).  The threads that copy a y chunk write its
+// y' image.  The current factor separates,
+// f(G,i) = a(G) + b(i): the b(i) c block (precomputed per launch, split like the
+// coefficient planes) is a second column block of y, and a(G) multiplies the c
+// block at read-back: M = a(G) D[c] + D[b c].  Each local-field tile sweeps the plane waves in the
 // opposite direction of the previous one, so the coefficient rows read last
 // are read again first while they are still in L2.
 // Three products per chunk, Xh Yl + Xl Yh + Xh Yh, into a fresh TMEM
@@ -54,7 +56,7 @@ struct VtxMnCtx {
   const double* Glf;
   const int* npw;
   const __half* planes;   // [kibz][npwx][4][nbp]
-  const float* btab;      // [k_local][nsum_max]: b(i) sB / 2^14 (current vertices)
+  const __half* ybt;      // [k_local][nsum_max][4][nbp]: b(i) c split like the planes (current vertices)
   const int16_t* map;     // [k_local][nlf][nsum_max]: gathered-side position of (G, i), -1 none
   const Trans* trans;
   const long long* offsets;
@@ -82,12 +84,11 @@ constexpr int VM_SMAX = 6;
 template <int NBY, bool CURRENT>
 struct VmCfg {
   static constexpr int NY = CURRENT ? 2 : 1;
-  static constexpr int NYN = NY * NBY;                   // MMA N
-  static constexpr int NYA = (NYN + 63) / 64;            // 64-wide atoms along N
+  static constexpr int NYN = NY * NBY;                   // columns of one block (y or y')
+  static constexpr int NTA = (2 * NYN + 63) / 64;        // 64-wide atoms along N of the Y tile
   static constexpr uint32_t XH = 64 * 128 * 2;           // one half (hi or lo) of X
-  static constexpr uint32_t YH = (uint32_t)NYA * 8192;   // one half of Y
-  static constexpr uint32_t B_OFF = 2 * XH + 2 * YH;       // b(i) of the chunk, one copy per forming warp
-  static constexpr uint32_t STAGE = (B_OFF + (CURRENT ? 512u : 0u) + 1023u) / 1024u * 1024u;
+  static constexpr uint32_t YH = (uint32_t)NTA * 8192;   // one half of Y
+  static constexpr uint32_t STAGE = 2 * XH + 2 * YH;
   static constexpr uint32_t PTAB = 32 * NBY * 2;         // int16 [32][NBY]
   static constexpr int S0 = (int)((VM_SMEM_MAX - 1024 - (int)PTAB) / (int)STAGE);
   static constexpr int S = S0 > VM_SMAX ? VM_SMAX : S0;
@@ -96,7 +97,7 @@ struct VmCfg {
                                                        : 4 * NYN <= 256 ? 256 : 512;
   static constexpr int CW = NBY / 4;                     // columns per thread per block
   static constexpr size_t SMEM = (size_t)S * STAGE + PTAB + 1024;
-  static_assert(NBY % 16 == 0 && NYN <= 128, "window too wide");
+  static_assert(NBY % 16 == 0 && 2 * NYN <= 256, "window too wide");
   static_assert(S >= 3, "shared-memory ring too shallow");
 };
 
@@ -145,7 +146,7 @@ __device__ __forceinline__ void tmem_ld_n(uint32_t addr, float* v) {
 template <int NBY, bool CURRENT>
 __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
   using Cfg = VmCfg<NBY, CURRENT>;
-  constexpr int S = Cfg::S, NYN = Cfg::NYN, NYA = Cfg::NYA, CW = Cfg::CW;
+  constexpr int S = Cfg::S, NYN = Cfg::NYN, NTA = Cfg::NTA, CW = Cfg::CW;
   constexpr uint32_t XH = Cfg::XH, YH = Cfg::YH, STAGE = Cfg::STAGE;
 
   extern __shared__ unsigned char smraw[];
@@ -199,10 +200,10 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
   if (warp == VM_WORKERS / 32) {
     // ---------------------------------------------------------------- MMA warp
     if (lane == 0) {
-      const uint32_t id_p = tc::idesc_f16_mn(128, NYN, false), id_n = tc::idesc_f16_mn(128, NYN, true);
+      const uint32_t idesc = tc::idesc_f16_mn(128, 2 * NYN, false);
       // descriptors of stage 0; a chunk adds its byte offsets / 16 to the start-address field
       const uint64_t dx0 = tc::desc_sw128_mn(sbase, 1024u, 2048u);
-      const uint64_t dy0 = tc::desc_sw128_mn(sbase + 2 * XH, 1024u, NYA * 1024u);
+      const uint64_t dy0 = tc::desc_sw128_mn(sbase + 2 * XH, 1024u, NTA * 1024u);
       int last = -1;
       int s = 0, ph = 0;
       for (int t = 0; t < total; ++t) {
@@ -216,18 +217,14 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
         tc::tc_fence_after();
         const uint64_t so = (uint64_t)(((uint32_t)s * STAGE) >> 4);
         const uint64_t dx = dx0 + so, dy = dy0 + so;
-        const uint32_t dre = taddr + (uint32_t)((t & 1) * Cfg::BUFC), dim = dre + NYN;
+        const uint32_t d = taddr + (uint32_t)((t & 1) * Cfg::BUFC);
 #pragma unroll
         for (int p = 0; p < 3; ++p) {  // Xh Yl, Xl Yh, Xh Yh
           const uint64_t xa = dx + (p == 1 ? XH >> 4 : 0u), yb = dy + (p == 0 ? YH >> 4 : 0u);
 #pragma unroll
-          for (int ks = 0; ks < 4; ++ks) {
-            const uint32_t acc = (p > 0 || ks > 0) ? 1u : 0u;
-            const uint64_t da = xa + (uint64_t)(ks * 256);
-            const uint32_t kb = ks < 2 ? 4 + 2 * ks : 2 * (ks - 2);
-            tc::mma_bf16(dre, da, yb + (uint64_t)(ks * 2 * NYA * 64), id_p, acc);
-            tc::mma_bf16(dim, da, yb + (uint64_t)(kb * NYA * 64), ks < 2 ? id_n : id_p, acc);
-          }
+          for (int ks = 0; ks < 4; ++ks)
+            tc::mma_bf16(d, xa + (uint64_t)(ks * 256), yb + (uint64_t)(ks * 2 * NTA * 64), idesc,
+                         (p > 0 || ks > 0) ? 1u : 0u);
         }
         tc::mma_commit(&done[t & 1]);
         last = t;
@@ -247,94 +244,45 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
     const size_t pstride = (size_t)4 * V.nbp;  // halves per plane wave
     const __half* xsrc = V.planes + (size_t)kX * V.npwx * pstride + V.xs + xb0;
     const int16_t* mp = V.map + (size_t)kl * V.nlf * V.nsum_max + xpw;
-    // Y copies (charge): e = tid + VM_WORKERS v over 2 halves x 64 K rows x NYN / 8 chunks
-    constexpr int YCH = NYN / 8, YE = CURRENT ? 0 : 128 * YCH, YV = (YE + VM_WORKERS - 1) / VM_WORKERS + (CURRENT ? 1 : 0);
+    // Y copies: e = tid + VM_WORKERS v over 2 halves x 64 K rows x NYN / 8 chunks of y
+    constexpr int YCH = NYN / 8, YE = 128 * YCH, YV = (YE + VM_WORKERS - 1) / VM_WORKERS;
     // ysrc: plane * nbp + band (bits 0-15), plane wave of the chunk (bits 16-20),
-    // zero fill (bit 22); -1: no copy
-    uint32_t ydst[YV];
+    // b(i) c block (bit 21), zero fill (bit 22), imaginary part (bit 23: negated
+    // in y'); -1: no copy
+    uint32_t ydst[YV], yidst[YV];  // the chunk in y, its image in y'
     int ysrc[YV];
 #pragma unroll
     for (int v = 0; v < YV; ++v) {
       const int e = tid + VM_WORKERS * v;
       ysrc[v] = -1;
-      ydst[v] = 0;
+      ydst[v] = yidst[v] = 0;
       if (e < YE) {
         const int line = e / YCH, j = e - line * YCH;
         const int half = line >> 6, kk = line & 63, part = kk >> 5, pw = kk & 31;
         const int col = 8 * j, u = 2 * half + part;
-        const int band = V.ys + col;
-        ydst[v] = 2 * XH + (uint32_t)half * YH + (uint32_t)(kk >> 3) * (NYA * 1024u) + (uint32_t)(col >> 6) * 1024u +
+        const bool bblk = CURRENT && col >= NBY;
+        const int band = V.ys + (bblk ? col - NBY : col);
+        ydst[v] = 2 * XH + (uint32_t)half * YH + (uint32_t)(kk >> 3) * (NTA * 1024u) + (uint32_t)(col >> 6) * 1024u +
                   (uint32_t)(kk & 7) * 128u + ((uint32_t)(((col >> 3) & 7) ^ (kk & 7)) << 4);
-        ysrc[v] = (band < V.nbp ? u * V.nbp + band : (1 << 22)) | (pw << 16);
+        const int ki = kk ^ 32, ci = NYN + col;  // y' row and column of the chunk
+        yidst[v] = 2 * XH + (uint32_t)half * YH + (uint32_t)(ki >> 3) * (NTA * 1024u) + (uint32_t)(ci >> 6) * 1024u +
+                   (uint32_t)(ki & 7) * 128u + ((uint32_t)(((ci >> 3) & 7) ^ (ki & 7)) << 4);
+        ysrc[v] = (band < V.nbp ? u * V.nbp + band : (1 << 22)) | (pw << 16) | (bblk ? (1 << 21) : 0) | (part << 23);
       }
     }
     const __half* ysrc_c = V.planes + (size_t)kY * V.npwx * pstride;
-    // current vertices: forming thread tid < 128, tasks f = tid + 128 r (r < FR) =
-    // (8-band chunk f / 32 of the c block, plane wave f % 32 = lane): copies the
-    // four planes of the c block, then writes the b(i) c block beside them
-    constexpr int FR = CURRENT ? (NBY * 4 + 127) / 128 : 1;
-    const bool former = CURRENT && tid < 128;
-    uint32_t fco[FR], fbo[FR];  // Re-hi offsets (within the stage) of the c and b c chunks; Im: + 4 NYA 1024, lo: + YH
-    int fsrc[FR];               // plane-row offset (halves) of the c chunk, -1: beyond the tasks, -2: zero fill
-#pragma unroll
-    for (int r = 0; r < FR; ++r) {
-      const int f = tid + 128 * r, j = f >> 5, pw = f & 31;
-      const int col = 8 * j, colb = NBY + col;
-      fco[r] = 2 * XH + (uint32_t)(pw >> 3) * (NYA * 1024u) + (uint32_t)(col >> 6) * 1024u + (uint32_t)(pw & 7) * 128u +
-               ((uint32_t)(((col >> 3) & 7) ^ (pw & 7)) << 4);
-      fbo[r] = 2 * XH + (uint32_t)(pw >> 3) * (NYA * 1024u) + (uint32_t)(colb >> 6) * 1024u + (uint32_t)(pw & 7) * 128u +
-               ((uint32_t)(((colb >> 3) & 7) ^ (pw & 7)) << 4);
-      fsrc[r] = (!former || f >= NBY * 4) ? -1 : (V.ys + col < V.nbp ? V.ys + col : -2);
-    }
-    const float* bsrc = CURRENT ? V.btab + (size_t)kl * V.nsum_max + lane : nullptr;
-    const uint32_t fb_off = Cfg::B_OFF + (uint32_t)warp * 128u + (uint32_t)lane * 4u;
+    const __half* ysrc_b = CURRENT ? V.ybt + (size_t)kl * V.nsum_max * pstride : nullptr;
 
-    // b(i) c chunks of the chunk in a stage, from this thread's own c copies
+    // y' images of the chunks this thread copied into a stage
+    constexpr uint32_t NEG = 0x80008000u;
     auto form = [&](int stage) {
-      if constexpr (CURRENT) {
-        if (!former) return;
-        const uint32_t st = sbase + (uint32_t)stage * STAGE;
-        const float b = lds_f32(st + fb_off);
+      const uint32_t st = sbase + (uint32_t)stage * STAGE;
 #pragma unroll
-        for (int r = 0; r < FR; ++r) {
-          if (fsrc[r] == -1) continue;
-          const uint32_t ci = 4 * NYA * 1024u;
-          uint4 rh = lds16(st + fco[r]), ih = lds16(st + fco[r] + ci);
-          uint4 rl = lds16(st + fco[r] + YH), il = lds16(st + fco[r] + YH + ci);
-          uint32_t* prh = &rh.x;
-          uint32_t* pih = &ih.x;
-          uint32_t* prl = &rl.x;
-          uint32_t* pil = &il.x;
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&prh[e]));
-            const float2 c = __half22float2(*reinterpret_cast<const __half2*>(&pih[e]));
-            const float2 al = __half22float2(*reinterpret_cast<const __half2*>(&prl[e]));
-            const float2 cl = __half22float2(*reinterpret_cast<const __half2*>(&pil[e]));
-            uint32_t ohr = 0, ohi = 0, olr = 0, oli = 0;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              const float re = ((h ? a.y : a.x) + (h ? al.y : al.x)) * b;
-              const float im = ((h ? c.y : c.x) + (h ? cl.y : cl.x)) * b;
-              const __half2 hh = __floats2half2_rn(re, im);
-              const float2 hf = __half22float2(hh);
-              const __half2 ll = __floats2half2_rn(re - hf.x, im - hf.y);
-              const __half2_raw hr = hh, lr = ll;
-              ohr |= (uint32_t)hr.x << (16 * h);
-              ohi |= (uint32_t)hr.y << (16 * h);
-              olr |= (uint32_t)lr.x << (16 * h);
-              oli |= (uint32_t)lr.y << (16 * h);
-            }
-            prh[e] = ohr;
-            pih[e] = ohi;
-            prl[e] = olr;
-            pil[e] = oli;
-          }
-          sts16(st + fbo[r], rh);
-          sts16(st + fbo[r] + ci, ih);
-          sts16(st + fbo[r] + YH, rl);
-          sts16(st + fbo[r] + YH + ci, il);
-        }
+      for (int v = 0; v < YV; ++v) {
+        if (ysrc[v] < 0) continue;
+        uint4 w = lds16(st + ydst[v]);
+        if (ysrc[v] & (1 << 23)) w = make_uint4(w.x ^ NEG, w.y ^ NEG, w.z ^ NEG, w.w ^ NEG);
+        sts16(st + yidst[v], w);
       }
     };
 
@@ -360,30 +308,14 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
         for (int u4 = 0; u4 < 4; ++u4)
           cp16z(st + xoff + (uint32_t)(u4 >> 1) * XH + (uint32_t)(u4 & 1) * 8192u, src + u4 * V.nbp, sz);
         const int i0 = chunk_of(u) * VM_I;
-        if constexpr (CURRENT) {
-          if (former) {
-            const int i = i0 + lane;
-#pragma unroll
-            for (int r = 0; r < FR; ++r) {
-              if (fsrc[r] == -1) continue;
-              const bool ok = fsrc[r] >= 0 && i < nsum;
-              const __half* src = ok ? ysrc_c + (size_t)i * pstride + fsrc[r] : ysrc_c;
-              const uint32_t sz = ok ? 16u : 0u;
-              cp16z(st + fco[r], src, sz);
-              cp16z(st + fco[r] + 4 * NYA * 1024u, src + V.nbp, sz);
-              cp16z(st + fco[r] + YH, src + 2 * V.nbp, sz);
-              cp16z(st + fco[r] + YH + 4 * NYA * 1024u, src + 3 * V.nbp, sz);
-            }
-            cp4(st + fb_off, bsrc + i0);
-          }
-        }
 #pragma unroll
         for (int v = 0; v < YV; ++v) {
-          if (CURRENT || ysrc[v] < 0) continue;
+          if (ysrc[v] < 0) continue;
           const int i = i0 + ((ysrc[v] >> 16) & 31);
           const bool ok = !(ysrc[v] & (1 << 22)) && i < nsum;
           const int so = ysrc[v] & 0xffff;
-          cp16z(st + ydst[v], ok ? ysrc_c + (size_t)i * pstride + so : ysrc_c, ok ? 16u : 0u);
+          const __half* b = (CURRENT && (ysrc[v] & (1 << 21))) ? ysrc_b : ysrc_c;
+          cp16z(st + ydst[v], ok ? b + (size_t)i * pstride + so : ysrc_c, ok ? 16u : 0u);
         }
       }
       cp_commit();
@@ -537,24 +469,28 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
   if (warp == 0) tc::tmem_dealloc(taddr, Cfg::NCOL);
 }
 
-// b(i) = Gcar (R1 G1_i)_mu sB / 2^14 of every FBZ k-point of the launch, zero
-// beyond nsum: btab[k_local][i].
-struct BtabCtx {
+// b(i) c of every FBZ k-point of the launch, split like the coefficient planes:
+// ybt[k_local][i][plane][band], b(i) = Gcar (R1 G1_i)_mu sB / 2^14 (zero beyond
+// nsum), c the planes of K1; (h + l) b is split again into fp16 hi + lo.
+struct YbtCtx {
   const int* kmap;
   const double* G;
   const double* Rcart;
   const int* gidx;
   const int* npw;
-  float* btab;
-  int k0, nk, npwx, nsum_max, legacy, nsum_legacy, comp;
+  const __half* planes;
+  __half* ybt;
+  int k0, nk, npwx, nbp, nsum_max, legacy, nsum_legacy, comp;
   double Gcar;
   float sB;
 };
 
-__global__ void k_vtx_btab_mn(BtabCtx Y) {
-  const size_t n = (size_t)Y.nk * Y.nsum_max;
+__global__ void k_vtx_ybt(YbtCtx Y) {
+  const size_t n = (size_t)Y.nk * Y.nsum_max * Y.nbp;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(e % Y.nsum_max), kl = (int)(e / Y.nsum_max);
+    const int band = (int)(e % Y.nbp);
+    const size_t r = e / Y.nbp;
+    const int i = (int)(r % Y.nsum_max), kl = (int)(r / Y.nsum_max);
     const int* km = Y.kmap + 5 * (Y.k0 + kl);
     const int K1 = km[0];
     const int nsum = Y.legacy ? Y.nsum_legacy : Y.npw[K1];
@@ -564,7 +500,17 @@ __global__ void k_vtx_btab_mn(BtabCtx Y) {
       const double* g1 = Y.G + 3 * Y.gidx[(size_t)K1 * Y.npwx + i];
       b = (float)(Y.Gcar * (R[0] * g1[0] + R[1] * g1[1] + R[2] * g1[2])) * Y.sB * (1.0f / 16384.0f);
     }
-    Y.btab[e] = b;
+    const __half* c = Y.planes + ((size_t)K1 * Y.npwx + (i < nsum ? i : 0)) * 4 * Y.nbp + band;
+    const float re = (__half2float(c[0]) + __half2float(c[2 * Y.nbp])) * b;
+    const float im = (__half2float(c[Y.nbp]) + __half2float(c[3 * Y.nbp])) * b;
+    const __half2 hh = __floats2half2_rn(re, im);
+    const float2 hf = __half22float2(hh);
+    const __half2 ll = __floats2half2_rn(re - hf.x, im - hf.y);
+    __half* o = Y.ybt + r * 4 * Y.nbp + band;
+    o[0] = __low2half(hh);
+    o[Y.nbp] = __high2half(hh);
+    o[2 * Y.nbp] = __low2half(ll);
+    o[3 * Y.nbp] = __high2half(ll);
   }
 }
 
@@ -581,23 +527,19 @@ static int launch_vmn(rpa_ctx* c, const VtxMnCtx& V, int nk) {
 
 template <bool CURRENT>
 static int launch_vmn_nby(rpa_ctx* c, const VtxMnCtx& V, int nk, int nby) {
-  switch (nby) {
-    case 16: return launch_vmn<16, CURRENT>(c, V, nk);
-    case 32: return launch_vmn<32, CURRENT>(c, V, nk);
-    case 48: return launch_vmn<48, CURRENT>(c, V, nk);
-    case 64: return launch_vmn<64, CURRENT>(c, V, nk);
-    default: break;
-  }
+  if (nby == 16) return launch_vmn<16, CURRENT>(c, V, nk);
+  if (nby == 32) return launch_vmn<32, CURRENT>(c, V, nk);
   if constexpr (!CURRENT) {
-    if (nby == 80) return launch_vmn<80, false>(c, V, nk);
-    if (nby == 96) return launch_vmn<96, false>(c, V, nk);
+    if (nby == 48) return launch_vmn<48, false>(c, V, nk);
+    if (nby == 64) return launch_vmn<64, false>(c, V, nk);
   }
   return fail(c, RPA_EINVAL, "vertices: no kernel for a %d-band window", nby);
 }
 
 // One launch per pair of band windows: gathered bands [x0, x1) in windows of
 // 32 starting on multiples of 8, sequential bands [y0, y1) in windows of at most
-// ymax (multiples of 16 wide, starting on a multiple of 8).
+// ymax (multiples of 16 wide, starting on a multiple of 8; the Y tile, y and y'
+// of every column block, spans at most 128 columns so that three stages fit).
 template <bool CURRENT>
 static int launch_windows_mn(rpa_ctx* c, VtxMnCtx V, int nk, int x0, int x1, int y0, int y1, int ymax) {
   const int ys0 = y0 & ~7, span = y1 - ys0;
@@ -682,7 +624,7 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
   V.Glf = c->d_Glf.as<double>();
   V.npw = c->d_npw.as<int>();
   V.planes = c->d_cpl.as<__half>();
-  V.btab = nullptr;
+  V.ybt = nullptr;
   V.map = map;
   V.trans = c->d_trans.as<Trans>();
   V.offsets = c->d_offsets.as<long long>();
@@ -707,7 +649,7 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
     V.M = Mf;
     V.amax = amax;
     *used = true;
-    return launch_windows_mn<false>(c, V, nk, x0, x1, y0, y1, 96);
+    return launch_windows_mn<false>(c, V, nk, x0, x1, y0, y1, 64);
   }
   // current vertices: |C| <= 1 (orthonormal bands), |b(i)| <= Gcar max|G|
   double gmax = 0.0;
@@ -727,18 +669,20 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
     case RPA_POL_YZ: comps[0] = 1; comps[1] = 2; break;
     default: comps[0] = 2; comps[1] = 1; break;
   }
-  RPA_TRY(ensure(c, c->d_vbt, sizeof(float) * (size_t)nk * nsum_max));
-  V.btab = c->d_vbt.as<float>();
-  BtabCtx Y;
+  RPA_TRY(ensure(c, c->d_ybt, sizeof(__half) * (size_t)nk * nsum_max * 4 * c->nbp));
+  V.ybt = c->d_ybt.as<__half>();
+  YbtCtx Y;
   Y.kmap = V.kmap;
   Y.G = c->d_G.as<double>();
   Y.Rcart = c->d_Rcart.as<double>();
   Y.gidx = c->d_gidx.as<int>();
   Y.npw = V.npw;
-  Y.btab = c->d_vbt.as<float>();
+  Y.planes = V.planes;
+  Y.ybt = c->d_ybt.as<__half>();
   Y.k0 = k0;
   Y.nk = nk;
   Y.npwx = c->npwx;
+  Y.nbp = c->nbp;
   Y.nsum_max = nsum_max;
   Y.legacy = V.legacy;
   Y.nsum_legacy = P.nsum_legacy;
@@ -749,10 +693,10 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
     V.comp = Y.comp = comps[a];
     V.M = a == 0 ? Mf : Mf2;
     V.amax = amax + a;
-    k_vtx_btab_mn<<<2048, 256, 0, c->stream>>>(Y);
+    k_vtx_ybt<<<4096, 256, 0, c->stream>>>(Y);
     RPA_CUDA(c, cudaGetLastError());
     ++c->launches;
-    RPA_TRY(launch_windows_mn<true>(c, V, nk, x0, x1, y0, y1, 64));
+    RPA_TRY(launch_windows_mn<true>(c, V, nk, x0, x1, y0, y1, 32));
   }
   *used = true;
   return RPA_OK;

@@ -575,7 +575,11 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
   if (c->npwx > 32767 || c->nbnd > 181 || c->d_cpl.p == nullptr) return RPA_OK;
   const bool current = P.mode == RPA_MODE_CURRENT;
   const bool two = current && (P.pol == RPA_POL_YZ || P.pol == RPA_POL_ZY);
-  const bool swap = !current && !c->legacy && P.nocc < c->nbnd - P.nocc;
+  // gathered side of charge vertices: the tuned choice, else the side with fewer bands
+  const int want_swap = c->vt_cur.swap >= 0 ? c->vt_cur.swap : (P.nocc < c->nbnd - P.nocc ? 1 : 0);
+  const bool swap = !current && !c->legacy && want_swap == 1;
+  const int ymax_cur = c->vt_cur.ymax > 0 ? std::min(c->vt_cur.ymax, 32) : 32;
+  const int ymax_chg = c->vt_cur.ymax > 0 ? std::min(c->vt_cur.ymax, 64) : 64;
   int x0, x1, y0, y1;
   if (current) {
     x0 = 0, x1 = c->nbnd, y0 = 0, y1 = c->nbnd;
@@ -649,7 +653,7 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
     V.M = Mf;
     V.amax = amax;
     *used = true;
-    return launch_windows_mn<false>(c, V, nk, x0, x1, y0, y1, 64);
+    return launch_windows_mn<false>(c, V, nk, x0, x1, y0, y1, ymax_chg);
   }
   // current vertices: |C| <= 1 (orthonormal bands), |b(i)| <= Gcar max|G|
   double gmax = 0.0;
@@ -696,7 +700,7 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
     k_vtx_ybt<<<4096, 256, 0, c->stream>>>(Y);
     RPA_CUDA(c, cudaGetLastError());
     ++c->launches;
-    RPA_TRY(launch_windows_mn<true>(c, V, nk, x0, x1, y0, y1, 32));
+    RPA_TRY(launch_windows_mn<true>(c, V, nk, x0, x1, y0, y1, ymax_cur));
   }
   *used = true;
   return RPA_OK;

@@ -324,6 +324,7 @@ int rpa_create_shared(rpa_ctx** out, rpa_ctx* parent, int precision) {
   c->split_f16 = parent->split_f16;
   c->tc_seg = parent->tc_seg;
   c->vertex_kind = parent->vertex_kind;
+  c->vt_table = parent->vt_table;
   c->nbp = parent->nbp;
   c->ng = parent->ng;
   c->h_miller = parent->h_miller;
@@ -606,6 +607,11 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
     return fail(c, RPA_EINVAL, "rpa_chi0: nocc must be in 1..nbnd-1");
   if (a->mode == RPA_MODE_CURRENT && !(a->T > 0)) return fail(c, RPA_EINVAL, "rpa_chi0: T must be > 0");
   cudaSetDevice(c->device);
+  if (!c->vt_forced) {
+    // tuned vertex configuration of this shape, if any
+    const auto it = c->vt_table.find(vtx_tune_key(a->mode, c->nbnd, a->mode == RPA_MODE_CHARGE ? a->nocc : 0, c->nlf));
+    c->vt_cur = it != c->vt_table.end() ? it->second : rpa_ctx::VtxTune();
+  }
 
   Chi0Plan P;
   P.mode = a->mode;

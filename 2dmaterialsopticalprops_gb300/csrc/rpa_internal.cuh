@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "../../include/rpa_gpu.h"
@@ -99,6 +100,18 @@ struct rpa_ctx {
   int last_mode = -1, last_no = 0, last_nw = 0;
   double last_domega = 0.0, last_Gcar = 0.0;
   bool have_S = false, have_chi0 = false, have_W = false;
+  // mixed-path vertex configuration: band-window width of the sequential side
+  // (0: default) and gathered side for charge vertices (-1: fewer bands, 0:
+  // empty bands through Gfast, 1: occupied bands through the inverse map); the
+  // choice of the running rpa_chi0 call and the table that rpa_autotune fills,
+  // keyed by (mode, nbnd, nocc, NGloc / 32)
+  struct VtxTune {
+    int ymax = 0, swap = -1;
+    double ms = 0.0;
+  };
+  VtxTune vt_cur;
+  bool vt_forced = false;
+  std::map<long long, VtxTune> vt_table;
   // fixed KK kernel on the device (d_kk, d_kkf): the (variant, no, domega) it was built for
   int kk_key_variant = -1, kk_key_no = 0;
   double kk_key_domega = 0.0;
@@ -138,6 +151,11 @@ struct Chi0Plan {
 };
 
 int build_gfast(rpa_ctx* c, int ik, int nsum_legacy, int* out);
+
+// key of the vertex tuning table: (mode, nbnd, nocc, NGloc / 32)
+inline long long vtx_tune_key(int mode, int nbnd, int nocc, int nlf) {
+  return (long long)mode | ((long long)nbnd << 4) | ((long long)nocc << 20) | ((long long)(nlf / 32) << 36);
+}
 int kk_apply_real_fp64(rpa_ctx* c, DevBuf& buf, const std::vector<double>& K, int nrow, int nw, const double* S,
                        double2* out, int np, bool pi_epilogue);
 

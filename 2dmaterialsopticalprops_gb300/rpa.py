@@ -28,7 +28,8 @@ EXPORTS = ["rpa_create", "rpa_destroy", "rpa_last_error", "rpa_set_gvectors", "r
            "rpa_basis_info", "rpa_create_shared", "rpa_server_create", "rpa_server_submit", "rpa_server_wait",
            "rpa_server_last_error", "rpa_server_destroy", "rpa_pi", "rpa_kk_w", "rpa_gen_fbz",
            "rpa_find_k_ibz", "rpa_find_kq", "rpa_qe_read_gvectors", "rpa_qe_wfc_info", "rpa_qe_read_wfc",
-           "rpa_write_corrfun", "rpa_read_corrfun", "rpa_write_wt"]
+           "rpa_write_corrfun", "rpa_read_corrfun", "rpa_write_wt", "rpa_autotune",
+           "rpa_tune_export", "rpa_tune_import"]
 
 
 class RpaOpts(C.Structure):
@@ -108,6 +109,9 @@ def load_library(path: str = LIB_PATH):
     L.rpa_write_corrfun.argtypes = [cp, cp, ip, ip, dp, vp, vp]
     L.rpa_read_corrfun.argtypes = [cp, cp, ip, ip, vp, vp]
     L.rpa_write_wt.argtypes = [cp, ip, ip, dp, vp]
+    L.rpa_autotune.argtypes = [vp, C.POINTER(RpaChi0Args), vp]
+    L.rpa_tune_export.argtypes = [vp, vp, ip, vp]
+    L.rpa_tune_import.argtypes = [vp, cp]
     L.rpa_create_shared.argtypes = [C.POINTER(vp), vp, ip]
     L.rpa_server_create.argtypes = [C.POINTER(vp), vp, ip, dp]
     L.rpa_server_submit.argtypes = [vp, C.POINTER(RpaRequest), C.POINTER(C.c_longlong)]
@@ -395,6 +399,28 @@ class Context:
         out = np.zeros(6)
         self._chk(self.L.rpa_stage_times(self.h, _p(out)))
         return dict(zip(["pairs", "vertices", "accumulate", "kk", "dyson", "copies"], out.tolist()))
+
+    def autotune(self, mode: int, **kw) -> float:
+        """rpa_autotune for the chi0 call chi0(mode, **kw) would make; returns the
+        best vertex-stage time (ms)."""
+        pol = kw.pop("pol", "xx")
+        args = RpaChi0Args(mode=mode, pol=POL[pol], ngd=kw.get("ngd", 0), nocc=kw.get("nocc", 0), no=kw["no"],
+                           ntot_norm=kw.get("ntot_norm", 0), domega=kw["domega"], eta=kw["eta"],
+                           lor_cut=kw.get("lor_cut", 1e-3), df_cut=kw.get("df_cut", 1e-4), T=kw.get("T", 0.0),
+                           Efermi=kw.get("Efermi", 0.0), Vcell=kw["Vcell"], Gcar=kw["Gcar"])
+        ms = C.c_double()
+        self._chk(self.L.rpa_autotune(self.h, C.byref(args), C.byref(ms)))
+        return ms.value
+
+    def tune_export(self) -> str:
+        n = C.c_int()
+        self._chk(self.L.rpa_tune_export(self.h, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        self._chk(self.L.rpa_tune_export(self.h, buf, n.value, C.byref(n)))
+        return buf.value.decode()
+
+    def tune_import(self, text: str):
+        self._chk(self.L.rpa_tune_import(self.h, text.encode()))
 
     def chi0_stats(self):
         out = np.zeros(4)

@@ -142,6 +142,23 @@ int rpa_find_k_ibz(rpa_ctx* ctx, int ntot, const double* ktot, int nki, const do
 int rpa_find_kq(rpa_ctx* ctx, int ntot, const double* ktot, int nki, const double* kI, const double* q, double eps,
                 int* iG0, int* R2, int* K2);
 
+/* ---- Vertex tile autotuner (mixed path; no counterpart in the reference) ------
+ * Runs the chi0 call of args on the current k map and q once per candidate
+ * tensor-core vertex configuration (band-window width of the sequential side;
+ * for charge vertices also the gathered side) and keeps the fastest for later
+ * rpa_chi0 calls with the same (mode, nbnd, nocc, NGloc / 32); *best_ms (may be
+ * NULL) = its vertex-stage time.  Shared contexts start with their parent's
+ * table.  RPA_ESTATE on an FP64 context or with reserved[1] != 0. */
+int rpa_autotune(rpa_ctx* ctx, const rpa_chi0_args* args, double* best_ms);
+
+/* The table as JSON text ({"vertex": [{"mode", "nbnd", "nocc", "nlf32", "ymax",
+ * "swap", "ms"}, ...]}); *len = bytes needed including the NUL (buf may be NULL
+ * to query it). */
+int rpa_tune_export(const rpa_ctx* ctx, char* buf, int cap, int* len);
+
+/* Replaces the table by the one in json (as written by rpa_tune_export). */
+int rpa_tune_import(rpa_ctx* ctx, const char* json);
+
 /* ---- On-disk formats (host only, no context; errors via rpa_last_error(NULL)) --
  *
  * Replaces: loadG (Modules/io_qe.f90:11-71).  Reads the Miller indices of

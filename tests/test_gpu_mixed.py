@@ -133,3 +133,46 @@ def test_vertex_kernels_agree(synth, rpa, orc, kind):
     assert rel(a, Sco) < TOL and rel(b, Sco) < TOL
     ref.close()
     alt.close()
+
+
+def test_autotune_and_every_vertex_configuration(synth, rpa, orc):
+    """rpa_autotune keeps one configuration per shape; every configuration it can
+    choose (band-window width, gathered side) gives S0 within the mixed-path
+    tolerance, and the table survives an export / import round trip."""
+    import json
+    s = synth.build(synth.config_small(nbnd=24, nocc=5, npw=120, nlf=11, no=31))
+    ctx = rpa.Context(precision=rpa.PREC_MIXED)
+    ctx.load_system(s)
+    So = orc.sloss_s0(orc.Bound(s))
+    Sco, _ = orc.optabs_s0(orc.Bound(s, pol="zz"))
+    ms = ctx.autotune(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+    assert ms > 0
+    ctx.autotune(rpa.MODE_CURRENT, **rpa.optabs_args(s, "zz"))
+    table = json.loads(ctx.tune_export())["vertex"]
+    assert {e["mode"] for e in table} == {rpa.MODE_CHARGE, rpa.MODE_CURRENT}
+    S, _ = ctx.chi0(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+    assert rel(S, So) < TOL
+    nlf32 = s.nlf // 32
+    for ymax in (16, 32, 48, 64):
+        for swap in (0, 1):
+            ctx.tune_import(json.dumps({"vertex": [{"mode": rpa.MODE_CHARGE, "nbnd": 24, "nocc": 5, "nlf32": nlf32,
+                                                    "ymax": ymax, "swap": swap}]}))
+            S, _ = ctx.chi0(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+            assert rel(S, So) < TOL, (ymax, swap)
+    for ymax in (16, 32):
+        ctx.tune_import(json.dumps({"vertex": [{"mode": rpa.MODE_CURRENT, "nbnd": 24, "nocc": 0, "nlf32": nlf32,
+                                                "ymax": ymax, "swap": -1}]}))
+        S, _ = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, "zz"))
+        assert rel(S, Sco) < TOL, ymax
+    other = rpa.Context(precision=rpa.PREC_MIXED)
+    other.tune_import(json.dumps({"vertex": table}))
+    assert json.loads(other.tune_export())["vertex"] == table
+    with pytest.raises(rpa.RpaError):
+        other.tune_import('{"vertex": [{"mode": 0, "nbnd": 24, "nocc": 5, "nlf32": 0, "ymax": 24, "swap": 1}]}')
+    fp = rpa.Context()
+    fp.load_system(s)
+    with pytest.raises(rpa.RpaError) as e:
+        fp.autotune(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+    assert e.value.code == rpa.RPA_ESTATE
+    for c in (ctx, other, fp):
+        c.close()

@@ -425,7 +425,7 @@ def kmap_run(nk: int = 120, oracle_sample: int = 24):
                                        f"{ktot.shape[0]} FBZ points, scaled by the point count"}}
 
 
-def c5_run(n_q: int = 16, nk_full: int = 96, nk_check: int = 24, q_check=(1, 8)):
+def c5_run(n_q: int = 16, nk_full: int = 96, nk_check: int = 24, q_check=(1, 8), autotune: bool = True):
     """W(q, w) for 16 q-points at full size on the mixed path (timed), and the
     mixed-vs-FP64 comparison (time ratio, per-q max / RMS error of Im W) on
     the same workload with a 24x24 k-grid."""
@@ -468,6 +468,14 @@ def c5_run(n_q: int = 16, nk_full: int = 96, nk_check: int = 24, q_check=(1, 8))
     t_setup = time.perf_counter() - t0
     steps = list(range(1, n_q + 1))
     w_chain(cm, s, steps[0])  # warm-up (buffers reach their sizes)
+    vert_default = cm.stage_times()["vertices"]
+    tune = None
+    if autotune:
+        # vertex tile autotuner on the first q-point; later q-points use its choice
+        t = time.perf_counter()
+        best = cm.autotune(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+        tune = {"tune_s": time.perf_counter() - t, "best_vertex_ms": best, "default_vertex_ms": vert_default,
+                "table": json.loads(cm.tune_export())["vertex"]}
     t = time.perf_counter()
     for st in steps:
         w_chain(cm, s, st)
@@ -478,7 +486,7 @@ def c5_run(n_q: int = 16, nk_full: int = 96, nk_check: int = 24, q_check=(1, 8))
                         f"NGloc=301, nw=701 on 0-50 eV, eta=50 meV, {n_q} q-points (1..{n_q} grid steps along "
                         f"Gamma-M); loss chain per q (S0, KK, FP64 Dyson, W)",
             "n_q": n_q, "mixed_s": t_full, "value": n_q / t_full, "unit": "q-spectra/s", "setup_s": t_setup,
-            "last_q_stage_ms": st_times,
+            "last_q_stage_ms": st_times, "autotune": tune,
             "check": {"grid": f"{nk_check}x{nk_check}", "mixed_s": tm, "fp64_s": t64, "mixed_over_fp64": t64 / tm,
                       "errors_vs_fp64_gpu": errs}}
 

@@ -510,31 +510,56 @@ int build_gmap(rpa_ctx* c, int k0, int nk, int nsum_max, int16_t* gmap, int nsum
   return RPA_OK;
 }
 
+// Basis position in K1 of the plane wave that Gfast sends to basis position p
+// of K2 for local field g, or -1: Gfast inverted in integer crystal
+// coordinates, G_i = R1^-1 (R2 G_p - Glf_g - G_iG0), then looked up in K1's basis.
+__device__ __forceinline__ int gfast_inv_pos(const MapCtx& C, const int* km, int g, int p) {
+  int K1 = km[0], R1 = km[1], K2 = km[2], R2 = km[3], iG0 = km[4];
+  int gp = C.gidx[(size_t)K2 * C.npwx + p];
+  const int* mp = C.miller + 3 * gp;
+  const int* r = C.Rc + 9 * R2;
+  int b0 = r[0] * mp[0] + r[1] * mp[1] + r[2] * mp[2];
+  int b1 = r[3] * mp[0] + r[4] * mp[1] + r[5] * mp[2];
+  int b2 = r[6] * mp[0] + r[7] * mp[1] + r[8] * mp[2];
+  const int* ml = C.lf_miller + 3 * g;
+  const int* m0 = C.miller + 3 * iG0;
+  b0 -= ml[0] + m0[0];
+  b1 -= ml[1] + m0[1];
+  b2 -= ml[2] + m0[2];
+  const int* ri = C.RIc + 9 * R1;
+  int c0 = ri[0] * b0 + ri[1] * b1 + ri[2] * b2 - C.box_lo0;
+  int c1 = ri[3] * b0 + ri[4] * b1 + ri[5] * b2 - C.box_lo1;
+  int c2 = ri[6] * b0 + ri[7] * b1 + ri[8] * b2 - C.box_lo2;
+  if ((unsigned)c0 >= (unsigned)C.box_d0 || (unsigned)c1 >= (unsigned)C.box_d1 ||
+      (unsigned)c2 >= (unsigned)C.box_d2)
+    return -1;
+  int gg = C.box[((size_t)c0 * C.box_d1 + c1) * C.box_d2 + c2];
+  if (gg < 0) return -1;
+  return C.inv[(size_t)K1 * C.ng + gg];
+}
+
 // Inverse maps of the FBZ k-points [k0, k0+nk): ginv[k_local][G][p] = the K1
-// plane wave i with Gfast(G, i) = p (a basis position of K2), -1 where none.
-// Gfast(G, .) is injective (distinct G_i give distinct G''), so each p is
-// written at most once.
-__global__ void k_ginv(MapCtx C, int k0, int nk, int nsum_max, int nsum1_max, int16_t* __restrict__ ginv) {
-  const size_t per_k = (size_t)C.nlf * nsum1_max;
+// plane wave i with Gfast(G, i) = p (a basis position of K2), -1 where none or
+// p >= npw(K2).  Gfast(G, .) is injective (distinct G_i give distinct G''), and
+// R1, R2 are unimodular integer matrices in crystal coordinates, so the inverse
+// is computed directly for every p (one coalesced write each) and agrees with
+// inverting the forward map.
+__global__ void k_ginv(MapCtx C, int k0, int nk, int nsum_max, int16_t* __restrict__ ginv) {
+  const size_t per_k = (size_t)C.nlf * nsum_max;
   const size_t n = (size_t)nk * per_k;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     const int kl = (int)(e / per_k);
     const size_t r = e % per_k;
-    const int g = (int)(r / nsum1_max), i = (int)(r % nsum1_max);
+    const int g = (int)(r / nsum_max), p = (int)(r % nsum_max);
     const int* km = C.kmap + 5 * (k0 + kl);
-    if (i >= C.npw[km[0]]) continue;
-    const int p = gfast_pos(C, km, g, i);
-    if (p >= 0 && p < nsum_max) ginv[((size_t)kl * C.nlf + g) * nsum_max + p] = (int16_t)i;
+    ginv[e] = (int16_t)(p < C.npw[km[2]] ? gfast_inv_pos(C, km, g, p) : -1);
   }
 }
 
 int build_ginv(rpa_ctx* c, int k0, int nk, int nsum_max, int16_t* ginv) {
   if (c->legacy) return fail(c, RPA_EINVAL, "inverse Gfast map: needs the igk map of the basis");
   MapCtx C = make_map_ctx(c);
-  int nsum1_max = 0;
-  for (int i = 0; i < nk; ++i) nsum1_max = std::max(nsum1_max, c->h_npw[c->h_kmap[5 * (size_t)(k0 + i)]]);
-  RPA_CUDA(c, cudaMemsetAsync(ginv, 0xff, sizeof(int16_t) * (size_t)nk * c->nlf * nsum_max, c->stream));
-  k_ginv<<<4096, 256, 0, c->stream>>>(C, k0, nk, nsum_max, nsum1_max, ginv);
+  k_ginv<<<4096, 256, 0, c->stream>>>(C, k0, nk, nsum_max, ginv);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
   return RPA_OK;

@@ -363,6 +363,88 @@ def build(cfg: SynthConfig, coeff_only=None, coeff_out: np.ndarray | None = None
     return sysd
 
 
+def build_symmetric(cfg: SynthConfig) -> System:
+    """A seeded system with the C6v point group: bases, coefficients and
+    energies live on the IBZ of the Gamma-centred nk x nk grid (mp_ibz); the FBZ
+    points are the images R_i kI_j (i outer, first occurrence kept, with R1 / K1
+    the generating operation and IBZ point) and K+Q is matched to an FBZ point
+    modulo G (iG0), whose R1 / K1 become R2 / K2.  q = q_steps b1 / nk."""
+    a0, c0, Vcell, KC = hex_cell(cfg.a_ang, cfg.c_ang)
+    Gcar = 2.0 * math.pi / a0
+    b = KC.T
+    nsym, R, RI = hex_symmetry()
+    nk = cfg.nk
+    kI = mp_ibz(KC, nk, R, nsym)
+    nki = kI.shape[0]
+    vol_rec = abs(np.linalg.det(KC))
+    r = (3.0 * cfg.npw * vol_rec / (4.0 * math.pi)) ** (1.0 / 3.0)
+    kmax = np.linalg.norm(b[0])
+    _, Gtrial = g_list(KC, (2.0 * r + 2.0 * kmax) ** 2)
+    g2s = np.sort(np.einsum("ij,ij->i", Gtrial, Gtrial))
+    target = min(cfg.npw, g2s.size) - 1
+    ecutw = float(0.5 * (g2s[target] + g2s[min(target + 1, g2s.size - 1)]))
+    miller, G = g_list(KC, (math.sqrt(ecutw) * 2.0 + 2.0 * kmax) ** 2)
+    # FBZ: images R_i kI_j, i outer, first occurrence kept
+    ktot, K1, R1 = [], [], []
+    for i in range(nsym):
+        for j in range(nki):
+            k = R[i] @ kI[j]
+            if all(np.abs(k - kk).max() > 1e-6 for kk in ktot):
+                ktot.append(k)
+                K1.append(j + 1)
+                R1.append(i + 1)
+    ktot = np.array(ktot)
+    K1 = np.array(K1, dtype=np.int32)
+    R1 = np.array(R1, dtype=np.int32)
+    ntot = ktot.shape[0]
+    # K+Q = G + ktot_jk
+    q = (cfg.q_steps or 1) * b[0] / nk
+    Kinv = np.linalg.inv(KC)
+    mil_index = {tuple(m): i + 1 for i, m in enumerate(miller.tolist())}
+    K2 = np.zeros(ntot, dtype=np.int32)
+    R2 = np.zeros(ntot, dtype=np.int32)
+    iG0 = np.zeros(ntot, dtype=np.int32)
+    for ik in range(ntot):
+        kq = ktot[ik] + q
+        for jk in range(ntot):
+            d = Kinv @ (kq - ktot[jk])
+            m = np.rint(d)
+            if np.abs(d - m).max() < 1e-6 and tuple(int(x) for x in m) in mil_index:
+                iG0[ik] = mil_index[tuple(int(x) for x in m)]
+                K2[ik], R2[ik] = K1[jk], R1[jk]
+                break
+        if iG0[ik] == 0:
+            raise ValueError("K+Q not on the grid")
+    rng = np.random.default_rng(np.random.SeedSequence([cfg.seed, 7]))
+    E_ibz = tb_energies(kI, cfg.nbnd, cfg.nocc, cfg.t_ev, cfg.band_gap_step_ev, rng)
+    igks = [gk_sort(kI[i], G, ecutw) for i in range(nki)]
+    npw = np.array([x.size for x in igks], dtype=np.int32)
+    npwx = int(npw.max())
+    igk = np.zeros((nki, npwx), dtype=np.int32)
+    for i, x in enumerate(igks):
+        igk[i, :x.size] = x
+    coeff = make_coefficients(npw, cfg.nbnd, npwx, cfg.seed, 11, cfg.threads)
+    if cfg.lf == "z":
+        zsel = np.nonzero((miller[:, 0] == 0) & (miller[:, 1] == 0))[0]
+    else:
+        zsel = np.arange(miller.shape[0])
+    ilf = (zsel[:cfg.nlf] + 1).astype(np.int32)
+    Glf = G[ilf - 1].copy()
+    parG = np.where(miller[ilf - 1, 2] % 2 == 0, 1, -1).astype(np.int32)
+    omax = cfg.omax_ev / HARTREE_EV
+    domega = omax / (cfg.no - 1)
+    s = System(cfg=cfg, a0=a0, c0=c0, Vcell=Vcell, Gcar=Gcar, KC=KC, miller=miller, G=G,
+               nks=nki, nbnd=cfg.nbnd, nocc=cfg.nocc, npwx=npwx, npw=npw, igk=igk, ngd=int(npw.min()),
+               coeff=coeff, E=np.ascontiguousarray((E_ibz / HARTREE_EV).T), R=R, RI=RI,
+               ntot=ntot, ktot=ktot, K1=K1, R1=R1, K2=K2, R2=R2, iG0=iG0, nlf=cfg.nlf,
+               ilf=ilf, Glf=Glf, parG=parG, q=q, no=cfg.no, domega=domega,
+               eta=cfg.eta_ev / HARTREE_EV, T=cfg.T_ev / HARTREE_EV, Efermi=0.0)
+    s.extra["ecutw"] = ecutw
+    s.extra["kpts"] = kI
+    s.extra["nsym"] = nsym
+    return s
+
+
 def q_kmap(s: System, steps: int, steps2: int = 0) -> dict:
     """K+Q bookkeeping of the commensurate q = (steps b1 + steps2 b2) / nk on
     the Gamma-centred grid of a system built with q_steps: the basis is

@@ -176,3 +176,28 @@ def test_autotune_and_every_vertex_configuration(synth, rpa, orc):
     assert e.value.code == rpa.RPA_ESTATE
     for c in (ctx, other, fp):
         c.close()
+
+
+def test_mixed_point_group_system(synth, rpa, orc):
+    """The tensor-core vertices with symmetry operations in the maps (C6v):
+    both gathered sides of the charge vertices, and the current vertices whose
+    b(i) uses R1."""
+    import json
+    s = synth.build_symmetric(synth.config_small(nk=6, q_steps=1, nbnd=12, nocc=3, npw=60, nlf=7, no=31))
+    ctx = rpa.Context(precision=rpa.PREC_MIXED)
+    ctx.set_gvectors(s.miller, s.G, s.KC)
+    ctx.set_symmetry(s.extra["nsym"], s.R, s.RI)
+    ctx.load_basis(s.npw, s.igk, s.coeff, s.E)
+    ctx.kmap(s.ktot, s.K1, s.R1, s.K2, s.R2, s.iG0)
+    ctx.set_q(s.q, s.ilf, s.parG)
+    So = orc.sloss_s0(orc.Bound(s))
+    for swap in (1, 0):
+        ctx.tune_import(json.dumps({"vertex": [{"mode": rpa.MODE_CHARGE, "nbnd": 12, "nocc": 3, "nlf32": 0,
+                                                "ymax": 0, "swap": swap}]}))
+        S, _ = ctx.chi0(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+        assert rel(S, So) < TOL, swap
+    for pol in ("xx", "zy"):
+        Sc, _ = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, pol))
+        Sco, _ = orc.optabs_s0(orc.Bound(s, pol=pol))
+        assert rel(Sc, Sco) < TOL, pol
+    ctx.close()

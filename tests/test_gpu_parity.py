@@ -135,3 +135,33 @@ def test_bad_arguments_are_errors_not_crashes(synth, rpa):
         ctx.set_q(s.q, np.array([0], dtype=np.int32))
     assert e.value.code == rpa.RPA_EINVAL
     ctx.close()
+
+
+def test_point_group_system(synth, rpa, orc):
+    """C6v: FBZ points are rotated IBZ points (R1 != 1) and K+Q lands on
+    rotated ones (R2 != 1), so the Gfast maps and the current factors use the
+    symmetry matrices.  Maps bit-exact, S0 / Qeff to 1e-11, W to 1e-9."""
+    s = synth.build_symmetric(synth.config_small(nk=6, q_steps=1, npw=60, nlf=7, no=31))
+    assert len(set(s.R1.tolist())) > 1 and len(set(s.R2.tolist())) > 1
+    ctx = rpa.Context()
+    ctx.set_gvectors(s.miller, s.G, s.KC)
+    ctx.set_symmetry(s.extra["nsym"], s.R, s.RI)
+    ctx.load_basis(s.npw, s.igk, s.coeff, s.E)
+    ctx.kmap(s.ktot, s.K1, s.R1, s.K2, s.R2, s.iG0)
+    ctx.set_q(s.q, s.ilf, s.parG)
+    ctx.sys = s
+    b = orc.Bound(s)
+    for ik in (0, 9, s.ntot - 1):
+        assert (ctx.gfast(ik + 1) == orc.gfast(b, ik)).all()
+    S, _ = ctx.chi0(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+    So = orc.sloss_s0(b)
+    assert rel(S, So) < TOL
+    chi = ctx.kk(rpa.KK_SLOSS_REAL)
+    WT, _, _ = ctx.dyson(s.c0, s.cfg.eps)
+    WTo, _, rc = orc.dyson(orc.kk_sloss(So, s.domega), orc.genV(s), fast_wt=True)
+    assert rc == 0 and rel(WT, WTo) < TOL_DYSON
+    for pol in ("xx", "yz"):
+        Sc, Qc = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, pol))
+        Sco, Qco = orc.optabs_s0(orc.Bound(s, pol=pol))
+        assert rel(Sc, Sco) < TOL and rel(Qc, Qco) < TOL
+    ctx.close()

@@ -261,27 +261,29 @@ int kk_apply_real_fp64(rpa_ctx* c, DevBuf& buf, const std::vector<double>& K, in
 
 int kk_run(rpa_ctx* c, int variant, int no, double domega) {
   // the fixed kernel depends on (variant, no, domega) only: built on the host and
-  // copied once, then reused by every transform with the same grid
-  const bool cached = c->kk_key_variant == variant && c->kk_key_no == no && c->kk_key_domega == domega;
+  // copied once per variant slot, then reused by every transform with the same grid
+  const int sl = variant == RPA_KK_OPTABS_COMPLEX ? 0 : 1;
+  const bool cached = c->kk_key_no[sl] == no && c->kk_key_domega[sl] == domega;
   const int nw = variant == RPA_KK_OPTABS_COMPLEX ? 2 * no + 1 : no;
   const int nrow = no - 1, np = c->nlf * c->nlf;
+  DevBuf& dk = c->d_kk[sl];
+  DevBuf& dkf = c->d_kkf[sl];
   if (!cached) {
     std::vector<double> K;
     int nwk = 0;
     kk_matrix(variant, no, domega, K, &nwk);
-    c->kk_key_variant = -1;
-    RPA_TRY(ensure(c, c->d_kk, sizeof(double) * K.size()));
-    RPA_CUDA(c, cudaMemcpyAsync(c->d_kk.p, K.data(), sizeof(double) * K.size(), cudaMemcpyHostToDevice, c->stream));
+    c->kk_key_no[sl] = 0;
+    RPA_TRY(ensure(c, dk, sizeof(double) * K.size()));
+    RPA_CUDA(c, cudaMemcpyAsync(dk.p, K.data(), sizeof(double) * K.size(), cudaMemcpyHostToDevice, c->stream));
     if (c->precision == RPA_PREC_MIXED) {
       std::vector<float> Kf(K.begin(), K.end());
-      RPA_TRY(ensure(c, c->d_kkf, sizeof(float) * Kf.size()));
-      RPA_CUDA(c, cudaMemcpyAsync(c->d_kkf.p, Kf.data(), sizeof(float) * Kf.size(), cudaMemcpyHostToDevice,
+      RPA_TRY(ensure(c, dkf, sizeof(float) * Kf.size()));
+      RPA_CUDA(c, cudaMemcpyAsync(dkf.p, Kf.data(), sizeof(float) * Kf.size(), cudaMemcpyHostToDevice,
                                   c->stream));
     }
     RPA_CUDA(c, cudaStreamSynchronize(c->stream));  // the host copies of K go out of scope
-    c->kk_key_variant = variant;
-    c->kk_key_no = no;
-    c->kk_key_domega = domega;
+    c->kk_key_no[sl] = no;
+    c->kk_key_domega[sl] = domega;
   }
   RPA_TRY(ensure(c, c->d_chi0, sizeof(double2) * (size_t)nrow * np));
   const bool cplx = variant == RPA_KK_OPTABS_COMPLEX;
@@ -292,20 +294,20 @@ int kk_run(rpa_ctx* c, int variant, int no, double domega) {
   if (c->precision == RPA_PREC_MIXED) {
     dim3 g2((ncols + 127) / 128, (nrow + 31) / 32);
     if (cplx)
-      k_kk_f32<true><<<g2, 256, 0, c->stream>>>(c->d_kkf.as<float>(), c->d_S.as<double>(), c->d_chi0.as<double2>(),
+      k_kk_f32<true><<<g2, 256, 0, c->stream>>>(dkf.as<float>(), c->d_S.as<double>(), c->d_chi0.as<double2>(),
                                                 nrow, nw, np, pi_row0);
     else
-      k_kk_f32<false><<<g2, 256, 0, c->stream>>>(c->d_kkf.as<float>(), c->d_S.as<double>(), c->d_chi0.as<double2>(),
+      k_kk_f32<false><<<g2, 256, 0, c->stream>>>(dkf.as<float>(), c->d_S.as<double>(), c->d_chi0.as<double2>(),
                                                  nrow, nw, np, pi_row0);
     RPA_CUDA(c, cudaGetLastError());
     ++c->launches;
     return RPA_OK;
   }
   if (cplx)
-    k_kk_fp64<true><<<grid, 256, 0, c->stream>>>(c->d_kk.as<double>(), c->d_S.as<double>(),
+    k_kk_fp64<true><<<grid, 256, 0, c->stream>>>(dk.as<double>(), c->d_S.as<double>(),
                                                  c->d_chi0.as<double2>(), nrow, nw, np, pi_row0, KK_PI);
   else
-    k_kk_fp64<false><<<grid, 256, 0, c->stream>>>(c->d_kk.as<double>(), c->d_S.as<double>(),
+    k_kk_fp64<false><<<grid, 256, 0, c->stream>>>(dk.as<double>(), c->d_S.as<double>(),
                                                   c->d_chi0.as<double2>(), nrow, nw, np, pi_row0, KK_PI);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;

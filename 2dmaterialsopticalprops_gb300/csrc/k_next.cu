@@ -160,12 +160,10 @@ int rpa_kk_w(rpa_ctx* c, double* gamma_p_out, double* gamma_m_out, double* check
   ++c->launches;
   std::vector<double> Km, Kp;
   w1w2_matrices(no, c->last_domega, Km, Kp);
-  // Gamma+ = (W1, -pi S_W(io)) = (W1, Im WT); Gamma- = (-W2, 0); the kernels
-  // take the place of the cached chi0 transform kernel in d_kk / d_kkf
-  c->kk_key_variant = -1;
-  RPA_TRY(kk_apply_real_fp64(c, c->d_kk, Km, nwo, no, SW, Gp, np, true));
+  // Gamma+ = (W1, -pi S_W(io)) = (W1, Im WT); Gamma- = (-W2, 0)
+  RPA_TRY(kk_apply_real_fp64(c, c->d_kkw, Km, nwo, no, SW, Gp, np, true));
   for (double& x : Kp) x = -x;
-  RPA_TRY(kk_apply_real_fp64(c, c->d_kkf, Kp, nwo, no, SW, Gm, np, false));
+  RPA_TRY(kk_apply_real_fp64(c, c->d_kkw, Kp, nwo, no, SW, Gm, np, false));
   cudaEventRecord(c->ev[1], c->stream);
   // self-check on the (1,1) element (Sloss.f90:515-530)
   std::vector<double2> gp(nwo), gm(nwo), wt(nwo);

@@ -112,10 +112,12 @@ struct rpa_ctx {
   VtxTune vt_cur;
   bool vt_forced = false;
   std::map<long long, VtxTune> vt_table;
-  // fixed KK kernel on the device (d_kk, d_kkf): the (variant, no, domega) it was built for
-  int kk_key_variant = -1, kk_key_no = 0;
-  double kk_key_domega = 0.0;
-  rpa::DevBuf d_S, d_Sdf, d_Q, d_chi0, d_kk, d_kkf, d_V, d_eps, d_WT, d_flags, d_tmp;
+  // fixed KK kernels on the device, one slot per variant (Optabs, Sloss): FP64
+  // and FP32 copies and the (no, domega) each was built for (no = 0: empty)
+  int kk_key_no[2] = {0, 0};
+  double kk_key_domega[2] = {0.0, 0.0};
+  rpa::DevBuf d_kk[2], d_kkf[2];
+  rpa::DevBuf d_S, d_Sdf, d_Q, d_chi0, d_kkw, d_V, d_eps, d_WT, d_flags, d_tmp;
   double stage_ms[6] = {0, 0, 0, 0, 0, 0};
   long long launches = 0;  // kernels launched by this context
   double stats[4] = {0, 0, 0, 0};

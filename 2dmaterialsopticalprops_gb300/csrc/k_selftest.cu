@@ -145,4 +145,44 @@ int selftest_umma(int which, double* result) {
   return RPA_OK;
 }
 
+// A wait on an mbarrier that nothing arrives on: the bounded wait gives up
+// after `polls` suspending polls and the kernel records it in *status and
+// returns, the way every wait of the production kernels ends.
+__global__ void k_wait_selftest(uint32_t polls, int* status, long long* cycles) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  const long long t0 = clock64();
+  const bool ok = tc::mbar_wait(&bar, 0u, polls);
+  if (threadIdx.x == 0) {
+    *status = ok ? 0 : 1;
+    *cycles = clock64() - t0;
+  }
+}
+
+// Runs k_wait_selftest; *result = the cycles the wait took.  RPA_ETIMEOUT when
+// it gave up (the expected outcome), RPA_OK if it was released.
+int selftest_wait(double* result) {
+  int* status = nullptr;
+  long long* cycles = nullptr;
+  if (cudaMalloc(&status, 4) != cudaSuccess || cudaMalloc(&cycles, 8) != cudaSuccess) return RPA_ENOMEM;
+  cudaMemset(status, 0, 4);
+  k_wait_selftest<<<1, 32>>>(256u, status, cycles);
+  cudaError_t e = cudaDeviceSynchronize();
+  int st = 0;
+  long long cyc = 0;
+  if (e == cudaSuccess) {
+    cudaMemcpy(&st, status, 4, cudaMemcpyDeviceToHost);
+    cudaMemcpy(&cyc, cycles, 8, cudaMemcpyDeviceToHost);
+  }
+  cudaFree(status);
+  cudaFree(cycles);
+  if (e != cudaSuccess) return RPA_ECUDA;
+  *result = (double)cyc;
+  return st ? RPA_ETIMEOUT : RPA_OK;
+}
+
 }  // namespace rpa

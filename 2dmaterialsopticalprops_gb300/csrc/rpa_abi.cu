@@ -40,6 +40,7 @@ int kk_run(rpa_ctx* c, int variant, int no, double domega);
 int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singular, int* n_zero);
 void kk_matrix(int variant, int no, double domega, std::vector<double>& K, int* nw_out);
 int selftest_umma(int which, double* result);
+int selftest_wait(double* result);
 int gk_sort_host(const double* k, int npwx, int ngm, const double* g, double ecut, int* ngk, int* igk, double* gk);
 
 static thread_local std::string g_create_err;
@@ -942,7 +943,8 @@ int rpa_chi0_stats(const rpa_ctx* c, double* out4) {
 }
 
 int rpa_selftest(int which, double* result) {
-  if (!result || which < 0 || which > 2) return RPA_EINVAL;
+  if (!result || which < 0 || which > 3) return RPA_EINVAL;
+  if (which == 3) return selftest_wait(result);
   return selftest_umma(which, result);
 }
 

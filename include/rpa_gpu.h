@@ -305,7 +305,10 @@ int rpa_chi0_stats(const rpa_ctx* ctx, double* out4);
  * device: which = 0, 1, 2 runs a 128 x N x 192 bf16 tcgen05 GEMM (N = 192,
  * 96, 256) from swizzled shared-memory tiles into TMEM and stores in *result
  * its max relative deviation from an FP32 CUDA-core product of the same
- * values.  Returns RPA_ETIMEOUT if the bounded completion wait gave up. */
+ * values.  Returns RPA_ETIMEOUT if the bounded completion wait gave up.
+ * which = 3 waits on an mbarrier that nothing arrives on: the bounded wait
+ * gives up (a few milliseconds) and the call returns RPA_ETIMEOUT with *result
+ * = the cycles waited, leaving the device usable. */
 int rpa_selftest(int which, double* result);
 
 /* Number of CUDA kernels this context has launched so far (its own kernels;

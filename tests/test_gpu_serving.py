@@ -122,3 +122,24 @@ def test_shared_basis_is_protected(parent, rpa):
     assert e.value.code == rpa.RPA_ESTATE
     assert ctx.L.rpa_destroy(ctx.h) == rpa.RPA_ESTATE
     c.close()
+
+
+def test_a_failing_request_does_not_stop_the_server(parent, rpa, synth):
+    """A request whose chi0 arguments are invalid fails with its own error code;
+    the requests around it are served normally and unchanged."""
+    s, ctx = parent
+    reqs = _requests(rpa, synth, s)[:3]
+    srv = rpa.Server(ctx, nslots=2, mem_bytes=1e9)
+    ref = [srv.wait(srv.submit(**r))[0] for r in reqs]
+    bad = dict(reqs[0])
+    bad["args"] = dict(bad["args"], nocc=0)  # Sloss needs 1 <= nocc < nbnd
+    ids = [srv.submit(**reqs[0]), srv.submit(**bad), srv.submit(**reqs[1]), srv.submit(**reqs[2])]
+    out0 = srv.wait(ids[0])[0]
+    with pytest.raises(rpa.RpaError) as e:
+        srv.wait(ids[1])
+    assert e.value.code == rpa.RPA_EINVAL
+    outs = [out0, srv.wait(ids[2])[0], srv.wait(ids[3])[0]]
+    srv.close()
+    for o, r in zip(outs, ref):
+        for k in r:
+            assert rel(o[k], r[k]) <= TOL_SAME, k

@@ -8,3 +8,14 @@ pytestmark = pytest.mark.gpu
 def test_umma_gemm_matches_cuda_core_product(rpa, which):
     err = rpa.selftest(which)
     assert err < 1e-5, err
+
+
+def test_bounded_wait_times_out_and_the_device_stays_usable(rpa):
+    """A device wait whose flag nothing sets gives up, the host reads
+    RPA_ETIMEOUT, and the next tensor-core self-test still passes."""
+    import ctypes as C
+    L = rpa.load_library()
+    cycles = C.c_double()
+    assert L.rpa_selftest(3, C.byref(cycles)) == rpa.RPA_ETIMEOUT
+    assert cycles.value > 0
+    assert rpa.selftest(0) < 1e-5

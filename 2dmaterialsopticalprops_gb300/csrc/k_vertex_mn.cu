@@ -23,16 +23,19 @@
 // tile holds two column blocks, [y | y'] with y' = (-Im y rows 0-31, Re y rows
 // 32-63), so one MMA of N = 2 NYN per K step gives
 //     Re D = X . y  and  Im D = X . y' = X[Re] . (-Im y) + X[Im] . Re y
-// (wide MMAs: each one re-reads the 128-row X operand from shared memory, so
-// the fewer and wider the better).  The threads that copy a y chunk write its
-// y' image.  The current factor separates,
+// The threads that copy a y chunk write its y' image.  Per K step two MMAs:
+// Xh . [Yh | Yl] (both halves side by side, N up to 256) into [hi hi | cross]
+// columns, then Xl . Yh added to the cross columns; the two column blocks are
+// summed in FP32 at read-back.  (The tensor core reads its operands from
+// shared memory at 128 bytes per cycle: an N = 128 MMA just keeps up, an N = 256
+// one leaves a quarter of the bandwidth to the gathers.)  The current factor separates,
 // f(G,i) = a(G) + b(i): the b(i) c block (precomputed per launch, split like the
 // coefficient planes) is a second column block of y, and a(G) multiplies the c
 // block at read-back: M = a(G) D[c] + D[b c].  Each local-field tile sweeps the plane waves in the
 // opposite direction of the previous one, so the coefficient rows read last
 // are read again first while they are still in L2.
-// Three products per chunk, Xh Yl + Xl Yh + Xh Yh, into a fresh TMEM
-// accumulator (two, ping-pong) that the worker warps add to FP32 registers.
+// Each chunk goes into a fresh TMEM accumulator (two, ping-pong) that the
+// worker warps add to FP32 registers.
 // Warp roles: 16 worker warps gather chunk t + S - 1 into the ring of S
 // shared-memory stages and read back chunk t - 1 from TMEM; warp 16 issues
 // the MMAs.  Every wait is bounded and ends in an error status.
@@ -85,19 +88,20 @@ template <int NBY, bool CURRENT>
 struct VmCfg {
   static constexpr int NY = CURRENT ? 2 : 1;
   static constexpr int NYN = NY * NBY;                   // columns of one block (y or y')
-  static constexpr int NTA = (2 * NYN + 63) / 64;        // 64-wide atoms along N of the Y tile
+  static constexpr int NTA = (2 * NYN + 63) / 64;        // 64-wide atoms along N of one half (lo or hi) of Y
   static constexpr uint32_t XH = 64 * 128 * 2;           // one half (hi or lo) of X
-  static constexpr uint32_t YH = (uint32_t)NTA * 8192;   // one half of Y
-  static constexpr uint32_t STAGE = 2 * XH + 2 * YH;
+  static constexpr uint32_t YKG = (uint32_t)NTA * 2048;  // Y bytes per group of 8 K rows: hi atoms, then lo atoms
+  static constexpr uint32_t YLO = (uint32_t)NTA * 1024;  // offset of the lo atoms in a K group
+  static constexpr uint32_t STAGE = 2 * XH + 8 * YKG;
   static constexpr uint32_t PTAB = 32 * NBY * 2;         // int16 [32][NBY]
   static constexpr int S0 = (int)((VM_SMEM_MAX - 1024 - (int)PTAB) / (int)STAGE);
   static constexpr int S = S0 > VM_SMAX ? VM_SMAX : S0;
-  static constexpr uint32_t BUFC = 2 * NYN;              // Re block + Im block
-  static constexpr uint32_t NCOL = 4 * NYN <= 32 ? 32 : 4 * NYN <= 64 ? 64 : 4 * NYN <= 128 ? 128
-                                                       : 4 * NYN <= 256 ? 256 : 512;
+  static constexpr uint32_t N2 = 64 * NTA;                // columns of one block (y and y', padded)
+  static constexpr uint32_t BUFC = 2 * N2;               // hi hi block + cross block
+  static constexpr uint32_t NCOL = 2 * BUFC <= 256 ? 256 : 512;
   static constexpr int CW = NBY / 4;                     // columns per thread per block
   static constexpr size_t SMEM = (size_t)S * STAGE + PTAB + 1024;
-  static_assert(NBY % 16 == 0 && 2 * NYN <= 256, "window too wide");
+  static_assert(NBY % 16 == 0 && NTA <= 2, "window too wide");
   static_assert(S >= 3, "shared-memory ring too shallow");
 };
 
@@ -146,8 +150,8 @@ __device__ __forceinline__ void tmem_ld_n(uint32_t addr, float* v) {
 template <int NBY, bool CURRENT>
 __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
   using Cfg = VmCfg<NBY, CURRENT>;
-  constexpr int S = Cfg::S, NYN = Cfg::NYN, NTA = Cfg::NTA, CW = Cfg::CW;
-  constexpr uint32_t XH = Cfg::XH, YH = Cfg::YH, STAGE = Cfg::STAGE;
+  constexpr int S = Cfg::S, NYN = Cfg::NYN, CW = Cfg::CW;
+  constexpr uint32_t XH = Cfg::XH, YKG = Cfg::YKG, YLO = Cfg::YLO, STAGE = Cfg::STAGE;
 
   extern __shared__ unsigned char smraw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
@@ -200,10 +204,11 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
   if (warp == VM_WORKERS / 32) {
     // ---------------------------------------------------------------- MMA warp
     if (lane == 0) {
-      const uint32_t idesc = tc::idesc_f16_mn(128, 2 * NYN, false);
+      constexpr uint32_t N2 = Cfg::N2;
+      const uint32_t id1 = tc::idesc_f16_mn(128, 2 * N2, false), id2 = tc::idesc_f16_mn(128, N2, false);
       // descriptors of stage 0; a chunk adds its byte offsets / 16 to the start-address field
       const uint64_t dx0 = tc::desc_sw128_mn(sbase, 1024u, 2048u);
-      const uint64_t dy0 = tc::desc_sw128_mn(sbase + 2 * XH, 1024u, NTA * 1024u);
+      const uint64_t dy0 = tc::desc_sw128_mn(sbase + 2 * XH, 1024u, YKG);
       int last = -1;
       int s = 0, ph = 0;
       for (int t = 0; t < total; ++t) {
@@ -219,12 +224,11 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
         const uint64_t dx = dx0 + so, dy = dy0 + so;
         const uint32_t d = taddr + (uint32_t)((t & 1) * Cfg::BUFC);
 #pragma unroll
-        for (int p = 0; p < 3; ++p) {  // Xh Yl, Xl Yh, Xh Yh
-          const uint64_t xa = dx + (p == 1 ? XH >> 4 : 0u), yb = dy + (p == 0 ? YH >> 4 : 0u);
-#pragma unroll
-          for (int ks = 0; ks < 4; ++ks)
-            tc::mma_bf16(d, xa + (uint64_t)(ks * 256), yb + (uint64_t)(ks * 2 * NTA * 64), idesc,
-                         (p > 0 || ks > 0) ? 1u : 0u);
+        for (int ks = 0; ks < 4; ++ks) {
+          const uint64_t xh = dx + (uint64_t)(ks * 256), xl = xh + (XH >> 4);
+          const uint64_t y = dy + (uint64_t)(ks * 2 * (YKG >> 4));
+          tc::mma_bf16(d, xh, y, id1, ks > 0 ? 1u : 0u);  // Xh . [Yh | Yl]
+          tc::mma_bf16(d + N2, xl, y, id2, 1u);            // + Xl . Yh into the cross block
         }
         tc::mma_commit(&done[t & 1]);
         last = t;
@@ -262,10 +266,10 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
         const int col = 8 * j, u = 2 * half + part;
         const bool bblk = CURRENT && col >= NBY;
         const int band = V.ys + (bblk ? col - NBY : col);
-        ydst[v] = 2 * XH + (uint32_t)half * YH + (uint32_t)(kk >> 3) * (NTA * 1024u) + (uint32_t)(col >> 6) * 1024u +
+        ydst[v] = 2 * XH + (uint32_t)(kk >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(col >> 6) * 1024u +
                   (uint32_t)(kk & 7) * 128u + ((uint32_t)(((col >> 3) & 7) ^ (kk & 7)) << 4);
         const int ki = kk ^ 32, ci = NYN + col;  // y' row and column of the chunk
-        yidst[v] = 2 * XH + (uint32_t)half * YH + (uint32_t)(ki >> 3) * (NTA * 1024u) + (uint32_t)(ci >> 6) * 1024u +
+        yidst[v] = 2 * XH + (uint32_t)(ki >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(ci >> 6) * 1024u +
                    (uint32_t)(ki & 7) * 128u + ((uint32_t)(((ci >> 3) & 7) ^ (ki & 7)) << 4);
         ysrc[v] = (band < V.nbp ? u * V.nbp + band : (1 << 22)) | (pw << 16) | (bblk ? (1 << 21) : 0) | (part << 23);
       }
@@ -348,34 +352,27 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
       }
       tc::tc_fence_after();
       const uint32_t ad = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)((t & 1) * Cfg::BUFC + cg * CW);
-      {
-        float v[CW];
-        tmem_ld_n<CW>(ad, v);
+      constexpr uint32_t HH = Cfg::N2;  // the cross block
+#pragma unroll
+      for (int part = 0; part < 2; ++part) {
+        float* acc = part ? accI : accR;
+        const uint32_t a = ad + part * NYN;
+        float v[CW], vh[CW];
+        tmem_ld_n<CW>(a, v);
+        tmem_ld_n<CW>(a + HH, vh);
+        tc::tmem_ld_wait();
         if constexpr (CURRENT) {
-          float w[CW];
-          tmem_ld_n<CW>(ad + NBY, w);
+#pragma unroll
+          for (int j = 0; j < CW; ++j) v[j] = fa * (v[j] + vh[j]);
+          tmem_ld_n<CW>(a + NBY, vh);
+          float wh[CW];
+          tmem_ld_n<CW>(a + HH + NBY, wh);
           tc::tmem_ld_wait();
 #pragma unroll
-          for (int j = 0; j < CW; ++j) accR[j] += fmaf(fa, v[j], w[j]);
+          for (int j = 0; j < CW; ++j) acc[j] += v[j] + (vh[j] + wh[j]);
         } else {
-          tc::tmem_ld_wait();
 #pragma unroll
-          for (int j = 0; j < CW; ++j) accR[j] += v[j];
-        }
-      }
-      {
-        float v[CW];
-        tmem_ld_n<CW>(ad + NYN, v);
-        if constexpr (CURRENT) {
-          float w[CW];
-          tmem_ld_n<CW>(ad + NYN + NBY, w);
-          tc::tmem_ld_wait();
-#pragma unroll
-          for (int j = 0; j < CW; ++j) accI[j] += fmaf(fa, v[j], w[j]);
-        } else {
-          tc::tmem_ld_wait();
-#pragma unroll
-          for (int j = 0; j < CW; ++j) accI[j] += v[j];
+          for (int j = 0; j < CW; ++j) acc[j] += v[j] + vh[j];
         }
       }
       tc::tc_fence_before();

@@ -36,6 +36,9 @@ PKG = "2dmaterialsopticalprops_gb300"
 
 
 ACC_DRAM_BYTES_PER_PAIR = 30.4e9 / 54.6e6
+# DRAM bytes per FBZ k-point of one current-vertex launch (k_vertex_mn<32, current>):
+# ncu measured 15.9 + 0.55 GB for the 1600 k-points of the 40x40 case
+VTX_DRAM_BYTES_PER_K = 16.45e9 / 1600
 
 
 def pkg(name):
@@ -132,7 +135,15 @@ def run_step(ctx, s, rpa, host=None):
 def step_work(ctx, s, rpa):
     """Algorithmic work of one step, from the library's own counters."""
     work = {}
-    tot_acc = tot_vert = 0.0
+    tot_acc = tot_vert = vbytes = 0.0
+    # coefficients per FBZ k-point on the summed side (npw of K1; the legacy basis: ngd)
+    nsum_k = float(np.sum(s.npw[np.asarray(s.K1) - 1])) if s.igk is not None else float(s.ngd) * s.ntot
+
+    def vertex_bytes(st, nb):
+        # algorithmic bytes of one vertex pass: the coefficients of the bands
+        # read on both k-points (8 B per complex: fp16 hi/lo re/im), the int16
+        # Gfast map, the FP32 complex vertex rows written
+        return nb * 8.0 * nsum_k + 2.0 * s.nlf * nsum_k + 8.0 * s.nlf * st["transitions"]
     t = {"accumulate": 0.0, "vertices": 0.0, "pairs": 0.0, "kk": 0.0, "dyson": 0.0}
     n2 = float(s.nlf) ** 2
     for pol in ("xx", "zz"):
@@ -140,6 +151,7 @@ def step_work(ctx, s, rpa):
         st, tm = ctx.chi0_stats(), ctx.stage_times()
         tot_acc += 8.0 * n2 * st["sum_nwin"]
         tot_vert += 8.0 * st["vertex_macs"]
+        vbytes += vertex_bytes(st, 2 * s.nbnd)
         for k in ("accumulate", "vertices", "pairs"):
             t[k] += tm[k]
         ctx.kk(rpa.KK_OPTABS_COMPLEX, want=False)
@@ -149,6 +161,7 @@ def step_work(ctx, s, rpa):
     st, tm = ctx.chi0_stats(), ctx.stage_times()
     tot_acc += 8.0 * n2 * st["sum_nwin"]
     tot_vert += 8.0 * st["vertex_macs"]
+    vbytes += vertex_bytes(st, s.nbnd)
     for k in ("accumulate", "vertices", "pairs"):
         t[k] += tm[k]
     ctx.kk(rpa.KK_SLOSS_REAL, want=False)
@@ -156,7 +169,7 @@ def step_work(ctx, s, rpa):
     ctx.dyson(s.c0, s.cfg.eps, want_wt=False, want_epsinv=False, want_head=False)
     t["dyson"] += ctx.stage_times()["dyson"]
     work["loss"] = st
-    return {"acc_flops": tot_acc, "vertex_flops": tot_vert, "stage_ms": t, "stats": work}
+    return {"acc_flops": tot_acc, "vertex_flops": tot_vert, "vertex_bytes": vbytes, "stage_ms": t, "stats": work}
 
 
 def cpu_sample(cfg_name: str, q_steps: int, budget_s: float):
@@ -652,34 +665,56 @@ def main():
                 "mixed_over_fp64": ms64 / ms, "errors_vs_fp64_gpu": errs}
         ctx = None
 
-    # roofline of the dominant stage (accumulation) from the library's CUDA events
+    # rooflines of the vertex and accumulation stages from the library's CUDA
+    # events; `roofline` is the one with the larger share of the step
     sm = work["stage_ms"]
     acc_s = sm["accumulate"] / 1000.0
+    vtx_s = sm["vertices"] / 1000.0
     achieved_tf = work["acc_flops"] / acc_s / 1e12 if acc_s > 0 else None
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         pass
+    hbm = peaks.get("hbm_gbs")
+    hbm_src = "MEASURED_PEAKS.json hbm_gbs" if hbm else "fallback 6800 GB/s (no MEASURED_PEAKS.json)"
+    hbm = hbm or 6800.0
+    vtx_gbs = work["vertex_bytes"] / vtx_s / 1e9 if vtx_s > 0 else None
+    roof_vtx = {"bound": "hbm", "achieved": vtx_gbs, "peak": hbm, "unit": "GB/s",
+                "frac": (vtx_gbs / hbm) if vtx_gbs else None, "peak_source": hbm_src,
+                "bytes_per_step": work["vertex_bytes"],
+                "byte_count": "sum over vertex passes of 8*Nb*sum_k NGd + 2*NG*sum_k NGd + 8*NG*T "
+                              "(Nb: bands read on both k-points; int16 Gfast map; FP32 rows out)",
+                "vertex_tflops": (work["vertex_flops"] / vtx_s / 1e12) if vtx_s > 0 else None}
     if args.precision == "fp64":
-        roof = {"bound": "fp64", "achieved": achieved_tf, "peak": 1.25, "unit": "TFLOP/s",
-                "frac": (achieved_tf / 1.25) if achieved_tf else None, "traffic": None,
-                "peak_source": "nominal GB300 FP64 rate (no measured FP64 peak in MEASURED_PEAKS.json)",
-                "kernel": "k_accum_fp64 (+ per-chunk calls)",
-                "flops_per_step": work["acc_flops"], "flop_count": "8*NGloc^2*sum_t N_win(t)"}
+        roof_vtx.update({"kernel": "k_vertex_fp64", "traffic": None})
+        roof_acc = {"bound": "fp64", "achieved": achieved_tf, "peak": 1.25, "unit": "TFLOP/s",
+                    "frac": (achieved_tf / 1.25) if achieved_tf else None, "traffic": None,
+                    "peak_source": "nominal GB300 FP64 rate (no measured FP64 peak in MEASURED_PEAKS.json)",
+                    "kernel": "k_accum_fp64 (+ per-chunk calls)",
+                    "flops_per_step": work["acc_flops"], "flop_count": "8*NGloc^2*sum_t N_win(t)"}
     else:
+        roof_vtx.update({"kernel": "k_vertex_mn (Optabs xx, zz: current; Sloss: charge), 3 launches per step",
+                         "traffic": VTX_DRAM_BYTES_PER_K * s.ntot,
+                         "traffic_basis": "DRAM bytes of one current launch, per k-point from an ncu capture "
+                                          "of the 40x40 case, times this workload's FBZ k-points"})
         pk = peaks.get("bf16_tflops_sustained", 1700.0)
         # DRAM bytes of one complex (Optabs) accumulation launch: ncu measured
         # 30.4 GB for 54.6 M (transition, frequency) pairs on the 60x60 case,
         # scaled here by this workload's pairs per launch
         nwin = [work["stats"][p]["sum_nwin"] for p in ("xx", "zz")]
         traffic = ACC_DRAM_BYTES_PER_PAIR * sum(nwin) / len(nwin)
-        roof = {"bound": "tensor", "achieved": achieved_tf, "peak": pk, "unit": "TFLOP/s",
-                "frac": (achieved_tf / pk) if achieved_tf else None, "traffic": traffic,
-                "kernel": "k_accum_ws (Optabs xx, zz: complex S0; Sloss: real S0), 3 launches per step",
-                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (kernel timed inside a long step)",
-                "flops_per_step": work["acc_flops"], "flop_count": "8*NGloc^2*sum_t N_win(t)",
-                "traffic_basis": "GB per complex launch scaled from an ncu capture of the 60x60 case"}
+        roof_acc = {"bound": "tensor", "achieved": achieved_tf, "peak": pk, "unit": "TFLOP/s",
+                    "frac": (achieved_tf / pk) if achieved_tf else None, "traffic": traffic,
+                    "kernel": "k_accum_ws (Optabs xx, zz: complex S0; Sloss: real S0), 3 launches per step",
+                    "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (kernel timed inside a long step)",
+                    "flops_per_step": work["acc_flops"], "flop_count": "8*NGloc^2*sum_t N_win(t)",
+                    "traffic_basis": "GB per complex launch scaled from an ncu capture of the 60x60 case"}
+    roof_vtx["stage_ms_per_step"] = sm["vertices"]
+    roof_acc["stage_ms_per_step"] = sm["accumulate"]
+    roof = dict(roof_vtx if sm["vertices"] >= sm["accumulate"] else roof_acc)
+    roof["stage"] = "vertices" if sm["vertices"] >= sm["accumulate"] else "accumulate"
+    roof_stages = {"vertices": roof_vtx, "accumulate": roof_acc}
 
     cpu = None
     if not args.no_cpu and rank == 0:
@@ -712,11 +747,11 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f16x3->f32 (vertices, S0), f32 (KK), f64 (Dyson)",
                 "data": "synthetic (seeded QE-layout Bloch basis)", "config": cfgd, "clocks": clocks,
-                "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches, "roofline": roof, "roofline_stages": roof_stages,
+                "cpu_baseline": cpu, "e2e": e2e,
                 "stage_ms_per_step": {k: round(v, 3) for k, v in sm.items()},
                 "fp64_gpu": fp64, "serving": serving, "dispersion": disp, "c5": c5, "kmap": kmap,
-                "serving_c4": serving_c4,
-                "vertex_tflops": (work["vertex_flops"] / (sm["vertices"] / 1e3) / 1e12) if sm["vertices"] else None}
+                "serving_c4": serving_c4}
         print(json.dumps(line), flush=True)
     if ctx is not None:
         ctx.close()

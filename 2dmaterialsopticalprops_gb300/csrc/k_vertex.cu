@@ -465,6 +465,7 @@ int vertices_f32(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, lo
   size_t smem = sizeof(float2) * ((size_t)IC * c->nbnd + (size_t)GC * IC * c->nbnd * (two ? 2 : 1)) +
                 sizeof(int) * (size_t)GC * IC + sizeof(float2) * (size_t)GC * IC;
   dim3 grid(nk, (c->nlf + GC - 1) / GC);
+  if (!c->d_coeff32.p) return fail(c, RPA_ESTATE, "FP32 vertices: no FP32 copy of the basis on the device");
   const float2* coeff = c->d_coeff32.as<float2>();
   const Trans* tr = c->d_trans.as<Trans>();
   const long long* off = c->d_offsets.as<long long>();

@@ -482,11 +482,14 @@ struct YbtCtx {
   float sB;
 };
 
+// One thread per (k-point, plane wave, 8-band group): 16-byte loads of the four
+// coefficient planes and 16-byte stores of the four b(i) c planes.
 __global__ void k_vtx_ybt(YbtCtx Y) {
-  const size_t n = (size_t)Y.nk * Y.nsum_max * Y.nbp;
+  const int ng = Y.nbp / 8;
+  const size_t n = (size_t)Y.nk * Y.nsum_max * ng;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-    const int band = (int)(e % Y.nbp);
-    const size_t r = e / Y.nbp;
+    const int g = (int)(e % ng);
+    const size_t r = e / ng;
     const int i = (int)(r % Y.nsum_max), kl = (int)(r / Y.nsum_max);
     const int* km = Y.kmap + 5 * (Y.k0 + kl);
     const int K1 = km[0];
@@ -497,17 +500,32 @@ __global__ void k_vtx_ybt(YbtCtx Y) {
       const double* g1 = Y.G + 3 * Y.gidx[(size_t)K1 * Y.npwx + i];
       b = (float)(Y.Gcar * (R[0] * g1[0] + R[1] * g1[1] + R[2] * g1[2])) * Y.sB * (1.0f / 16384.0f);
     }
-    const __half* c = Y.planes + ((size_t)K1 * Y.npwx + (i < nsum ? i : 0)) * 4 * Y.nbp + band;
-    const float re = (__half2float(c[0]) + __half2float(c[2 * Y.nbp])) * b;
-    const float im = (__half2float(c[Y.nbp]) + __half2float(c[3 * Y.nbp])) * b;
-    const __half2 hh = __floats2half2_rn(re, im);
-    const float2 hf = __half22float2(hh);
-    const __half2 ll = __floats2half2_rn(re - hf.x, im - hf.y);
-    __half* o = Y.ybt + r * 4 * Y.nbp + band;
-    o[0] = __low2half(hh);
-    o[Y.nbp] = __high2half(hh);
-    o[2 * Y.nbp] = __low2half(ll);
-    o[3 * Y.nbp] = __high2half(ll);
+    const __half* c = Y.planes + ((size_t)K1 * Y.npwx + (i < nsum ? i : 0)) * 4 * Y.nbp + 8 * g;
+    uint4 p[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) p[u] = __ldg(reinterpret_cast<const uint4*>(c + u * Y.nbp));
+    uint4 o[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      // bands 2q, 2q + 1 of the group: re = re_hi + re_lo, im = im_hi + im_lo
+      const float2 rh = __half22float2(reinterpret_cast<const __half2*>(&p[0])[q]);
+      const float2 ih = __half22float2(reinterpret_cast<const __half2*>(&p[1])[q]);
+      const float2 rl = __half22float2(reinterpret_cast<const __half2*>(&p[2])[q]);
+      const float2 il = __half22float2(reinterpret_cast<const __half2*>(&p[3])[q]);
+      const float2 re = make_float2((rh.x + rl.x) * b, (rh.y + rl.y) * b);
+      const float2 im = make_float2((ih.x + il.x) * b, (ih.y + il.y) * b);
+      const __half2 reh = __floats2half2_rn(re.x, re.y), imh = __floats2half2_rn(im.x, im.y);
+      const float2 rehf = __half22float2(reh), imhf = __half22float2(imh);
+      const __half2 rel = __floats2half2_rn(re.x - rehf.x, re.y - rehf.y);
+      const __half2 iml = __floats2half2_rn(im.x - imhf.x, im.y - imhf.y);
+      reinterpret_cast<__half2*>(&o[0])[q] = reh;
+      reinterpret_cast<__half2*>(&o[1])[q] = imh;
+      reinterpret_cast<__half2*>(&o[2])[q] = rel;
+      reinterpret_cast<__half2*>(&o[3])[q] = iml;
+    }
+    __half* out = Y.ybt + r * 4 * Y.nbp + 8 * g;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) *reinterpret_cast<uint4*>(out + u * Y.nbp) = o[u];
   }
 }
 
@@ -694,7 +712,7 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
     V.comp = Y.comp = comps[a];
     V.M = a == 0 ? Mf : Mf2;
     V.amax = amax + a;
-    k_vtx_ybt<<<4096, 256, 0, c->stream>>>(Y);
+    k_vtx_ybt<<<2 * 152 * 8, 256, 0, c->stream>>>(Y);
     RPA_CUDA(c, cudaGetLastError());
     ++c->launches;
     RPA_TRY(launch_windows_mn<true>(c, V, nk, x0, x1, y0, y1, ymax_cur));

@@ -99,6 +99,16 @@ __global__ void k_basis_transpose(const double2* __restrict__ src, double2* __re
   }
 }
 
+void launch_basis_transpose(const double2* src, double2* dst, int nkc, int nbnd, int npwx, cudaStream_t s) {
+  k_basis_transpose<<<2048, 256, 0, s>>>(src, dst, nkc, nbnd, npwx);
+}
+
+// gidx[k][i] = igk(i, k) - 1 (0-based G index), or i for the legacy basis
+__global__ void k_gidx(int* __restrict__ gidx, const int* __restrict__ igk, size_t n, int npwx) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    gidx[e] = igk ? igk[e] - 1 : (int)(e % npwx);
+}
+
 __global__ void k_to_f32(const double2* __restrict__ src, float2* __restrict__ dst, size_t n) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     double2 v = src[e];
@@ -381,6 +391,7 @@ int rpa_destroy(rpa_ctx* c) {
                     &c->d_ntrans, &c->d_S, &c->d_Sdf, &c->d_Q, &c->d_chi0, &c->d_kk[0], &c->d_kk[1], &c->d_kkf[0], &c->d_kkf[1], &c->d_kkw, &c->d_V, &c->d_eps, &c->d_WT,
                     &c->d_flags, &c->d_tmp};
   for (DevBuf* b : bufs) release(*b);
+  host_io_release(c);
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
   cudaStreamDestroy(c->stream);
@@ -475,10 +486,12 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
   RPA_CUDA(c, cudaMemcpyAsync(c->d_npw.p, npw, sizeof(int) * nks, cudaMemcpyHostToDevice, c->stream));
   RPA_CUDA(c, cudaMemcpyAsync(c->d_E.p, c->h_E.data(), sizeof(double) * (size_t)nks * nbnd, cudaMemcpyHostToDevice,
                               c->stream));
-  std::vector<int> gidx((size_t)nks * npwx);
-  for (int k = 0; k < nks; ++k)
-    for (int i = 0; i < npwx; ++i) gidx[(size_t)k * npwx + i] = igk ? igk[(size_t)k * npwx + i] - 1 : i;
-  RPA_CUDA(c, cudaMemcpyAsync(c->d_gidx.p, gidx.data(), sizeof(int) * gidx.size(), cudaMemcpyHostToDevice, c->stream));
+  if (igk)
+    RPA_CUDA(c, cudaMemcpyAsync(c->d_gidx.p, igk, sizeof(int) * (size_t)nks * npwx, cudaMemcpyHostToDevice, c->stream));
+  k_gidx<<<1024, 256, 0, c->stream>>>(c->d_gidx.as<int>(), igk ? c->d_gidx.as<int>() : nullptr, (size_t)nks * npwx,
+                                      npwx);
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
   if (!c->legacy) {
     RPA_TRY(ensure(c, c->d_inv, sizeof(int) * (size_t)nks * c->ng));
     RPA_TRY(ensure(c, c->d_flags, sizeof(int) * 4));
@@ -494,25 +507,21 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
     if (bad == 1) return fail(c, RPA_EINVAL, "igk entry outside 1..NG");
     if (bad == 2) return fail(c, RPA_EINVAL, "igk repeats a G vector within one k-point");
   }
-  // coefficients: stage raw Fortran blocks and transpose to [k][i][b]
+  // coefficients: raw Fortran blocks, transposed to [k][i][b] on the device
   const size_t per_k = (size_t)nbnd * npwx;
   RPA_TRY(ensure(c, c->d_coeff, sizeof(double2) * per_k * nks));
-  int kc = (int)std::max<size_t>(1, std::min<size_t>(nks, ((size_t)512 << 20) / (sizeof(double2) * per_k)));
-  RPA_TRY(ensure(c, c->d_tmp, sizeof(double2) * per_k * kc));
-  for (int k0 = 0; k0 < nks; k0 += kc) {
-    int nk = std::min(kc, nks - k0);
-    RPA_CUDA(c, cudaMemcpyAsync(c->d_tmp.p, coeff + 2 * per_k * k0, sizeof(double2) * per_k * nk,
-                                cudaMemcpyHostToDevice, c->stream));
-    k_basis_transpose<<<2048, 256, 0, c->stream>>>(c->d_tmp.as<double2>(), c->d_coeff.as<double2>() + per_k * k0, nk,
-                                                   nbnd, npwx);
-    RPA_CUDA(c, cudaGetLastError());
-  ++c->launches;
-  }
+  RPA_TRY(upload_basis(c, coeff, nks, nbnd, npwx, c->d_coeff.as<double2>()));
   if (c->precision == RPA_PREC_MIXED) {
-    RPA_TRY(ensure(c, c->d_coeff32, sizeof(float2) * per_k * nks));
-    k_to_f32<<<2048, 256, 0, c->stream>>>(c->d_coeff.as<double2>(), c->d_coeff32.as<float2>(), per_k * nks);
-    RPA_CUDA(c, cudaGetLastError());
-    ++c->launches;
+    // the FP32 copy feeds the CUDA-core vertex kernel only: chosen explicitly, or
+    // where the fp16 planes do not apply (int16 maps, band windows)
+    if (c->vertex_kind != 0 || npwx > 32767 || nbnd > 181) {
+      RPA_TRY(ensure(c, c->d_coeff32, sizeof(float2) * per_k * nks));
+      k_to_f32<<<2048, 256, 0, c->stream>>>(c->d_coeff.as<double2>(), c->d_coeff32.as<float2>(), per_k * nks);
+      RPA_CUDA(c, cudaGetLastError());
+      ++c->launches;
+    } else {
+      release(c->d_coeff32);
+    }
     c->nbp = (nbnd + 7) / 8 * 8;
     RPA_TRY(ensure(c, c->d_cpl, sizeof(__half) * (size_t)nks * npwx * 4 * c->nbp));
     k_to_planes16<<<2048, 256, 0, c->stream>>>(c->d_coeff.as<double2>(), c->d_cpl.as<__half>(), (size_t)nks * npwx,
@@ -804,7 +813,7 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
       launch_transpose_wp_to_fortran(c->d_S.as<double>(), c->d_tmp.as<double>(), P.nw, np, cplx ? 2 : 1, c->stream);
       RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
-      RPA_CUDA(c, cudaMemcpyAsync(S0_out, c->d_tmp.p, s_bytes, cudaMemcpyDeviceToHost, c->stream));
+      RPA_TRY(copy_d2h(c, S0_out, c->d_tmp.p, s_bytes));
     }
     if (Qeff_out && cplx)
       RPA_CUDA(c, cudaMemcpyAsync(Qeff_out, c->d_Q.p, sizeof(double2) * np, cudaMemcpyDeviceToHost, c->stream));
@@ -838,8 +847,7 @@ int rpa_kk(rpa_ctx* c, int variant, double* chi0_out) {
     launch_transpose_wp_to_fortran(c->d_chi0.as<double>(), c->d_tmp.as<double>(), nwo, np, 2, c->stream);
     RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
-    RPA_CUDA(c, cudaMemcpyAsync(chi0_out, c->d_tmp.p, sizeof(double2) * (size_t)nwo * np, cudaMemcpyDeviceToHost,
-                                c->stream));
+    RPA_TRY(copy_d2h(c, chi0_out, c->d_tmp.p, sizeof(double2) * (size_t)nwo * np));
     cudaEventRecord(c->ev[7], c->stream);
     RPA_CUDA(c, cudaStreamSynchronize(c->stream));
     c->stage_ms[5] = elapsed(c, 6, 7);
@@ -880,16 +888,13 @@ int rpa_dyson(rpa_ctx* c, double c0, double eps, double* WT_out, double* epsinv_
       launch_transpose_wp_to_fortran(c->d_WT.as<double>(), c->d_tmp.as<double>(), nwo, np, 2, c->stream);
       RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
-      RPA_CUDA(c, cudaMemcpyAsync(WT_out, c->d_tmp.p, sizeof(double2) * (size_t)nwo * np, cudaMemcpyDeviceToHost,
-                                  c->stream));
-      RPA_CUDA(c, cudaStreamSynchronize(c->stream));
+      RPA_TRY(copy_d2h(c, WT_out, c->d_tmp.p, sizeof(double2) * (size_t)nwo * np));
     }
     if (epsinv_out) {
       launch_transpose_wp_to_fortran(c->d_eps.as<double>(), c->d_tmp.as<double>(), nwo, np, 2, c->stream);
       RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
-      RPA_CUDA(c, cudaMemcpyAsync(epsinv_out, c->d_tmp.p, sizeof(double2) * (size_t)nwo * np,
-                                  cudaMemcpyDeviceToHost, c->stream));
+      RPA_TRY(copy_d2h(c, epsinv_out, c->d_tmp.p, sizeof(double2) * (size_t)nwo * np));
     }
   }
   cudaEventRecord(c->ev[7], c->stream);

@@ -38,6 +38,19 @@ static constexpr int KEY_INTRA = 0x7fffffff;
 
 }  // namespace rpa
 
+namespace rpa {
+struct CopyPool;
+}
+
+// page-locked staging ring, copy threads and copy stream of a context's large
+// host transfers (created on first use)
+struct RpaHostIo {
+  void* ring[2] = {nullptr, nullptr};
+  cudaEvent_t ev[4] = {};
+  cudaStream_t copy_stream = nullptr;
+  rpa::CopyPool* pool = nullptr;
+};
+
 struct rpa_ctx {
   int device = 0;
   int precision = RPA_PREC_FP64;
@@ -122,6 +135,7 @@ struct rpa_ctx {
   long long launches = 0;  // kernels launched by this context
   double stats[4] = {0, 0, 0, 0};
   cudaEvent_t ev[8] = {};
+  RpaHostIo io;
 };
 
 namespace rpa {
@@ -160,6 +174,14 @@ inline long long vtx_tune_key(int mode, int nbnd, int nocc, int nlf) {
 }
 int kk_apply_real_fp64(rpa_ctx* c, DevBuf& buf, const std::vector<double>& K, int nrow, int nw, const double* S,
                        double2* out, int np, bool pi_epilogue);
+
+// large host transfers (host_io.cu): synchronous device -> host copy through
+// the page-locked ring when dst is pageable; basis upload overlapping copies
+// and transposes; release of the ring, threads and copy stream
+int copy_d2h(rpa_ctx* c, void* dst, const void* src, size_t bytes);
+int upload_basis(rpa_ctx* c, const double* coeff, int nks, int nbnd, int npwx, double2* dst);
+void host_io_release(rpa_ctx* c);
+void launch_basis_transpose(const double2* src, double2* dst, int nkc, int nbnd, int npwx, cudaStream_t s);
 
 // device layout transposes between [w][p] (library) and (w fastest) Fortran
 void launch_transpose_wp_to_fortran(const double* src, double* dst, int nw, int np, int ncomp,

@@ -355,8 +355,15 @@ class Context:
         self.mode = mode
         return S0, Q
 
-    def kk(self, variant: int, want: bool = True):
-        out = np.zeros((self.nlf, self.nlf, self.no - 1), dtype=np.complex128) if want else None
+    def kk(self, variant: int, want: bool = True, out: np.ndarray | None = None):
+        """chi0 after the KK transform, (nlf, nlf, no-1) complex; `out` may be a
+        caller-owned array of that shape (e.g. page-locked memory)."""
+        shape = (self.nlf, self.nlf, self.no - 1)
+        if out is not None:
+            if out.shape != shape or out.dtype != np.complex128 or not out.flags.c_contiguous:
+                raise ValueError("kk: out must be a contiguous complex128 array of shape %s" % (shape,))
+        elif want:
+            out = np.zeros(shape, dtype=np.complex128)
         self._chk(self.L.rpa_kk(self.h, variant, _p(out)))
         return out
 

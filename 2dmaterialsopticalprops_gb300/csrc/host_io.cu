@@ -107,6 +107,8 @@ static int ensure_ring(rpa_ctx* c) {
   return RPA_OK;
 }
 
+int host_io_prepare(rpa_ctx* c) { return ensure_ring(c); }
+
 void host_io_release(rpa_ctx* c) {
   delete c->io.pool;
   c->io.pool = nullptr;

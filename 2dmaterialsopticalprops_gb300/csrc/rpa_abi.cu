@@ -368,6 +368,13 @@ int rpa_create_shared(rpa_ctx** out, rpa_ctx* parent, int precision) {
   for (auto& ev : c->ev) cudaEventCreate(&ev);
   c->parent = parent;
   ++parent->children;
+  // shared contexts serve requests concurrently: their page-locked staging
+  // ring is made now rather than inside the first request
+  const int rc = host_io_prepare(c);
+  if (rc != RPA_OK) {
+    rpa_destroy(c);
+    return rc;
+  }
   *out = c;
   return RPA_OK;
 }

@@ -180,6 +180,7 @@ int kk_apply_real_fp64(rpa_ctx* c, DevBuf& buf, const std::vector<double>& K, in
 // and transposes; release of the ring, threads and copy stream
 int copy_d2h(rpa_ctx* c, void* dst, const void* src, size_t bytes);
 int upload_basis(rpa_ctx* c, const double* coeff, int nks, int nbnd, int npwx, double2* dst);
+int host_io_prepare(rpa_ctx* c);
 void host_io_release(rpa_ctx* c);
 void launch_basis_transpose(const double2* src, double2* dst, int nkc, int nbnd, int npwx, cudaStream_t s);
 

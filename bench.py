@@ -266,8 +266,10 @@ def serving_run(n_req: int = 32, rate: float = 200.0, nslots: int = 4, mem_gb: f
 
     reqs = [make(i) for i in range(n_req + 4)]
     srv = rpa.Server(parent, nslots=nslots, mem_bytes=mem_gb * 1e9)
-    for r, _ in reqs[:4]:  # warm-up: device buffers of the slots reach their sizes
-        srv.wait(srv.submit(**r))
+    # warm-up: one request per slot at once, so that every slot's device
+    # buffers reach their sizes before the timed stream
+    for i in [srv.submit(**r) for r, _ in reqs[:4]]:
+        srv.wait(i)
     reqs = reqs[4:]
     gaps = rng.exponential(1.0 / rate, size=n_req)
     ids = [None] * n_req

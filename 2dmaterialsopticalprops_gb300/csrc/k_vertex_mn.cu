@@ -23,19 +23,18 @@
 // tile holds two column blocks, [y | y'] with y' = (-Im y rows 0-31, Re y rows
 // 32-63), so one MMA of N = 2 NYN per K step gives
 //     Re D = X . y  and  Im D = X . y' = X[Re] . (-Im y) + X[Im] . Re y
-// The threads that copy a y chunk write its y' image.  Per K step two MMAs:
-// Xh . [Yh | Yl] (both halves side by side, N up to 256) into [hi hi | cross]
-// columns, then Xl . Yh added to the cross columns; the two column blocks are
-// summed in FP32 at read-back.  (The tensor core reads its operands from
-// shared memory at 128 bytes per cycle: an N = 128 MMA just keeps up, an N = 256
-// one leaves a quarter of the bandwidth to the gathers.)  The current factor separates,
+// The threads that copy a y chunk write its y' image.  Per K step three MMAs
+// of N = 2 NYN into one accumulator, small products first: Xl . Yh, Xh . Yl,
+// Xh . Yh.  (The tensor core reads its operands from shared memory at 128
+// bytes per cycle: an N = 128 MMA just keeps up.)  The current factor separates,
 // f(G,i) = a(G) + b(i): the b(i) c block (precomputed per launch, split like the
 // coefficient planes) is a second column block of y, and a(G) multiplies the c
 // block at read-back: M = a(G) D[c] + D[b c].  Each local-field tile sweeps the plane waves in the
 // opposite direction of the previous one, so the coefficient rows read last
 // are read again first while they are still in L2.
-// Each chunk goes into a fresh TMEM accumulator (two, ping-pong) that the
-// worker warps add to FP32 registers.
+// Each chunk goes into a fresh TMEM accumulator that the worker warps add to
+// FP32 registers; a ring of four accumulators keeps the MMA warp from waiting
+// for the read-back of the chunk before last.
 // Warp roles: 16 worker warps gather chunk t + S - 1 into the ring of S
 // shared-memory stages and read back chunk t - 1 from TMEM; warp 16 issues
 // the MMAs.  Every wait is bounded and ends in an error status.
@@ -96,9 +95,9 @@ struct VmCfg {
   static constexpr uint32_t PTAB = 32 * NBY * 2;         // int16 [32][NBY]
   static constexpr int S0 = (int)((VM_SMEM_MAX - 1024 - (int)PTAB) / (int)STAGE);
   static constexpr int S = S0 > VM_SMAX ? VM_SMAX : S0;
-  static constexpr uint32_t N2 = 64 * NTA;                // columns of one block (y and y', padded)
-  static constexpr uint32_t BUFC = 2 * N2;               // hi hi block + cross block
-  static constexpr uint32_t NCOL = 2 * BUFC <= 256 ? 256 : 512;
+  static constexpr uint32_t N2 = 64 * NTA;                // accumulator columns (y and y', padded)
+  static constexpr int NBUF = 4;                         // TMEM accumulators in the ring
+  static constexpr uint32_t NCOL = NBUF * N2 <= 256 ? 256 : 512;
   static constexpr int CW = NBY / 4;                     // columns per thread per block
   static constexpr size_t SMEM = (size_t)S * STAGE + PTAB + 1024;
   static_assert(NBY % 16 == 0 && NTA <= 2, "window too wide");
@@ -157,7 +156,7 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
   const uint32_t sbase = tc::smem_u32(base);
   int16_t* ptab = reinterpret_cast<int16_t*>(base + (size_t)S * STAGE);  // [a][b]: local transition, -1 none
-  __shared__ uint64_t full[VM_SMAX], done[2], tfree[2];
+  __shared__ uint64_t full[VM_SMAX], done[Cfg::NBUF], tfree[Cfg::NBUF];
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
 
@@ -180,7 +179,7 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
   }
   if (tid == 0) {
     for (int s = 0; s < S; ++s) tc::mbar_init(&full[s], VM_WORKERS / 32);
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < Cfg::NBUF; ++b) {
       tc::mbar_init(&done[b], 1);
       tc::mbar_init(&tfree[b], VM_WORKERS / 32);
     }
@@ -205,7 +204,8 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
     // ---------------------------------------------------------------- MMA warp
     if (lane == 0) {
       constexpr uint32_t N2 = Cfg::N2;
-      const uint32_t id1 = tc::idesc_f16_mn(128, 2 * N2, false), id2 = tc::idesc_f16_mn(128, N2, false);
+      constexpr int NB = Cfg::NBUF;
+      const uint32_t id = tc::idesc_f16_mn(128, N2, false);
       // descriptors of stage 0; a chunk adds its byte offsets / 16 to the start-address field
       const uint64_t dx0 = tc::desc_sw128_mn(sbase, 1024u, 2048u);
       const uint64_t dy0 = tc::desc_sw128_mn(sbase + 2 * XH, 1024u, YKG);
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
       for (int t = 0; t < total; ++t) {
         if (abort_flag) break;
         if (!tc::mbar_wait(&full[s], (uint32_t)ph, VM_SPINS) ||
-            (t >= 2 && !tc::mbar_wait(&tfree[t & 1], (uint32_t)(((t - 2) >> 1) & 1), VM_SPINS))) {
+            (t >= NB && !tc::mbar_wait(&tfree[t % NB], (uint32_t)((t / NB - 1) & 1), VM_SPINS))) {
           atomicExch(V.status, 1);
           abort_flag = 1;
           break;
@@ -222,19 +222,20 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
         tc::tc_fence_after();
         const uint64_t so = (uint64_t)(((uint32_t)s * STAGE) >> 4);
         const uint64_t dx = dx0 + so, dy = dy0 + so;
-        const uint32_t d = taddr + (uint32_t)((t & 1) * Cfg::BUFC);
+        const uint32_t d = taddr + (uint32_t)((t % NB) * N2);
 #pragma unroll
         for (int ks = 0; ks < 4; ++ks) {
           const uint64_t xh = dx + (uint64_t)(ks * 256), xl = xh + (XH >> 4);
-          const uint64_t y = dy + (uint64_t)(ks * 2 * (YKG >> 4));
-          tc::mma_bf16(d, xh, y, id1, ks > 0 ? 1u : 0u);  // Xh . [Yh | Yl]
-          tc::mma_bf16(d + N2, xl, y, id2, 1u);            // + Xl . Yh into the cross block
+          const uint64_t yh = dy + (uint64_t)(ks * 2 * (YKG >> 4)), yl = yh + (YLO >> 4);
+          tc::mma_bf16(d, xl, yh, id, ks > 0 ? 1u : 0u);  // Xl . Yh
+          tc::mma_bf16(d, xh, yl, id, 1u);                // + Xh . Yl
+          tc::mma_bf16(d, xh, yh, id, 1u);                // + Xh . Yh
         }
-        tc::mma_commit(&done[t & 1]);
+        tc::mma_commit(&done[t % NB]);
         last = t;
         if (++s == S) s = 0, ph ^= 1;
       }
-      if (last >= 0) tc::mbar_wait(&done[last & 1], (uint32_t)((last >> 1) & 1), VM_SPINS);
+      if (last >= 0) tc::mbar_wait(&done[last % NB], (uint32_t)((last / NB) & 1), VM_SPINS);
     }
   } else {
     // ------------------------------------------------------------- worker warps
@@ -345,39 +346,34 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
       }
     };
     auto consume = [&](int t) -> bool {
-      if (!tc::mbar_wait(&done[t & 1], (uint32_t)((t >> 1) & 1), VM_SPINS)) {
+      constexpr int NB = Cfg::NBUF;
+      if (!tc::mbar_wait(&done[t % NB], (uint32_t)((t / NB) & 1), VM_SPINS)) {
         atomicExch(V.status, 1);
         abort_flag = 1;
         return false;
       }
       tc::tc_fence_after();
-      const uint32_t ad = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)((t & 1) * Cfg::BUFC + cg * CW);
-      constexpr uint32_t HH = Cfg::N2;  // the cross block
+      const uint32_t ad = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)((t % NB) * Cfg::N2 + cg * CW);
+      float v[2][CW], w[2][CW];
 #pragma unroll
       for (int part = 0; part < 2; ++part) {
-        float* acc = part ? accI : accR;
-        const uint32_t a = ad + part * NYN;
-        float v[CW], vh[CW];
-        tmem_ld_n<CW>(a, v);
-        tmem_ld_n<CW>(a + HH, vh);
-        tc::tmem_ld_wait();
-        if constexpr (CURRENT) {
-#pragma unroll
-          for (int j = 0; j < CW; ++j) v[j] = fa * (v[j] + vh[j]);
-          tmem_ld_n<CW>(a + NBY, vh);
-          float wh[CW];
-          tmem_ld_n<CW>(a + HH + NBY, wh);
-          tc::tmem_ld_wait();
-#pragma unroll
-          for (int j = 0; j < CW; ++j) acc[j] += v[j] + (vh[j] + wh[j]);
-        } else {
-#pragma unroll
-          for (int j = 0; j < CW; ++j) acc[j] += v[j] + vh[j];
-        }
+        tmem_ld_n<CW>(ad + part * NYN, v[part]);
+        if constexpr (CURRENT) tmem_ld_n<CW>(ad + part * NYN + NBY, w[part]);
       }
+      tc::tmem_ld_wait();
       tc::tc_fence_before();
       __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&tfree[t & 1]);
+      if (lane == 0) tc::mbar_arrive(&tfree[t % NB]);
+#pragma unroll
+      for (int j = 0; j < CW; ++j) {
+        if constexpr (CURRENT) {
+          accR[j] += fa * v[0][j] + w[0][j];
+          accI[j] += fa * v[1][j] + w[1][j];
+        } else {
+          accR[j] += v[0][j];
+          accI[j] += v[1][j];
+        }
+      }
       return true;
     };
     float amx = 0.f;

@@ -92,7 +92,7 @@ struct VmCfg {
   static constexpr uint32_t YKG = (uint32_t)NTA * 2048;  // Y bytes per group of 8 K rows: hi atoms, then lo atoms
   static constexpr uint32_t YLO = (uint32_t)NTA * 1024;  // offset of the lo atoms in a K group
   static constexpr uint32_t STAGE = 2 * XH + 8 * YKG;
-  static constexpr uint32_t PTAB = 32 * NBY * 2;         // int16 [32][NBY]
+  static constexpr uint32_t PTAB = 32 * NBY * 4;         // int32 [32][NBY]
   static constexpr int S0 = (int)((VM_SMEM_MAX - 1024 - (int)PTAB) / (int)STAGE);
   static constexpr int S = S0 > VM_SMAX ? VM_SMAX : S0;
   static constexpr uint32_t N2 = 64 * NTA;                // accumulator columns (y and y', padded)
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
   extern __shared__ unsigned char smraw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
   const uint32_t sbase = tc::smem_u32(base);
-  int16_t* ptab = reinterpret_cast<int16_t*>(base + (size_t)S * STAGE);  // [a][b]: local transition, -1 none
+  int* ptab = reinterpret_cast<int*>(base + (size_t)S * STAGE);  // [a][b]: vertex row of the pair, -1 none
   __shared__ uint64_t full[VM_SMAX], done[Cfg::NBUF], tfree[Cfg::NBUF];
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
     const int n = nm & 0xffff, m = nm >> 16;
     const int xa = V.swap ? n : m, yb = V.swap ? m : n;
     if (xa >= V.xo0 && xa < V.xo1 && yb >= V.yo0 && yb < V.yo1)
-      ptab[(xa - V.xs) * NBY + (yb - V.ys)] = (int16_t)(t - t0);
+      ptab[(xa - V.xs) * NBY + (yb - V.ys)] = V.pos_of[t];
   }
   tc::tc_fence_before();
   __syncthreads();
@@ -383,9 +383,8 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
       if (eg < GPT && G < V.nlf) {
 #pragma unroll
         for (int j = 0; j < CW; ++j) {
-          const int lt = ptab[ea * NBY + cg * CW + j];
-          if (lt >= 0) {
-            const int r = V.pos_of[t0 + lt];
+          const int r = ptab[ea * NBY + cg * CW + j];
+          if (r >= 0) {
             const float re = accR[j] * V.out_scale, im = accI[j] * isign;
             V.M[(size_t)r * V.nlf + G] = make_float2(re, im);
             amx = fmaxf(amx, fmaxf(fabsf(re), fabsf(im)));

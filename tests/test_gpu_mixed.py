@@ -135,6 +135,23 @@ def test_vertex_kernels_agree(synth, rpa, orc, kind):
     alt.close()
 
 
+@pytest.mark.parametrize("nbnd,nocc,nlf", [(30, 8, 11), (40, 12, 8)])
+def test_current_vertices_32_band_windows(synth, rpa, orc, nbnd, nocc, nlf):
+    """Current vertices in 32-band windows (one window, and two windows on
+    each side), odd NGloc, plane-wave counts that are not a multiple of the
+    32-plane-wave chunk: S0 and Qeff of xx, zz and the yz pair against the
+    oracle."""
+    s = synth.build(synth.config_small(nbnd=nbnd, nocc=nocc, npw=150, nlf=nlf, no=31))
+    ctx = rpa.Context(precision=rpa.PREC_MIXED)
+    ctx.load_system(s)
+    for pol in ("xx", "zz", "yz"):
+        So, Qo = orc.optabs_s0(orc.Bound(s, pol=pol))
+        a, qa = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, pol))
+        assert rel(a, So) < TOL
+        assert rel(qa, Qo) < TOL
+    ctx.close()
+
+
 def test_autotune_and_every_vertex_configuration(synth, rpa, orc):
     """rpa_autotune keeps one configuration per shape; every configuration it can
     choose (band-window width, gathered side) gives S0 within the mixed-path

@@ -838,7 +838,7 @@ static int launch_tc(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char*
   constexpr size_t STAGE = (size_t)NTB * TC_TILE + (size_t)NIO * 2 * TC_GA * 128;
   const size_t smem = 2 * STAGE + 1024 + (STAGE_M ? 2 * (size_t)TC_TT * A.nlf * sizeof(float2) : 0);
   auto kern = k_accum_tc<NIO, CPLX, F16, STAGE_M>;
-  RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
   dim3 grid((nw + NIO - 1) / NIO, (A.nlf + TC_GA - 1) / TC_GA, (A.nlf + TC_GB - 1) / TC_GB);
   kern<<<grid, 256, smem, c->stream>>>(A, tiles);
   RPA_CUDA(c, cudaGetLastError());
@@ -850,7 +850,7 @@ template <int NIO, bool CPLX, bool SEPA>
 static int launch_ws(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char* tiles, const unsigned char* tilesA) {
   using Cfg = WsCfg<NIO, CPLX, SEPA>;
   auto kern = k_accum_ws<NIO, CPLX, SEPA>;
-  RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM));
+  RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
   dim3 grid((nw + NIO - 1) / NIO, A.nht, A.nht);
   kern<<<grid, WS_THREADS, Cfg::SMEM, c->stream>>>(A, tiles, tilesA);
   RPA_CUDA(c, cudaGetLastError());

@@ -236,7 +236,7 @@ int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singul
   D.n = n;
   D.nwo = nwo;
   size_t smem = ((3 * (size_t)n * sizeof(int) + 15) & ~(size_t)15) + sizeof(double2) * n;
-  RPA_CUDA(c, cudaFuncSetAttribute(k_dyson_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  RPA_CUDA(c, allow_dynamic_smem(k_dyson_fp64, c->device));
   k_dyson_fp64<<<grid, 256, smem, c->stream>>>(D);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;

@@ -423,15 +423,15 @@ int vertices_fp64(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, l
   const long long* off = c->d_offsets.as<long long>();
   if (!current) {
     auto kern = k_vertex_fp64<IC, MAXO, false, false>;
-    RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
     kern<<<grid, 256, smem, c->stream>>>(C, coeff, tr, off, k0, GC, c->nbnd, ca, cb, M, M2);
   } else if (!two) {
     auto kern = k_vertex_fp64<IC, MAXO, true, false>;
-    RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
     kern<<<grid, 256, smem, c->stream>>>(C, coeff, tr, off, k0, GC, c->nbnd, ca, cb, M, M2);
   } else {
     auto kern = k_vertex_fp64<IC, MAXO, true, true>;
-    RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
     kern<<<grid, 256, smem, c->stream>>>(C, coeff, tr, off, k0, GC, c->nbnd, ca, cb, M, M2);
   }
   RPA_CUDA(c, cudaGetLastError());
@@ -471,15 +471,15 @@ int vertices_f32(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, lo
   const long long* off = c->d_offsets.as<long long>();
   if (!current) {
     auto kern = k_vertex_f32<IC, MAXO, false, false>;
-    RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
     kern<<<grid, 256, smem, c->stream>>>(C, coeff, tr, off, pos_of, k0, GC, c->nbnd, ca, cb, Mf, Mf, amax);
   } else if (!two) {
     auto kern = k_vertex_f32<IC, MAXO, true, false>;
-    RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
     kern<<<grid, 256, smem, c->stream>>>(C, coeff, tr, off, pos_of, k0, GC, c->nbnd, ca, cb, Mf, Mf, amax);
   } else {
     auto kern = k_vertex_f32<IC, MAXO, true, true>;
-    RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
     kern<<<grid, 256, smem, c->stream>>>(C, coeff, tr, off, pos_of, k0, GC, c->nbnd, ca, cb, Mf, Mf2, amax);
   }
   RPA_CUDA(c, cudaGetLastError());

@@ -528,7 +528,7 @@ template <int NBY, bool CURRENT>
 static int launch_vmn(rpa_ctx* c, const VtxMnCtx& V, int nk) {
   using Cfg = VmCfg<NBY, CURRENT>;
   auto kern = k_vertex_mn<NBY, CURRENT>;
-  RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM));
+  RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
   kern<<<nk, VM_THREADS, Cfg::SMEM, c->stream>>>(V);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;

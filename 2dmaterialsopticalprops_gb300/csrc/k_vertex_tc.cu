@@ -427,7 +427,7 @@ template <int NB, bool CURRENT>
 static int launch_vtc(rpa_ctx* c, const VtxTcCtx& V, int nk) {
   using Cfg = VtCfg<NB, CURRENT>;
   auto kern = k_vertex_tc<NB, CURRENT>;
-  RPA_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM));
+  RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
   kern<<<nk, VT_THREADS, Cfg::SMEM, c->stream>>>(V);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;

@@ -151,6 +151,22 @@ void release(DevBuf& b);
     if (e_ != cudaSuccess) return rpa::cuda_fail(ctx, e_, #call); \
   } while (0)
 
+// Raises a kernel's dynamic shared-memory limit to the most the device allows
+// next to the kernel's static shared memory.  Every caller sets the same value,
+// so contexts that launch the kernel from several host threads (with sizes
+// that depend on their own request) never lower the limit under another's
+// launch.
+template <class K>
+inline cudaError_t allow_dynamic_smem(K kern, int device) {
+  int optin = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, kern);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+}
+
 #define RPA_TRY(...)                 \
   do {                               \
     int rc_ = (__VA_ARGS__);         \

@@ -11,7 +11,11 @@
 // one in (row, column) scan order wins (`>= big`).  A repeated pivot column
 // is reported as singular (gjel's stop); a zero pivot is counted (gjel prints
 // and carries on).  Each block works on its frequency's matrices in a
-// per-block global scratch (L1/L2 resident); the stage is FP64-pipe bound.
+// per-block global scratch (L1/L2 resident); the stage is FP64-pipe bound,
+// and the pivot search (n^2 candidates per step) is most of it: the FP64 path
+// ranks candidates by hypot, as gjel's ABS does; the mixed path (MAG2) by
+// |a|^2, the same order up to ties that hypot's rounding makes, at a tenth of
+// the cost.
 
 #include "rpa_internal.cuh"
 
@@ -43,6 +47,7 @@ struct DysonArgs {
   int n, nwo;
 };
 
+template <bool MAG2>
 __global__ void __launch_bounds__(256) k_dyson_fp64(DysonArgs D) {
   extern __shared__ unsigned char smraw[];
   const int n = D.n, nn = n * n;
@@ -88,7 +93,7 @@ __global__ void __launch_bounds__(256) k_dyson_fp64(DysonArgs D) {
           int pk = ipiv[k];
           if (pk == 0) {
             double2 a = E[j + (size_t)n * k];
-            double v = hypot(a.x, a.y);
+            const double v = MAG2 ? a.x * a.x + a.y * a.y : hypot(a.x, a.y);
             if (v > bv || (v == bv && e > be)) {
               bv = v;
               be = e;
@@ -236,8 +241,13 @@ int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singul
   D.n = n;
   D.nwo = nwo;
   size_t smem = ((3 * (size_t)n * sizeof(int) + 15) & ~(size_t)15) + sizeof(double2) * n;
-  RPA_CUDA(c, allow_dynamic_smem(k_dyson_fp64, c->device));
-  k_dyson_fp64<<<grid, 256, smem, c->stream>>>(D);
+  if (c->precision == RPA_PREC_MIXED) {
+    RPA_CUDA(c, allow_dynamic_smem(k_dyson_fp64<true>, c->device));
+    k_dyson_fp64<true><<<grid, 256, smem, c->stream>>>(D);
+  } else {
+    RPA_CUDA(c, allow_dynamic_smem(k_dyson_fp64<false>, c->device));
+    k_dyson_fp64<false><<<grid, 256, smem, c->stream>>>(D);
+  }
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
   int fl[4];
@@ -317,7 +327,7 @@ extern "C" int rpa_dyson_noalloc(const double* chi0, const double* V, int n, int
   D.nwo = nwo;
   const size_t smem = ((3 * (size_t)n * sizeof(int) + 15) & ~(size_t)15) + sizeof(double2) * n;
   k_noalloc_clear_flags<<<1, 32, 0, s>>>();
-  k_dyson_fp64<<<grid, 256, smem, s>>>(D);
+  k_dyson_fp64<false><<<grid, 256, smem, s>>>(D);
   if (cudaGetLastError() != cudaSuccess) return RPA_ECUDA;
   if (n_singular) {
     int fl[2] = {0, 0};

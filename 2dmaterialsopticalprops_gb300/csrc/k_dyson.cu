@@ -15,7 +15,8 @@
 // and the pivot search (n^2 candidates per step) is most of it: the FP64 path
 // ranks candidates by hypot, as gjel's ABS does; the mixed path (MAG2) by
 // |a|^2, the same order up to ties that hypot's rounding makes, at a tenth of
-// the cost.
+// the cost.  The mixed path also forms W as V eps^-1, which equals the
+// reference's V + V chi V (see below) with a quarter of its FP64 products.
 
 #include "rpa_internal.cuh"
 
@@ -174,44 +175,62 @@ __global__ void __launch_bounds__(256) k_dyson_fp64(DysonArgs D) {
       }
       __syncthreads();
     }
-    // chi = eps^-1 chi0
-    for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-      int i = e % n, j = e / n;
-      double re = 0.0, im = 0.0;
-      for (int k = 0; k < n; ++k) {
-        double2 a = E[i + (size_t)n * k], b = A[k + (size_t)n * j];
-        re += a.x * b.x - a.y * b.y;
-        im += a.x * b.y + a.y * b.x;
-      }
-      Cx[e] = make_double2(re, im);
-    }
-    __syncthreads();
-    // T = chi V
-    for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-      int i = e % n, j = e / n;
-      double re = 0.0, im = 0.0;
-      for (int k = 0; k < n; ++k) {
-        double2 a = Cx[i + (size_t)n * k];
-        double v = D.V[k + (size_t)n * j];
-        re += a.x * v;
-        im += a.y * v;
-      }
-      T[e] = make_double2(re, im);
-    }
-    __syncthreads();
-    // WT = V + V T
     double2* W = D.WT + (size_t)io0 * nn;
-    for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-      int i = e % n, j = e / n;
-      double re = 0.0, im = 0.0;
-      for (int k = 0; k < n; ++k) {
-        double v = D.V[i + (size_t)n * k];
-        double2 b = T[k + (size_t)n * j];
-        re += v * b.x;
-        im += v * b.y;
+    if constexpr (MAG2) {
+      // W = V + V chi V with chi = eps^-1 chi0 and eps = I - chi0 V: since
+      // eps^-1 chi0 V = eps^-1 - I, V chi V = V eps^-1 - V and W = V eps^-1,
+      // one product and no cancellation between V and V chi V
+      for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+        const int i = e % n, j = e / n;
+        double re = 0.0, im = 0.0;
+        for (int k = 0; k < n; ++k) {
+          const double v = D.V[i + (size_t)n * k];
+          const double2 b = E[k + (size_t)n * j];
+          re += v * b.x;
+          im += v * b.y;
+        }
+        W[e] = make_double2(re, im);
+        if (D.epsinv) D.epsinv[(size_t)io0 * nn + e] = E[e];
       }
-      W[e] = make_double2(D.V[e] + re, im);
-      if (D.epsinv) D.epsinv[(size_t)io0 * nn + e] = E[e];
+    } else {
+      // chi = eps^-1 chi0
+      for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+        int i = e % n, j = e / n;
+        double re = 0.0, im = 0.0;
+        for (int k = 0; k < n; ++k) {
+          double2 a = E[i + (size_t)n * k], b = A[k + (size_t)n * j];
+          re += a.x * b.x - a.y * b.y;
+          im += a.x * b.y + a.y * b.x;
+        }
+        Cx[e] = make_double2(re, im);
+      }
+      __syncthreads();
+      // T = chi V
+      for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+        int i = e % n, j = e / n;
+        double re = 0.0, im = 0.0;
+        for (int k = 0; k < n; ++k) {
+          double2 a = Cx[i + (size_t)n * k];
+          double v = D.V[k + (size_t)n * j];
+          re += a.x * v;
+          im += a.y * v;
+        }
+        T[e] = make_double2(re, im);
+      }
+      __syncthreads();
+      // WT = V + V T
+      for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+        int i = e % n, j = e / n;
+        double re = 0.0, im = 0.0;
+        for (int k = 0; k < n; ++k) {
+          double v = D.V[i + (size_t)n * k];
+          double2 b = T[k + (size_t)n * j];
+          re += v * b.x;
+          im += v * b.y;
+        }
+        W[e] = make_double2(D.V[e] + re, im);
+        if (D.epsinv) D.epsinv[(size_t)io0 * nn + e] = E[e];
+      }
     }
     if (D.head && threadIdx.x == 0) D.head[io0] = E[0];
     __syncthreads();

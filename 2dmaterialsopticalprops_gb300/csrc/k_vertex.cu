@@ -19,6 +19,8 @@
 // row of nbnd complex values), then every thread accumulates its
 // (transition, G) outputs in FP64.
 
+#include <climits>
+
 #include "rpa_internal.cuh"
 
 namespace rpa {
@@ -487,6 +489,84 @@ int vertices_f32(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, lo
   return RPA_OK;
 }
 
+// Gfast maps, one block per FBZ k-point.  The box coordinate of a pair
+// separates, c(G, i) = base(i) + shift(G):
+//   forward  base(i) = RI2 (R1 G_i + G_iG0) - lo,    shift(G) = RI2 Glf_G
+//   inverse  base(p) = RI1 (R2 G_p - G_iG0) - lo,    shift(G) = -RI1 Glf_G
+// (i a plane wave of K1, p one of K2; gfast_pos / gfast_inv_pos give the same
+// positions element by element), so both tables go to shared memory and every
+// (G, i) is one add, a bounds test, the box lookup and the basis lookup.
+// out[k_local][G][i] for i < nsum_max, -1 where absent or beyond the basis.
+template <bool INV>
+__global__ void __launch_bounds__(512) k_map_k(MapCtx C, int k0, int nsum_max, int16_t* __restrict__ out) {
+  extern __shared__ int msm[];
+  int* base = msm;                   // [3][nsum_max]
+  int* shift = msm + 3 * nsum_max;   // [3][nlf]
+  const int kl = blockIdx.x;
+  const int* km = C.kmap + 5 * (k0 + kl);
+  const int K1 = km[0], R1 = km[1], K2 = km[2], R2 = km[3], iG0 = km[4];
+  const int kS = INV ? K2 : K1;  // basis of the summed index
+  const int kL = INV ? K1 : K2;  // basis the positions refer to
+  const int ns = INV ? C.npw[K2] : (C.legacy ? C.nsum_legacy : C.npw[K1]);
+  const int* r = C.Rc + 9 * (INV ? R2 : R1);
+  const int* ri = C.RIc + 9 * (INV ? R1 : R2);
+  const int* m0 = C.miller + 3 * iG0;
+  const int sg = INV ? -1 : 1;
+  for (int i = threadIdx.x; i < nsum_max; i += blockDim.x) {
+    int c0 = 0, c1 = 0, c2 = 0;
+    if (i < ns) {
+      const int* m = C.miller + 3 * C.gidx[(size_t)kS * C.npwx + i];
+      const int b0 = r[0] * m[0] + r[1] * m[1] + r[2] * m[2] + sg * m0[0];
+      const int b1 = r[3] * m[0] + r[4] * m[1] + r[5] * m[2] + sg * m0[1];
+      const int b2 = r[6] * m[0] + r[7] * m[1] + r[8] * m[2] + sg * m0[2];
+      c0 = ri[0] * b0 + ri[1] * b1 + ri[2] * b2 - C.box_lo0;
+      c1 = ri[3] * b0 + ri[4] * b1 + ri[5] * b2 - C.box_lo1;
+      c2 = ri[6] * b0 + ri[7] * b1 + ri[8] * b2 - C.box_lo2;
+    } else {
+      c0 = INT_MIN / 2;  // outside the box for every shift
+    }
+    base[i] = c0;
+    base[nsum_max + i] = c1;
+    base[2 * nsum_max + i] = c2;
+  }
+  for (int g = threadIdx.x; g < C.nlf; g += blockDim.x) {
+    const int* ml = C.lf_miller + 3 * g;
+    shift[g] = sg * (ri[0] * ml[0] + ri[1] * ml[1] + ri[2] * ml[2]);
+    shift[C.nlf + g] = sg * (ri[3] * ml[0] + ri[4] * ml[1] + ri[5] * ml[2]);
+    shift[2 * C.nlf + g] = sg * (ri[6] * ml[0] + ri[7] * ml[1] + ri[8] * ml[2]);
+  }
+  __syncthreads();
+  const int* inv = C.inv + (size_t)kL * C.ng;
+  const int nposL = C.npw[kL];
+  int16_t* o = out + (size_t)kl * C.nlf * nsum_max;
+  for (int g = 0; g < C.nlf; ++g) {
+    const int s0 = shift[g], s1 = shift[C.nlf + g], s2 = shift[2 * C.nlf + g];
+    for (int i = threadIdx.x; i < nsum_max; i += blockDim.x) {
+      const int c0 = base[i] + s0, c1 = base[nsum_max + i] + s1, c2 = base[2 * nsum_max + i] + s2;
+      int pos = -1;
+      if ((unsigned)c0 < (unsigned)C.box_d0 && (unsigned)c1 < (unsigned)C.box_d1 && (unsigned)c2 < (unsigned)C.box_d2) {
+        const int gg = C.box[((size_t)c0 * C.box_d1 + c1) * C.box_d2 + c2];
+        if (gg >= 0) pos = (C.legacy && !INV) ? (gg < nposL ? gg : -1) : inv[gg];
+      }
+      o[(size_t)g * nsum_max + i] = (int16_t)pos;
+    }
+  }
+}
+
+static bool map_k_fits(const rpa_ctx* c, int nsum_max) {
+  return (size_t)(3 * nsum_max + 3 * c->nlf) * sizeof(int) <= (size_t)160 << 10;
+}
+
+template <bool INV>
+static int launch_map_k(rpa_ctx* c, const MapCtx& C, int k0, int nk, int nsum_max, int16_t* out) {
+  const size_t smem = (size_t)(3 * nsum_max + 3 * c->nlf) * sizeof(int);
+  RPA_CUDA(c, allow_dynamic_smem(k_map_k<INV>, c->device));
+  k_map_k<INV><<<nk, 512, smem, c->stream>>>(C, k0, nsum_max, out);
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  return RPA_OK;
+}
+
 // Gfast maps of the FBZ k-points [k0, k0+nk) as int16 basis positions
 // (-1 absent), gmap[k_local][G][i] for i < nsum_max (-1 beyond nsum).
 __global__ void k_gmap(MapCtx C, int k0, int nk, int nsum_max, int16_t* __restrict__ gmap) {
@@ -505,6 +585,7 @@ __global__ void k_gmap(MapCtx C, int k0, int nk, int nsum_max, int16_t* __restri
 int build_gmap(rpa_ctx* c, int k0, int nk, int nsum_max, int16_t* gmap, int nsum_legacy) {
   MapCtx C = make_map_ctx(c);
   C.nsum_legacy = nsum_legacy;
+  if (map_k_fits(c, nsum_max)) return launch_map_k<false>(c, C, k0, nk, nsum_max, gmap);
   k_gmap<<<4096, 256, 0, c->stream>>>(C, k0, nk, nsum_max, gmap);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
@@ -560,6 +641,7 @@ __global__ void k_ginv(MapCtx C, int k0, int nk, int nsum_max, int16_t* __restri
 int build_ginv(rpa_ctx* c, int k0, int nk, int nsum_max, int16_t* ginv) {
   if (c->legacy) return fail(c, RPA_EINVAL, "inverse Gfast map: needs the igk map of the basis");
   MapCtx C = make_map_ctx(c);
+  if (map_k_fits(c, nsum_max)) return launch_map_k<true>(c, C, k0, nk, nsum_max, ginv);
   k_ginv<<<4096, 256, 0, c->stream>>>(C, k0, nk, nsum_max, ginv);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;

@@ -791,7 +791,9 @@ __global__ void k_presplit_ws(const float2* __restrict__ M, int nlf, int nchunks
     const long long cht = task / (TC_GB * 4);
     const int rem = (int)(task % (TC_GB * 4));
     const int ch = (int)(cht / nht), ht = (int)(cht % nht);
-    const int row = rem % TC_GB, grp = rem / TC_GB, g = ht * TC_GB + row;
+    // the four 16-byte groups of a row on neighbouring threads: every warp
+    // store fills whole 32-byte sectors of eight rows
+    const int row = rem >> 2, grp = rem & 3, g = ht * TC_GB + row;
     float re[8], im[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {

@@ -175,17 +175,19 @@ __device__ __forceinline__ void kk_df_add(float& hi, float& lo, float v) {
 }
 
 template <bool CPLX>
-__global__ void __launch_bounds__(256) k_kk_f32(const float* __restrict__ K, const double* __restrict__ S,
+__global__ void __launch_bounds__(256, 2) k_kk_f32(const float* __restrict__ K, const double* __restrict__ S,
                                                 double2* __restrict__ out, int nrow, int nw, int np, int pi_row0) {
-  constexpr int BM = 32, BN = 128, BK = 32;
-  __shared__ float Ks[BK][BM + 1];
-  __shared__ float Ss[BK][BN];
+  // 64 x 128 output tile per block, 8 rows x 4 columns per thread; K-panel
+  // rows padded to 68 floats so that each thread's 8 rows are two 16-byte loads
+  constexpr int BM = 64, BN = 128, BK = 32, KP = BM + 4;
+  __shared__ __align__(16) float Ks[BK][KP];
+  __shared__ __align__(16) float Ss[BK][BN];
   const int ncols = CPLX ? 2 * np : np;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads: 4 rows x 4 cols each
-  float hi[4][4], lo[4][4];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads: 8 rows x 4 cols each
+  float hi[8][4], lo[8][4];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < 8; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) hi[i][j] = lo[i][j] = 0.f;
   for (int k0 = 0; k0 < nw; k0 += BK) {
@@ -200,33 +202,33 @@ __global__ void __launch_bounds__(256) k_kk_f32(const float* __restrict__ K, con
       Ss[kk][nn] = (k < nw && col < ncols) ? (float)S[(size_t)k * ncols + col] : 0.f;
     }
     __syncthreads();
-    float acc[4][4];
+    float acc[8][4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 8; ++i)
 #pragma unroll
       for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
 #pragma unroll 8
     for (int kk = 0; kk < BK; ++kk) {
-      float a[4], b[4];
+      const float4 a0 = *reinterpret_cast<const float4*>(&Ks[kk][ty * 8]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&Ks[kk][ty * 8 + 4]);
+      const float4 bv = *reinterpret_cast<const float4*>(&Ss[kk][tx * 4]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[4] = {bv.x, bv.y, bv.z, bv.w};
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = Ks[kk][ty * 4 + i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = Ss[kk][tx * 4 + j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < 8; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 8; ++i)
 #pragma unroll
       for (int j = 0; j < 4; ++j) kk_df_add(hi[i][j], lo[i][j], acc[i][j]);
     __syncthreads();
   }
   const double pi = 3.141592653589793238462643383279502884;
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    int r = m0 + ty * 4 + i;
+  for (int i = 0; i < 8; ++i) {
+    int r = m0 + ty * 8 + i;
     if (r >= nrow) continue;
     const double* srow = S + (size_t)(pi_row0 + r) * ncols;
 #pragma unroll
@@ -292,7 +294,7 @@ int kk_run(rpa_ctx* c, int variant, int no, double domega) {
   // S row holding S0(io-1): Sloss row io-1 (io0), Optabs row (io-1)+no
   const int pi_row0 = cplx ? no : 0;
   if (c->precision == RPA_PREC_MIXED) {
-    dim3 g2((ncols + 127) / 128, (nrow + 31) / 32);
+    dim3 g2((ncols + 127) / 128, (nrow + 63) / 64);
     if (cplx)
       k_kk_f32<true><<<g2, 256, 0, c->stream>>>(dkf.as<float>(), c->d_S.as<double>(), c->d_chi0.as<double2>(),
                                                 nrow, nw, np, pi_row0);

@@ -24,6 +24,7 @@ struct PairCtx {
   const double2* occ;  // [kibz][nbnd]: (f, Qeff prefactor)
   int nbnd, nocc, mode, nw, obase;
   double domega, eta, cut_over_eta, df_cut, Efermi, tenT, c_charge, c_current;
+  int2* scr;           // [ntot][npairs]: (lo | kind << 28, hi) from the count pass
 };
 
 // L(io) >= cut/eta, evaluated as ((o + e1) - e2)^2 + eta^2 without contraction.
@@ -104,12 +105,44 @@ __device__ int eval_pair(const PairCtx& P, int ik, int p, Trans* t) {
   return 1;
 }
 
+// Record of pair p of k-point ik from its kind (1 interband, 2 intraband) and
+// window, as eval_pair writes it.
+__device__ void fill_pair(const PairCtx& P, int ik, int p, int kind, int lo, int hi, Trans* t) {
+  const int* km = P.kmap + 5 * ik;
+  const int K1 = km[0], K2 = km[2];
+  int n, m;
+  if (P.mode == RPA_MODE_CHARGE) {
+    const int nemp = P.nbnd - P.nocc;
+    n = p / nemp;
+    m = P.nocc + p % nemp;
+  } else {
+    n = p / P.nbnd;
+    m = p % P.nbnd;
+  }
+  t->k = ik;
+  t->nm = n | (m << 16);
+  t->e1 = P.E[(size_t)K1 * P.nbnd + n];
+  t->e2 = P.E[(size_t)K2 * P.nbnd + m];
+  if (P.mode == RPA_MODE_CHARGE) {
+    t->c = P.c_charge;
+  } else {
+    const double2 o1 = P.occ[(size_t)K1 * P.nbnd + n];
+    t->c = kind == 2 ? o1.y : P.c_current * (o1.x - P.occ[(size_t)K2 * P.nbnd + m].x);
+  }
+  t->lo = lo;
+  t->hi = hi;
+}
+
+// The count pass evaluates every pair (the FP64 window search) once and keeps
+// its kind and window in P.scr for the emit pass.
 __global__ void k_pairs_count(PairCtx P, int k0, int npairs, int* counts, int* maxpairs) {
   int ik = k0 + blockIdx.x;
   int cnt = 0;
   for (int p = threadIdx.x; p < npairs; p += blockDim.x) {
     Trans t;
-    cnt += eval_pair(P, ik, p, &t) != 0;
+    const int kind = eval_pair(P, ik, p, &t);
+    cnt += kind != 0;
+    P.scr[(size_t)ik * npairs + p] = kind ? make_int2(t.lo | (kind << 28), t.hi) : make_int2(0, 0);
   }
   typedef cub::BlockReduce<int, 256> BR;
   __shared__ typename BR::TempStorage tmp;
@@ -136,7 +169,12 @@ __global__ void k_pairs_emit(PairCtx P, int k0, int npairs, const long long* off
   for (int p0 = 0; p0 < npairs; p0 += blockDim.x) {
     int p = p0 + threadIdx.x;
     Trans t;
-    int kind = p < npairs ? eval_pair(P, ik, p, &t) : 0;
+    int kind = 0;
+    if (p < npairs) {
+      const int2 r = P.scr[(size_t)ik * npairs + p];
+      kind = (int)((unsigned)r.x >> 28);
+      if (kind) fill_pair(P, ik, p, kind, r.x & 0x0fffffff, r.y, &t);
+    }
     int flag = kind != 0, rank, total;
     BS(tmp).ExclusiveSum(flag, rank, total);
     if (flag) {
@@ -188,6 +226,7 @@ static PairCtx make_pair_ctx(rpa_ctx* c, const Chi0Plan& Pl) {
   P.tenT = 10.0 * Pl.T;
   P.c_charge = 2.0 / Pl.norm_s;
   P.c_current = -2.0 / Pl.norm_s;
+  P.scr = c->d_pairscr.as<int2>();
   return P;
 }
 
@@ -198,6 +237,7 @@ static int npairs_of(rpa_ctx* c, const Chi0Plan& P) {
 // Counts the contributing transitions of every FBZ k-point in [k0, k0+nk)
 // into d_counts (host copy returned through counts).
 int count_pairs(rpa_ctx* c, const Chi0Plan& Pl, int k0, int nk, std::vector<int>& counts, int* maxp) {
+  RPA_TRY(ensure(c, c->d_pairscr, sizeof(int2) * (size_t)(k0 + nk) * npairs_of(c, Pl)));
   PairCtx P = make_pair_ctx(c, Pl);
   RPA_TRY(ensure(c, c->d_counts, sizeof(int) * (size_t)(nk + 1)));
   RPA_TRY(ensure(c, c->d_wmax, 32));

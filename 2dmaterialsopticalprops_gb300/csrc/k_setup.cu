@@ -12,6 +12,7 @@
 // identical to a plain IEEE evaluation of the Fortran expression.
 
 #include <cub/cub.cuh>
+#include <cmath>
 #include <cstring>
 
 #include "rpa_internal.cuh"
@@ -25,6 +26,8 @@ struct PairCtx {
   int nbnd, nocc, mode, nw, obase;
   double domega, eta, cut_over_eta, df_cut, Efermi, tenT, c_charge, c_current;
   int2* scr;           // [ntot][npairs]: (lo | kind << 28, hi) from the count pass
+  double half_width;   // eta sqrt(1/cut - 1) / domega: half-width of a window in rows
+  double inv_domega;
 };
 
 // L(io) >= cut/eta, evaluated as ((o + e1) - e2)^2 + eta^2 without contraction.
@@ -38,11 +41,11 @@ __device__ __forceinline__ bool in_window(const PairCtx& P, int r, double e1, do
 
 // Exact window [lo, hi] of rows r in [0, nw), or lo > hi when empty.
 __device__ void window_of(const PairCtx& P, double e1, double e2, int* lo_out, int* hi_out) {
-  // |dE| <= R with R = eta sqrt(1/cut - 1); centre where o = e2 - e1.
-  double cut = P.cut_over_eta * P.eta;
-  double R = P.eta * sqrt(fmax(1.0 / cut - 1.0, 0.0));
-  double rc = (e2 - e1) / P.domega - (double)P.obase;
-  double h = R / P.domega;
+  // |dE| <= R with R = eta sqrt(1/cut - 1); centre where o = e2 - e1.  The
+  // bracket only has to contain the window (its edges are then found with the
+  // exact predicate), so it uses the precomputed half-width and 1/domega.
+  double rc = (e2 - e1) * P.inv_domega - (double)P.obase;
+  double h = P.half_width;
   double flo = floor(rc - h) - 1.0, fhi = ceil(rc + h) + 1.0;
   if (fhi < 0.0 || flo > (double)(P.nw - 1)) {
     *lo_out = 1;
@@ -227,6 +230,9 @@ static PairCtx make_pair_ctx(rpa_ctx* c, const Chi0Plan& Pl) {
   P.c_charge = 2.0 / Pl.norm_s;
   P.c_current = -2.0 / Pl.norm_s;
   P.scr = c->d_pairscr.as<int2>();
+  const double cut = Pl.cut;
+  P.half_width = Pl.eta * std::sqrt(std::fmax(1.0 / cut - 1.0, 0.0)) / Pl.domega;
+  P.inv_domega = 1.0 / Pl.domega;
   return P;
 }
 

@@ -37,8 +37,8 @@ PKG = "2dmaterialsopticalprops_gb300"
 
 ACC_DRAM_BYTES_PER_PAIR = 30.4e9 / 54.6e6
 # DRAM bytes per FBZ k-point of one current-vertex launch (k_vertex_mn<32, current>):
-# ncu measured 15.9 + 0.55 GB for the 1600 k-points of the 40x40 case
-VTX_DRAM_BYTES_PER_K = 16.45e9 / 1600
+# ncu measured 16.0 + 0.55 GB for the 1600 k-points of the 40x40 case
+VTX_DRAM_BYTES_PER_K = 16.56e9 / 1600
 
 
 def pkg(name):

@@ -92,3 +92,27 @@ def test_kmap_oracle_reproduces_the_grid_bookkeeping(synth, orc):
         km = synth.q_kmap(s, steps, steps2)
         iG0, R2, K2 = orc.find_kq(s.ktot, s.ktot, s.RI, 1, s.G, km["q"], 1e-4)
         assert (K2 == km["K2"]).all() and (iG0 == km["iG0"]).all() and (R2 == 1).all()
+
+
+def test_w_equals_v_times_inverse_epsilon(orc):
+    """The identity behind the mixed path's Dyson step: for eps = I - chi0 V,
+    eps^-1 chi0 V = eps^-1 - I, so the reference's W = V + V chi V (chi =
+    eps^-1 chi0) equals V eps^-1.  Checked on the oracle's loop-for-loop gjel
+    and genWT restatement with a random complex chi0 (strong screening, so V
+    and V chi V nearly cancel) and a real symmetric V."""
+    rng = np.random.default_rng(7)
+    n, nw = 9, 5
+    A = rng.standard_normal((n, n))
+    Vm = A @ A.T + n * np.eye(n)  # real symmetric, well conditioned
+    chi = rng.standard_normal((n, n, nw)) + 1j * rng.standard_normal((n, n, nw))
+    chi *= 0.5
+    WT, Ei, rc = orc.dyson(chi, np.ascontiguousarray(Vm.T), fast_wt=False)
+    assert rc == 0
+    for w in range(nw):
+        W = orc.fortran_mat(WT[:, :, w])
+        E = orc.fortran_mat(Ei[:, :, w])
+        C = orc.fortran_mat(chi[:, :, w])
+        eps = np.eye(n) - C @ Vm
+        assert np.allclose(E @ eps, np.eye(n), atol=1e-10)
+        VE = Vm @ E
+        assert np.max(np.abs(W - VE)) <= 1e-10 * np.max(np.abs(W))

@@ -98,8 +98,7 @@ def test_w_equals_v_times_inverse_epsilon(orc):
     """The identity behind the mixed path's Dyson step: for eps = I - chi0 V,
     eps^-1 chi0 V = eps^-1 - I, so the reference's W = V + V chi V (chi =
     eps^-1 chi0) equals V eps^-1.  Checked on the oracle's loop-for-loop gjel
-    and genWT restatement with a random complex chi0 (strong screening, so V
-    and V chi V nearly cancel) and a real symmetric V."""
+    and genWT restatement with a random complex chi0 and a real symmetric V."""
     rng = np.random.default_rng(7)
     n, nw = 9, 5
     A = rng.standard_normal((n, n))

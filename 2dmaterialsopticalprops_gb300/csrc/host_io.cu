@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <condition_variable>
+#include <exception>
 #include <cstring>
 #include <mutex>
 #include <thread>
@@ -33,16 +34,23 @@ struct CopyPool {
   bool stop = false;
 
   explicit CopyPool(int nt) {
-    for (int t = 0; t < nt; ++t) th.emplace_back([this, t] { loop(t); });
+    try {
+      for (int t = 0; t < nt; ++t) th.emplace_back([this, t] { loop(t); });
+    } catch (...) {
+      shutdown();  // join the threads already started before the exception leaves
+      throw;
+    }
   }
-  ~CopyPool() {
+  ~CopyPool() { shutdown(); }
+  void shutdown() {
     {
       std::lock_guard<std::mutex> l(m);
       stop = true;
       ++gen;
     }
     cv.notify_all();
-    for (auto& x : th) x.join();
+    for (auto& x : th)
+      if (x.joinable()) x.join();
   }
   void loop(int t) {
     unsigned seen = 0;
@@ -94,16 +102,30 @@ static bool host_pinned(const void* p) {
   return a.type == cudaMemoryTypeHost;
 }
 
+void host_io_release(rpa_ctx* c);
+
 static int ensure_ring(rpa_ctx* c) {
-  if (c->io.ring[0]) return RPA_OK;
-  for (int b = 0; b < 2; ++b) {
-    RPA_CUDA(c, cudaHostAlloc(&c->io.ring[b], RING_BYTES, cudaHostAllocDefault));
-    RPA_CUDA(c, cudaEventCreateWithFlags(&c->io.ev[b], cudaEventDisableTiming));
-    RPA_CUDA(c, cudaEventCreateWithFlags(&c->io.ev[2 + b], cudaEventDisableTiming));
+  if (c->io.pool) return RPA_OK;  // the pool is made last: the ring is complete
+  host_io_release(c);             // whatever an earlier, failed attempt left
+  cudaError_t e = cudaSuccess;
+  for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+    e = cudaHostAlloc(&c->io.ring[b], RING_BYTES, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->io.ev[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->io.ev[2 + b], cudaEventDisableTiming);
   }
-  RPA_CUDA(c, cudaStreamCreateWithFlags(&c->io.copy_stream, cudaStreamNonBlocking));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->io.copy_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    host_io_release(c);
+    return cuda_fail(c, e, "page-locked staging ring");
+  }
   const unsigned hw = std::thread::hardware_concurrency();
-  c->io.pool = new CopyPool((int)std::max(1u, std::min(8u, hw ? hw : 4u)));
+  try {
+    c->io.pool = new CopyPool((int)std::max(1u, std::min(8u, hw ? hw : 4u)));
+  } catch (const std::exception& ex) {
+    // no exception crosses the C ABI: thread or memory exhaustion is an error code
+    host_io_release(c);
+    return fail(c, RPA_ENOMEM, "host copy threads: %s", ex.what());
+  }
   return RPA_OK;
 }
 

@@ -7,7 +7,10 @@ k+G spheres), NGloc = 91 local fields, nw = 1001 frequencies on 0-30 eV,
 eta = 25 meV, q one grid step along Gamma-M.  A step computes, for that q:
 the current-current correlation S0 and chi0 for pol xx and pol zz (Optabs:
 vertices, S0 over -no..no, Qeff, KK) and the loss chain (Sloss: vertices,
-S0, KK, eps = 1 - chi0 V, gjel, chi, W).  Metric: q-point spectra per second.
+S0, KK, eps = 1 - chi0 V, gjel, W).  Metric: q-point spectra per second.
+With N ranks, rank r computes its own q-point (r + 1 grid steps) and the
+step time is the slowest rank's (weak scaling, no collective on the data
+path).
 
 value : inputs resident in HBM (basis loaded once), outputs left on the device.
 e2e   : the same step through the C ABI with host buffers: the basis is copied
@@ -58,6 +61,23 @@ def config_of(name: str, q_steps: int):
     if name == "small":
         return synth.config_small(q_steps=q_steps)
     raise SystemExit(f"unknown config {name}")
+
+
+def q_steps_of_rank(rank: int) -> int:
+    """q-point of a rank: rank r computes q = (r + 1) grid steps along Gamma-M
+    (independent q-points, weak scaling, no collective on the data path)."""
+    return 1 + rank
+
+
+def max_over_ranks(dist, value: float, device: str = "cuda") -> float:
+    """The largest value over all ranks (the slowest rank's time); value
+    itself without a process group."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def workload_desc(s, name):
@@ -563,7 +583,7 @@ def main():
     torch.cuda.set_device(local)
     rpa, synth = pkg("rpa"), pkg("synth")
     pkg("build").build()
-    q_steps = 1 + rank  # independent q-point per rank (weak scaling, no collective)
+    q_steps = q_steps_of_rank(rank)
     cfg = config_of(args.config, q_steps)
     t0 = time.time()
     s = synth.build(cfg)
@@ -593,11 +613,8 @@ def main():
     torch.cuda.synchronize()
     ctx.synchronize()
     clocks = sampler.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = max_over_ranks(dist, ev0.elapsed_time(ev1) / args.steps)
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
     value = world * 1000.0 / ms
 
@@ -628,11 +645,7 @@ def main():
                     for a in v:
                         if a is not None:
                             d2h += a.nbytes
-        ems = float(np.median(e2e_ms))
-        if dist:
-            t = torch.tensor([ems], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ems = float(t.item())
+        ems = max_over_ranks(dist, float(np.median(e2e_ms)))
         e2e = {"value": world * 1000.0 / ems, "unit": "q-spectra/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": ems}
 

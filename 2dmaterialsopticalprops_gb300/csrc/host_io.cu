@@ -93,13 +93,16 @@ struct CopyPool {
 static constexpr size_t RING_BYTES = (size_t)64 << 20;  // per staging buffer
 static constexpr size_t DIRECT_BELOW = (size_t)4 << 20;
 
-static bool host_pinned(const void* p) {
+// Page-locked host memory and memory the device can address (device or
+// managed allocations) are copied directly by the DMA engines; only ordinary
+// pageable memory goes through the staging ring.
+static bool direct_copy(const void* p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeHost;
+  return a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
 void host_io_release(rpa_ctx* c);
@@ -143,8 +146,8 @@ void host_io_release(rpa_ctx* c) {
 
 int copy_d2h(rpa_ctx* c, void* dst, const void* src, size_t bytes) {
   if (bytes == 0) return RPA_OK;
-  if (bytes < DIRECT_BELOW || host_pinned(dst)) {
-    RPA_CUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (bytes < DIRECT_BELOW || direct_copy(dst)) {
+    RPA_CUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c->stream));
     RPA_CUDA(c, cudaStreamSynchronize(c->stream));
     return RPA_OK;
   }
@@ -182,7 +185,7 @@ int copy_d2h(rpa_ctx* c, void* dst, const void* src, size_t bytes) {
 int upload_basis(rpa_ctx* c, const double* coeff, int nks, int nbnd, int npwx, double2* dst) {
   const size_t per_k = (size_t)nbnd * npwx * sizeof(double2);
   RPA_TRY(ensure_ring(c));
-  const bool pinned = host_pinned(coeff);
+  const bool pinned = direct_copy(coeff);
   // device chunk: up to 256 MB of whole k-points (at least one); a pageable
   // source also fits the chunk in one ring buffer
   size_t cap = pinned ? ((size_t)256 << 20) : RING_BYTES;
@@ -212,7 +215,7 @@ int upload_basis(rpa_ctx* c, const double* coeff, int nks, int nbnd, int npwx, d
     char* dbuf = c->d_tmp.as<char>() + (size_t)b * chunk;
     if (j >= 2) RPA_CUDA(c, cudaStreamWaitEvent(c->io.copy_stream, tdone[b], 0));
     if (pinned) {
-      RPA_CUDA(c, cudaMemcpyAsync(dbuf, src, len, cudaMemcpyHostToDevice, c->io.copy_stream));
+      RPA_CUDA(c, cudaMemcpyAsync(dbuf, src, len, cudaMemcpyDefault, c->io.copy_stream));
     } else {
       if (j >= 2) RPA_CUDA(c, cudaEventSynchronize(cdone[b]));  // ring b still feeding copy j - 2
       c->io.pool->copy(c->io.ring[b], src, len);

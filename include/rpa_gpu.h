@@ -108,7 +108,11 @@ int rpa_set_symmetry(rpa_ctx* ctx, int nsym, const double* R, const double* RI);
  *           or NULL for the legacy drivers, where coefficient i belongs to G(:,i)
  *   coeff : C(npwx,nbnd,nks) complex(dp)
  *   E     : E(nks,nbnd) Hartree (any scissor already applied)
- * The basis stays resident on the device until the next call or rpa_destroy. */
+ * The basis stays resident on the device until the next call or rpa_destroy.
+ * coeff may be ordinary (pageable) memory — it then passes through the
+ * context's page-locked staging ring — or page-locked / device memory, which
+ * is copied directly; the same holds for the large outputs of rpa_chi0,
+ * rpa_kk and rpa_dyson. */
 int rpa_load_basis(rpa_ctx* ctx, int nks, int nbnd, int npwx, const int* npw, const int* igk,
                    const double* coeff, const double* E);
 
@@ -213,6 +217,9 @@ int rpa_kk(rpa_ctx* ctx, int variant, double* chi0_out);
 
 /* Replaces: the Dyson loop of Sloss.f90:452-481 for io = 1..no-1:
  * genV, eps = I - chi0 V, gjel (W/gjel.f), chi = eps^-1 chi0, WT = V + V chi V.
+ * RPA_PREC_FP64 follows these steps; RPA_PREC_MIXED inverts eps in FP64 as
+ * well but forms WT as V eps^-1, the same matrix (eps^-1 chi0 V = eps^-1 - I)
+ * with one product and no cancellation between V and V chi V.
  *   c0, eps    : the &parameters c0 (bohr) and eps of the driver
  *   WT_out     : complex WT(no-1,nlf,nlf) (may be NULL)
  *   epsinv_out : complex eps^-1(no-1,nlf,nlf) (may be NULL)

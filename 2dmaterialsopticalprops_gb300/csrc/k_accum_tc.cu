@@ -52,6 +52,9 @@ struct AccTcCtx {
   float inv_scale;      // 1 / (scaleA scaleB)
   float inv_src;        // 1 / (scale of the pre-split A-side tile)
   int nht;              // 96-row tiles of the local fields
+  int sym;              // 1: S0 is Hermitian (complex) or symmetric (real) -- M2 = M --, so only the
+                        // tile pairs gi <= gj are computed (blockIdx.y enumerates them) and the
+                        // conversion to FP64 mirrors the others
   long long a_chunk, a_tile;  // A-side source: bytes per chunk and per tile
   int a_lo;             // A-side source: offset of the lo rows
   int n_rows;           // rows of M / M2 (n_inter rounded up to a multiple of 32, zero padded)
@@ -497,7 +500,18 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int r0 = blockIdx.x * NIO;
-  const int gi = blockIdx.y, gj = blockIdx.z;  // G tile (A rows), G' tile (B rows), 96 local fields each
+  // G tile (A rows) and G' tile (B rows), 96 local fields each
+  int gi = blockIdx.y, gj = blockIdx.z;
+  if (A.sym) {
+    // blockIdx.y enumerates the pairs gi <= gj row by row
+    int p = blockIdx.y;
+    gi = 0;
+    while (p >= A.nht - gi) {
+      p -= A.nht - gi;
+      ++gi;
+    }
+    gj = gi + p;
+  }
   const int nrowA = min(TC_GB, A.nlf - gi * TC_GB);
   const size_t np = (size_t)A.nlf * A.nlf;
 
@@ -834,6 +848,30 @@ __global__ void k_df_to_f64(const float2* __restrict__ Sdf, double* __restrict__
   }
 }
 
+// The same conversion for an S0 whose tile pairs gi > gj were not computed
+// (M2 = M): entry (G, G') of such a pair is taken from (G', G), conjugated for
+// the complex S0 (S(G', G) = sum w M(G') conj M(G) = conj S(G, G')).
+template <bool CPLX>
+__global__ void k_df_to_f64_sym(const float2* __restrict__ Sdf, double* __restrict__ S, int nw, int nlf,
+                                int tile) {
+  const size_t np = (size_t)nlf * nlf, n = (size_t)nw * np;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t io = e / np;
+    const int p = (int)(e - io * np), iG = p % nlf, jG = p / nlf;
+    const bool mirror = iG / tile > jG / tile;
+    const size_t src = mirror ? io * np + (size_t)jG + (size_t)nlf * iG : e;
+    if (CPLX) {
+      const float2 re = Sdf[2 * src], im = Sdf[2 * src + 1];
+      const double vi = (double)im.x + (double)im.y;
+      S[2 * e] += (double)re.x + (double)re.y;
+      S[2 * e + 1] += mirror ? -vi : vi;
+    } else {
+      const float2 v = Sdf[src];
+      S[e] += (double)v.x + (double)v.y;
+    }
+  }
+}
+
 template <int NIO, bool CPLX, bool F16, bool STAGE_M>
 static int launch_tc(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char* tiles) {
   constexpr int NTB = CPLX ? 4 : 2;
@@ -853,7 +891,7 @@ static int launch_ws(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char*
   using Cfg = WsCfg<NIO, CPLX, SEPA>;
   auto kern = k_accum_ws<NIO, CPLX, SEPA>;
   RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
-  dim3 grid((nw + NIO - 1) / NIO, A.nht, A.nht);
+  dim3 grid((nw + NIO - 1) / NIO, A.sym ? A.nht * (A.nht + 1) / 2 : A.nht, A.sym ? 1 : A.nht);
   kern<<<grid, WS_THREADS, Cfg::SMEM, c->stream>>>(A, tiles, tilesA);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
@@ -884,6 +922,7 @@ int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const fl
                   float amaxM, float amaxM2, double cmax) {
   if (n_inter == 0) return RPA_OK;
   AccTcCtx A;
+  A.sym = 0;
   A.rec = c->d_sorted.as<Trans>();
   A.M = Mf;
   A.M2 = Mf2;
@@ -937,6 +976,8 @@ int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const fl
       A.a_lo = TC_TILE;
     }
     const bool sepa = two || nht > 1;
+    A.sym = (!two && nht > 1) ? 1 : 0;
+    c->s_sym = A.sym != 0;
     if (cplx) return sepa ? launch_ws<1, true, true>(c, A, P.nw, tiles, tilesA) : launch_ws<1, true, false>(c, A, P.nw, tiles, tilesA);
     return sepa ? launch_ws<1, false, true>(c, A, P.nw, tiles, tilesA) : launch_ws<2, false, false>(c, A, P.nw, tiles, tilesA);
   }
@@ -1014,8 +1055,17 @@ int cmax_of(rpa_ctx* c, int n_inter, double* cmax) {
   return RPA_OK;
 }
 
-int df_to_f64(rpa_ctx* c, size_t n) {
-  k_df_to_f64<<<2048, 256, 0, c->stream>>>(c->d_Sdf.as<float2>(), c->d_S.as<double>(), n);
+int df_to_f64(rpa_ctx* c, size_t n, int nw, bool cplx) {
+  if (c->s_sym) {
+    if (cplx)
+      k_df_to_f64_sym<true><<<2048, 256, 0, c->stream>>>(c->d_Sdf.as<float2>(), c->d_S.as<double>(), nw, c->nlf,
+                                                         TC_GB);
+    else
+      k_df_to_f64_sym<false><<<2048, 256, 0, c->stream>>>(c->d_Sdf.as<float2>(), c->d_S.as<double>(), nw, c->nlf,
+                                                          TC_GB);
+  } else {
+    k_df_to_f64<<<2048, 256, 0, c->stream>>>(c->d_Sdf.as<float2>(), c->d_S.as<double>(), n);
+  }
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
   return RPA_OK;

@@ -18,6 +18,8 @@
 // the cost.  The mixed path also forms W as V eps^-1, which equals the
 // reference's V + V chi V (see below) with a quarter of its FP64 products.
 
+#include <mutex>
+
 #include "rpa_internal.cuh"
 
 namespace rpa {
@@ -237,7 +239,8 @@ __global__ void __launch_bounds__(256) k_dyson_fp64(DysonArgs D) {
   }
 }
 
-int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singular, int* n_zero) {
+int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singular, int* n_zero,
+               const double2** head_dev) {
   const int n = c->nlf, nn = n * n, nwo = c->last_no - 1;
   RPA_TRY(ensure(c, c->d_V, sizeof(double) * nn));
   RPA_CUDA(c, cudaMemcpyAsync(c->d_V.p, V_host, sizeof(double) * nn, cudaMemcpyHostToDevice, c->stream));
@@ -274,6 +277,7 @@ int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singul
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
   *n_singular = fl[0];
   *n_zero = fl[1];
+  if (head_dev) *head_dev = D.head;
   return RPA_OK;
 }
 
@@ -305,9 +309,18 @@ static __device__ __align__(256) double2 g_noalloc_scratch[(size_t)NOALLOC_BLOCK
 static __device__ __align__(256) int g_noalloc_flags[4];
 
 // Device addresses of the two arrays, looked up once per device with that
-// device current (the host-side names are only stand-ins, not device addresses).
-static void* g_noalloc_scratch_dev[64];
-static void* g_noalloc_flags_dev[64];
+// device current (the host-side names are only stand-ins, not device
+// addresses).  std::call_once publishes both addresses together, so threads
+// making their first calls at the same time see either nothing or both.  The
+// addresses belong to the device's primary context: after a cudaDeviceReset
+// they are stale, and the entry point must not be used again in the process.
+struct NoallocAddrs {
+  void* scratch = nullptr;
+  void* flags = nullptr;
+  int rc = RPA_OK;
+};
+static NoallocAddrs g_noalloc_addr[64];
+static std::once_flag g_noalloc_once[64];
 
 static __global__ void k_noalloc_clear_flags() {
   if (threadIdx.x < 4) g_noalloc_flags[threadIdx.x] = 0;
@@ -323,15 +336,18 @@ extern "C" int rpa_dyson_noalloc(const double* chi0, const double* V, int n, int
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return RPA_ECUDA;
   // One-time set-up on this device: the first call looks up the device
-  // addresses of the workspace; make that first call before any stream capture.
-  if (!g_noalloc_scratch_dev[dev]) {
-    void* ps = nullptr;
-    void* pf = nullptr;
-    if (cudaGetSymbolAddress(&ps, g_noalloc_scratch) != cudaSuccess) return RPA_ECUDA;
-    if (cudaGetSymbolAddress(&pf, g_noalloc_flags) != cudaSuccess) return RPA_ECUDA;
-    g_noalloc_flags_dev[dev] = pf;
-    g_noalloc_scratch_dev[dev] = ps;
-  }
+  // addresses of the workspace (loading this library's kernels onto the device
+  // if nothing has yet, which reserves the workspace); make that first call
+  // before any stream capture.
+  std::call_once(g_noalloc_once[dev], [dev]() {
+    NoallocAddrs a;
+    if (cudaGetSymbolAddress(&a.scratch, g_noalloc_scratch) != cudaSuccess ||
+        cudaGetSymbolAddress(&a.flags, g_noalloc_flags) != cudaSuccess)
+      a = NoallocAddrs{nullptr, nullptr, RPA_ECUDA};
+    g_noalloc_addr[dev] = a;
+  });
+  const NoallocAddrs& addr = g_noalloc_addr[dev];
+  if (addr.rc != RPA_OK) return addr.rc;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const int grid = nwo < NOALLOC_BLOCKS ? nwo : NOALLOC_BLOCKS;
   DysonArgs D;
@@ -340,8 +356,8 @@ extern "C" int rpa_dyson_noalloc(const double* chi0, const double* V, int n, int
   D.WT = reinterpret_cast<double2*>(WT);
   D.epsinv = nullptr;
   D.head = reinterpret_cast<double2*>(head);
-  D.scratch = reinterpret_cast<double2*>(g_noalloc_scratch_dev[dev]);
-  D.flags = reinterpret_cast<int*>(g_noalloc_flags_dev[dev]);
+  D.scratch = reinterpret_cast<double2*>(addr.scratch);
+  D.flags = reinterpret_cast<int*>(addr.flags);
   D.n = n;
   D.nwo = nwo;
   const size_t smem = ((3 * (size_t)n * sizeof(int) + 15) & ~(size_t)15) + sizeof(double2) * n;

@@ -25,7 +25,7 @@ int vertices_fp64(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, l
 int accumulate_fp64(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax);
 int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const float2* Mf, const float2* Mf2,
                   float amaxM, float amaxM2, double cmax);
-int df_to_f64(rpa_ctx* c, size_t n);
+int df_to_f64(rpa_ctx* c, size_t n, int nw, bool cplx);
 int inverse_perm(rpa_ctx* c, int n, int* pos_of);
 int qeff_f32(rpa_ctx* c, int n_inter, int n_trans, const float2* Mf, const float2* Mf2);
 int cmax_of(rpa_ctx* c, int n_inter, double* cmax);
@@ -33,11 +33,10 @@ int vertices_f32(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, lo
                  float2* Mf, float2* Mf2, unsigned* amax);
 int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans, const int* pos_of, float2* Mf,
                 float2* Mf2, unsigned* amax, bool* used);
-int vertices_tc(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans, const int* pos_of, float2* Mf,
-                float2* Mf2, unsigned* amax, bool* used);
 int qeff_fp64(rpa_ctx* c, const Chi0Plan& P, int n_inter, int n_trans);
 int kk_run(rpa_ctx* c, int variant, int no, double domega);
-int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singular, int* n_zero);
+int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singular, int* n_zero,
+               const double2** head_dev);
 void kk_matrix(int variant, int no, double domega, std::vector<double>& K, int* nw_out);
 int selftest_umma(int which, double* result);
 int selftest_wait(double* result);
@@ -116,10 +115,13 @@ __global__ void k_to_f32(const double2* __restrict__ src, float2* __restrict__ d
   }
 }
 
-// Coefficients scaled by 2^14 and split into fp16 hi + lo halves (as
-// k_to_split16), stored as four planes per plane wave, [re_hi, im_hi, re_lo,
-// im_lo][nbp bands], zero beyond nbnd: a run of bands of one plane wave is
-// contiguous for the MN-major vertex operands.
+// Coefficients scaled by 2^14 and split into fp16 hi + lo halves (hi = the
+// fp16 rounding of 2^14 c, lo = the fp16 rounding of the remainder), stored as
+// four planes per plane wave, [re_hi, im_hi, re_lo, im_lo][nbp bands], zero
+// beyond nbnd: a run of bands of one plane wave is contiguous for the MN-major
+// vertex operands.  Normalised coefficients have |c| <= 1, so 2^14 c stays
+// below the fp16 maximum; the representation's absolute resolution is about
+// 2^-24 / 2^14 ~ 4e-12 of a coefficient.
 __global__ void k_to_planes16(const double2* __restrict__ src, __half* __restrict__ dst, size_t nrows, int nbnd,
                               int nbp) {
   const size_t n = nrows * nbp;
@@ -140,20 +142,6 @@ __global__ void k_to_planes16(const double2* __restrict__ src, __half* __restric
     d[nbp] = __high2half(hi);
     d[2 * nbp] = __low2half(lo);
     d[3 * nbp] = __high2half(lo);
-  }
-}
-
-// Coefficients scaled by 2^14 and split into fp16 hi + lo halves, packed per
-// element as {re_hi | im_hi << 16, re_lo | im_lo << 16}: the tensor-core
-// vertex kernel moves these words into its operand tiles without arithmetic.
-__global__ void k_to_split16(const double2* __restrict__ src, uint2* __restrict__ dst, size_t n) {
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-    double2 v = src[e];
-    float re = (float)v.x * 16384.0f, im = (float)v.y * 16384.0f;
-    __half2 hi = __floats2half2_rn(re, im);
-    float2 h = __half22float2(hi);
-    __half2 lo = __floats2half2_rn(re - h.x, im - h.y);
-    dst[e] = make_uint2(*reinterpret_cast<uint32_t*>(&hi), *reinterpret_cast<uint32_t*>(&lo));
   }
 }
 
@@ -301,7 +289,7 @@ int rpa_create(rpa_ctx** out, const rpa_opts* opts) {
   c->verbose = opts ? opts->verbose : 0;
   c->split_f16 = opts ? opts->split == 0 : true;
   c->tc_seg = (opts && opts->reserved[0] > 0) ? opts->reserved[0] : 1;
-  c->vertex_kind = (opts && (opts->reserved[1] == 1 || opts->reserved[1] == 2)) ? opts->reserved[1] : 0;
+  c->vertex_kind = (opts && opts->reserved[1] == 1) ? 1 : 0;
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete c;
@@ -355,10 +343,10 @@ int rpa_create_shared(rpa_ctx** out, rpa_ctx* parent, int precision) {
   c->h_npw = parent->h_npw;
   c->h_E = parent->h_E;
   DevBuf* mine[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
-                    &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_coeffs, &c->d_cpl, &c->d_E};
+                    &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_cpl, &c->d_E};
   const DevBuf* theirs[] = {&parent->d_miller, &parent->d_G, &parent->d_box, &parent->d_Rc, &parent->d_RIc,
                             &parent->d_Rcart, &parent->d_npw, &parent->d_gidx, &parent->d_inv, &parent->d_coeff,
-                            &parent->d_coeff32, &parent->d_coeffs, &parent->d_cpl, &parent->d_E};
+                            &parent->d_coeff32, &parent->d_cpl, &parent->d_E};
   for (size_t i = 0; i < sizeof(mine) / sizeof(mine[0]); ++i) *mine[i] = *theirs[i];
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -387,12 +375,12 @@ int rpa_destroy(rpa_ctx* c) {
   if (c->parent) {
     // borrowed from the parent: not ours to free
     DevBuf* borrowed[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
-                          &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_coeffs, &c->d_cpl, &c->d_E};
+                          &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_cpl, &c->d_E};
     for (DevBuf* b : borrowed) *b = DevBuf();
     --c->parent->children;
   }
   DevBuf* bufs[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
-                    &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_coeffs, &c->d_cpl, &c->d_E, &c->d_kmap, &c->d_ktot, &c->d_lf_miller,
+                    &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_cpl, &c->d_E, &c->d_kmap, &c->d_ktot, &c->d_lf_miller,
                     &c->d_Glf, &c->d_occ, &c->d_counts, &c->d_offsets, &c->d_trans, &c->d_keys, &c->d_keys_alt,
                     &c->d_vals, &c->d_vals_alt, &c->d_sorted, &c->d_M, &c->d_M2, &c->d_Mf, &c->d_Mf2, &c->d_tiles, &c->d_tilesA, &c->d_gmap, &c->d_ginv, &c->d_vbt, &c->d_ybt, &c->d_cub, &c->d_wmax, &c->d_pairscr,
                     &c->d_ntrans, &c->d_S, &c->d_Sdf, &c->d_Q, &c->d_chi0, &c->d_kk[0], &c->d_kk[1], &c->d_kkf[0], &c->d_kkf[1], &c->d_kkw, &c->d_V, &c->d_eps, &c->d_WT,
@@ -519,9 +507,16 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
   RPA_TRY(ensure(c, c->d_coeff, sizeof(double2) * per_k * nks));
   RPA_TRY(upload_basis(c, coeff, nks, nbnd, npwx, c->d_coeff.as<double2>()));
   if (c->precision == RPA_PREC_MIXED) {
-    // the FP32 copy feeds the CUDA-core vertex kernel only: chosen explicitly, or
-    // where the fp16 planes do not apply (int16 maps, band windows)
-    if (c->vertex_kind != 0 || npwx > 32767 || nbnd > 181) {
+    // the tensor-core vertex kernel keeps plane-wave positions in int16 maps and
+    // band pairs in an int16 table; larger bases need the FP32 CUDA-core vertex
+    // kernel, which the caller must choose (opts.reserved[1] = 1)
+    if (c->vertex_kind == 0 && (npwx > 32767 || nbnd > 181))
+      return fail(c, RPA_EINVAL,
+                  "rpa_load_basis: the mixed path's tensor-core vertices take at most 32767 plane waves and 181 "
+                  "bands per k-point (npwx=%d, nbnd=%d); create the context with opts.reserved[1] = 1 for the "
+                  "FP32 CUDA-core vertex kernel, or use RPA_PREC_FP64", npwx, nbnd);
+    // the FP32 copy feeds the CUDA-core vertex kernel only
+    if (c->vertex_kind == 1) {
       RPA_TRY(ensure(c, c->d_coeff32, sizeof(float2) * per_k * nks));
       k_to_f32<<<2048, 256, 0, c->stream>>>(c->d_coeff.as<double2>(), c->d_coeff32.as<float2>(), per_k * nks);
       RPA_CUDA(c, cudaGetLastError());
@@ -535,12 +530,6 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
                                                nbnd, c->nbp);
     RPA_CUDA(c, cudaGetLastError());
     ++c->launches;
-    if (c->vertex_kind == 2) {
-      RPA_TRY(ensure(c, c->d_coeffs, sizeof(uint2) * per_k * nks));
-      k_to_split16<<<2048, 256, 0, c->stream>>>(c->d_coeff.as<double2>(), c->d_coeffs.as<uint2>(), per_k * nks);
-      RPA_CUDA(c, cudaGetLastError());
-      ++c->launches;
-    }
   }
   cudaEventRecord(c->ev[7], c->stream);
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -688,6 +677,7 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
   const bool cplx = a->mode == RPA_MODE_CURRENT;
   const size_t s_bytes = (size_t)P.nw * np * (cplx ? 16 : 8);
   RPA_TRY(ensure(c, c->d_S, s_bytes));
+  c->s_sym = false;
   RPA_TRY(ensure(c, c->d_Q, sizeof(double2) * np));
   RPA_CUDA(c, cudaMemsetAsync(c->d_S.p, 0, s_bytes, c->stream));
   if (c->precision == RPA_PREC_MIXED) {
@@ -750,12 +740,13 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
       RPA_TRY(ensure(c, c->d_ntrans, 32));
       RPA_CUDA(c, cudaMemsetAsync(c->d_ntrans.p, 0, 32, c->stream));
       cudaEventRecord(c->ev[2], c->stream);
-      bool used_tc = false;
-      if (c->vertex_kind == 0)
+      if (c->vertex_kind == 1) {
+        RPA_TRY(vertices_f32(c, P, k0, nk, maxp, tot, pos_of, Mf, Mf2, c->d_ntrans.as<unsigned>()));
+      } else {
+        bool used_tc = false;
         RPA_TRY(vertices_mn(c, P, k0, nk, tot, pos_of, Mf, Mf2, c->d_ntrans.as<unsigned>(), &used_tc));
-      else if (c->vertex_kind == 2)
-        RPA_TRY(vertices_tc(c, P, k0, nk, tot, pos_of, Mf, Mf2, c->d_ntrans.as<unsigned>(), &used_tc));
-      if (!used_tc) RPA_TRY(vertices_f32(c, P, k0, nk, maxp, tot, pos_of, Mf, Mf2, c->d_ntrans.as<unsigned>()));
+        if (!used_tc && tot > 0) return fail(c, RPA_ESTATE, "rpa_chi0: the tensor-core vertex kernel did not run");
+      }
       cudaEventRecord(c->ev[3], c->stream);
       double cmax = 0.0;
       RPA_TRY(cmax_of(c, n_inter, &cmax));
@@ -788,7 +779,7 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
     }
     k0 = k1;
   }
-  if (c->precision == RPA_PREC_MIXED) RPA_TRY(df_to_f64(c, s_bytes / sizeof(double)));
+  if (c->precision == RPA_PREC_MIXED) RPA_TRY(df_to_f64(c, s_bytes / sizeof(double), P.nw, cplx));
   cudaEventRecord(c->ev[5], c->stream);
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
   {
@@ -870,23 +861,16 @@ int rpa_dyson(rpa_ctx* c, double c0, double eps, double* WT_out, double* epsinv_
   std::vector<double> V;
   genV_host(c, c->last_Gcar, c0, eps, V);
   int nsing = 0, nzero = 0;
+  const double2* head = nullptr;
   cudaEventRecord(c->ev[0], c->stream);
-  RPA_TRY(dyson_fp64(c, V.data(), epsinv_out != nullptr, &nsing, &nzero));
+  RPA_TRY(dyson_fp64(c, V.data(), epsinv_out != nullptr, &nsing, &nzero, &head));
   cudaEventRecord(c->ev[1], c->stream);
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
   c->stage_ms[4] = elapsed(c, 0, 1);
   const int nwo = c->last_no - 1, np = c->nlf * c->nlf;
-  const int grid_used = (int)((c->d_tmp.bytes / sizeof(double2) - (nwo + 1)) / (3 * (size_t)np));
-  (void)grid_used;
   cudaEventRecord(c->ev[6], c->stream);
-  if (head_out) {
-    // heads live right after the per-block scratch of the Dyson kernel
-    int dev_sms = 0;
-    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device);
-    int grid = nwo < 2 * dev_sms ? nwo : 2 * dev_sms;
-    const double2* head = c->d_tmp.as<double2>() + (size_t)grid * 3 * np;
+  if (head_out)
     RPA_CUDA(c, cudaMemcpyAsync(head_out, head, sizeof(double2) * nwo, cudaMemcpyDeviceToHost, c->stream));
-  }
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
   if (WT_out || epsinv_out) {
     // d_tmp is reused for the transposes; heads were copied above

@@ -57,7 +57,7 @@ struct rpa_ctx {
   int verbose = 0;
   bool split_f16 = true;  // mixed path: fp16 (scaled) or bf16 hi/lo operands
   int tc_seg = 1;         // mixed path: chunks per TMEM accumulation segment
-  int vertex_kind = 0;    // mixed-path vertices: 0 tensor cores (MN-major), 1 FP32 CUDA cores, 2 tensor cores (K-major)
+  int vertex_kind = 0;    // mixed-path vertices: 0 tensor cores (MN-major), 1 FP32 CUDA cores (chosen by the caller)
   cudaStream_t stream = nullptr;
   std::string err;
   // a context made by rpa_create_shared borrows the G list, symmetry and basis
@@ -85,7 +85,7 @@ struct rpa_ctx {
   std::vector<int> h_npw;
   std::vector<double> h_E;        // [k][b]
   int nbp = 0;                    // bands rounded up to 8 (coefficient planes)
-  rpa::DevBuf d_npw, d_gidx, d_inv, d_coeff, d_coeff32, d_coeffs, d_cpl, d_E;
+  rpa::DevBuf d_npw, d_gidx, d_inv, d_coeff, d_coeff32, d_cpl, d_E;
 
   // k map
   int ntot = 0;
@@ -132,6 +132,9 @@ struct rpa_ctx {
   double kk_key_domega[2] = {0.0, 0.0};
   rpa::DevBuf d_kk[2], d_kkf[2];
   rpa::DevBuf d_S, d_Sdf, d_Q, d_chi0, d_kkw, d_V, d_eps, d_WT, d_flags, d_tmp;
+  // the mixed-path accumulation of the running rpa_chi0 computed only the tile
+  // pairs gi <= gj of S0 (M2 = M); the conversion to FP64 mirrors the rest
+  bool s_sym = false;
   double stage_ms[6] = {0, 0, 0, 0, 0, 0};
   long long launches = 0;  // kernels launched by this context
   double stats[4] = {0, 0, 0, 0};

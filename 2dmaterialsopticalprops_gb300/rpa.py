@@ -128,6 +128,11 @@ def load_library(path: str = LIB_PATH):
     return L
 
 
+def _check_out(a, shape, dtype, name):
+    if a.shape != tuple(shape) or a.dtype != dtype or not a.flags.c_contiguous or not a.flags.writeable:
+        raise ValueError(f"{name}: out must be a writeable contiguous {np.dtype(dtype).name} array of shape {shape}")
+
+
 def _p(a):
     return None if a is None else a.ctypes.data
 
@@ -235,14 +240,15 @@ class Context:
     """One rpa_ctx: resident basis + per-q state, Fortran-layout I/O."""
 
     def __init__(self, device: int = 0, precision: int = PREC_FP64, verbose: int = 0, split: int = 0,
-                 tc_seg: int = 0, vertex_simt: bool = False, vertex_kmajor: bool = False):
+                 tc_seg: int = 0, vertex_simt: bool = False):
         self.L = load_library()
         self.h = C.c_void_p()
         opts = RpaOpts(device=device, precision=precision, verbose=verbose, split=split)
         opts.reserved[0] = tc_seg
-        # mixed-path vertices: MN-major tensor-core kernel (default), FP32 CUDA cores,
-        # or the K-major tensor-core kernel
-        opts.reserved[1] = 1 if vertex_simt else (2 if vertex_kmajor else 0)
+        # mixed-path vertices: the tensor-core kernel (default) or, chosen
+        # explicitly, the FP32 CUDA-core kernel (bases beyond 32767 plane waves
+        # or 181 bands per k-point)
+        opts.reserved[1] = 1 if vertex_simt else 0
         rc = self.L.rpa_create(C.byref(self.h), C.byref(opts))
         if rc != RPA_OK:
             raise RpaError(rc, self.L.rpa_last_error(None).decode())
@@ -339,17 +345,27 @@ class Context:
     # -- the hot path ----------------------------------------------------------
     def chi0(self, mode: int, *, no: int, domega: float, eta: float, Vcell: float, Gcar: float, pol: str = "xx",
              ngd: int = 0, nocc: int = 0, lor_cut: float = 1e-3, df_cut: float = 1e-4, T: float = 0.0,
-             Efermi: float = 0.0, ntot_norm: int = 0, want: bool = True):
+             Efermi: float = 0.0, ntot_norm: int = 0, want: bool = True, out: tuple | None = None):
+        """S0 (and Qeff for the current mode) in the drivers' layouts.  `out`
+        may give caller-owned arrays (S0, Qeff or None) of those shapes, e.g.
+        page-locked buffers reused from call to call."""
         args = RpaChi0Args(mode=mode, pol=POL[pol], ngd=ngd, nocc=nocc, no=no, ntot_norm=ntot_norm, domega=domega,
                            eta=eta, lor_cut=lor_cut, df_cut=df_cut, T=T, Efermi=Efermi, Vcell=Vcell, Gcar=Gcar)
         nlf = self.nlf
         S0 = Q = None
-        if want:
-            if mode == MODE_CURRENT:
-                S0 = np.zeros((nlf, nlf, 2 * no + 1), dtype=np.complex128)
-                Q = np.zeros((nlf, nlf), dtype=np.complex128)
-            else:
-                S0 = np.zeros((nlf, nlf, no), dtype=np.float64)
+        cplx = mode == MODE_CURRENT
+        s_shape = (nlf, nlf, 2 * no + 1) if cplx else (nlf, nlf, no)
+        s_type = np.complex128 if cplx else np.float64
+        if out is not None:
+            S0, Q = out
+            _check_out(S0, s_shape, s_type, "chi0 S0")
+            if cplx and Q is not None:
+                _check_out(Q, (nlf, nlf), np.complex128, "chi0 Qeff")
+            if not cplx:
+                Q = None
+        elif want:
+            S0 = np.zeros(s_shape, dtype=s_type)
+            Q = np.zeros((nlf, nlf), dtype=np.complex128) if cplx else None
         self._chk(self.L.rpa_chi0(self.h, C.byref(args), _p(S0), _p(Q)))
         self.no = no
         self.mode = mode
@@ -367,11 +383,20 @@ class Context:
         self._chk(self.L.rpa_kk(self.h, variant, _p(out)))
         return out
 
-    def dyson(self, c0: float, eps: float, want_wt: bool = True, want_epsinv: bool = False, want_head: bool = True):
+    def dyson(self, c0: float, eps: float, want_wt: bool = True, want_epsinv: bool = False, want_head: bool = True,
+              out: tuple | None = None):
+        """(WT, eps^-1, eps^-1_00); `out` may give caller-owned arrays
+        (WT, eps^-1, head; None for an output not wanted)."""
         n, nw = self.nlf, self.no - 1
-        WT = np.zeros((n, n, nw), dtype=np.complex128) if want_wt else None
-        Ei = np.zeros((n, n, nw), dtype=np.complex128) if want_epsinv else None
-        head = np.zeros(nw, dtype=np.complex128) if want_head else None
+        if out is not None:
+            WT, Ei, head = out
+            for a, shp, name in ((WT, (n, n, nw), "WT"), (Ei, (n, n, nw), "eps^-1"), (head, (nw,), "head")):
+                if a is not None:
+                    _check_out(a, shp, np.complex128, "dyson " + name)
+        else:
+            WT = np.zeros((n, n, nw), dtype=np.complex128) if want_wt else None
+            Ei = np.zeros((n, n, nw), dtype=np.complex128) if want_epsinv else None
+            head = np.zeros(nw, dtype=np.complex128) if want_head else None
         rc = self.L.rpa_dyson(self.h, c0, eps, _p(WT), _p(Ei), _p(head))
         self._chk(rc)
         return WT, Ei, head
@@ -554,6 +579,29 @@ def optabs_args(s, pol: str = "xx") -> dict:
     c = s.cfg
     return dict(no=s.no, domega=s.domega, eta=s.eta, Vcell=s.Vcell, Gcar=s.Gcar, pol=pol, lor_cut=c.lor_cut,
                 df_cut=c.df_cut, T=s.T, Efermi=s.Efermi, ngd=0 if s.igk is not None else s.ngd)
+
+
+def errstats(a: np.ndarray, b: np.ndarray, floor: float = 1e-3) -> dict:
+    """Error of a against the reference b, three ways:
+    normwise    max |a - b| / max |b|;
+    rms         ||a - b||_2 / ||b||_2;
+    element     max and RMS over the elements of |a - b| / |b|, taken where
+                |b| >= floor * max |b| (elements below the floor are close to
+                zero, where a relative error says nothing about the spectrum)."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    d = np.abs(a - b)
+    mb = float(np.abs(b).max()) if b.size else 0.0
+    out = {"normwise": float(d.max() / mb) if mb > 0 else float(d.max(initial=0.0)),
+           "rms": float(np.linalg.norm(d) / max(np.linalg.norm(b), 1e-300)), "floor": floor}
+    sel = np.abs(b) >= floor * mb
+    if mb > 0 and sel.any():
+        r = d[sel] / np.abs(b[sel])
+        out.update({"elem_max": float(r.max()), "elem_rms": float(np.sqrt(np.mean(r ** 2))),
+                    "elem_n": int(sel.sum()), "n": int(b.size)})
+    else:
+        out.update({"elem_max": None, "elem_rms": None, "elem_n": 0, "n": int(b.size)})
+    return out
 
 
 def relerr(a: np.ndarray, b: np.ndarray) -> tuple[float, float]:

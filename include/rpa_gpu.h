@@ -53,8 +53,9 @@ typedef struct rpa_opts {
   int reserved[4]; /* reserved[0]: mixed path, chunks of 32 transitions summed in one
                       TMEM accumulator before read-back (0 -> 1); keep 0.
                       reserved[1]: mixed-path vertex kernel, 0 = tensor cores with
-                      MN-major operands (default), 1 = FP32 CUDA cores, 2 = tensor
-                      cores with K-major operands (transposing 4-byte gathers) */
+                      MN-major operands (default; at most 32767 plane waves and
+                      181 bands per k-point, else rpa_load_basis returns
+                      RPA_EINVAL), 1 = FP32 CUDA cores (any basis size) */
 } rpa_opts;
 
 /* Arguments of one chi0 accumulation (the namelist values the drivers use).
@@ -265,10 +266,20 @@ int rpa_kk_matrix(int variant, int no, double domega, double* K);
  *   stream : cudaStream_t (as void*) the kernels are launched on
  *   n_singular : host; if not NULL the call waits for the stream and returns
  *          the number of frequencies where gjel would stop (RPA_ESINGULAR)
- * Limits: n <= 96 (RPA_EINVAL otherwise), any nwo >= 1.  The first call on a
- * device looks up the workspace's device address with that device current;
- * make that first call before any stream capture.  Every call shares the one
- * workspace: calls that overlap on the GPU race.  Uses the current device. */
+ * Limits: n <= 96 (RPA_EINVAL otherwise), any nwo >= 1.  The kernel runs on
+ * at most 32 blocks (32 of the GPU's SMs, one frequency per block at a time),
+ * which is what the fixed workspace holds.
+ * Set-up: with CUDA's lazy module loading, the library's kernels and this
+ * workspace are put on a device at the first launch from the library there
+ * (any entry point) or at this call's first use on the device, which also
+ * looks up the workspace's device address with that device current.  That
+ * first call reserves the 13.5 MiB and can fail with RPA_ECUDA if the device
+ * is full: make it at start-up, before a framework's memory pool takes the
+ * device memory, and before any stream capture.  The address stays valid for
+ * the device's primary context; after a cudaDeviceReset do not call this
+ * entry point again in the same process.
+ * Every call shares the one workspace: calls that overlap on the GPU race.
+ * Uses the current device. */
 int rpa_dyson_noalloc(const double* chi0, const double* V, int n, int nwo, double* WT, double* head,
                       void* stream, int* n_singular);
 

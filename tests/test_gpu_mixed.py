@@ -55,6 +55,24 @@ def test_mixed_multi_tile_nlf131(synth, rpa, orc):
     ctx.close()
 
 
+def test_mixed_three_tiles_symmetric_skip(synth, rpa, orc):
+    """nlf = 250 spans three 96-row tiles: with M2 = M (xx, charge) only the
+    six tile pairs gi <= gj are accumulated and the other three are mirrored
+    (conjugated for the complex S0) when S0 is converted to FP64; the yz pair
+    (M2 != M) computes all nine."""
+    s = synth.build(synth.config_small(npw=300, nlf=250, lf="xyz", no=21))
+    ctx = rpa.Context(precision=rpa.PREC_MIXED)
+    ctx.load_system(s)
+    for pol in ("xx", "yz"):
+        S, Q = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, pol))
+        So, Qo = orc.optabs_s0(orc.Bound(s, pol=pol))
+        assert rel(S, So) < TOL
+        assert rel(Q, Qo) < TOL
+    S, _ = ctx.chi0(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+    assert rel(S, orc.sloss_s0(orc.Bound(s))) < TOL
+    ctx.close()
+
+
 def test_mixed_grid24_loss_function(synth, rpa, orc):
     s = synth.build(synth.config_grid24())
     ctx = rpa.Context(precision=rpa.PREC_MIXED)
@@ -114,13 +132,12 @@ def test_mixed_legacy_basis(synth, rpa, orc):
     ctx.close()
 
 
-@pytest.mark.parametrize("kind", ["kmajor", "simt"])
-def test_vertex_kernels_agree(synth, rpa, orc, kind):
+def test_vertex_kernels_agree(synth, rpa, orc):
     """The MN-major vertex kernel (default), the K-major tensor-core kernel and
     the FP32 CUDA-core kernel give the same S0 to the mixed-path tolerance."""
     s = synth.build(synth.config_small(nbnd=12, nocc=3, npw=120, nlf=11, no=31))
     ref = rpa.Context(precision=rpa.PREC_MIXED)
-    alt = rpa.Context(precision=rpa.PREC_MIXED, vertex_kmajor=kind == "kmajor", vertex_simt=kind == "simt")
+    alt = rpa.Context(precision=rpa.PREC_MIXED, vertex_simt=True)
     for c in (ref, alt):
         c.load_system(s)
     So = orc.sloss_s0(orc.Bound(s))

@@ -63,6 +63,10 @@ class SynthConfig:
     df_cut: float = 1.0e-4
     eps: float = 1.0e-4
     threads: int = 0
+    # decaying plane-wave envelope: coefficients scaled by exp(-|k+G|^2 / 2 sigma^2)
+    # before orthonormalisation, sigma chosen so that the envelope falls by
+    # env_decades decades from k+G = 0 to the wavefunction cutoff (0: flat)
+    env_decades: float = 0.0
 
 
 @dataclass
@@ -207,13 +211,17 @@ def tb_energies(kcart: np.ndarray, nbnd: int, nocc: int, t_ev: float, step_ev: f
     return E
 
 
-def _coeff_block(seed_seq: np.random.SeedSequence, nb: int, npw_list, npwx: int):
-    """N(0,1) complex blocks orthonormalised by Cholesky-QR (Q = Z L^-H, Z^H Z = L L^H)."""
+def _coeff_block(seed_seq: np.random.SeedSequence, nb: int, npw_list, npwx: int, env=None):
+    """N(0,1) complex blocks (times the plane-wave envelope env, (nc, npwx), if
+    given) orthonormalised by Cholesky-QR (Q = Z L^-H, Z^H Z = L L^H; the band
+    mixing keeps each plane wave's envelope)."""
     rng = np.random.default_rng(seed_seq)
     npw_list = np.asarray(npw_list)
     nc = npw_list.size
     z = rng.standard_normal((nc, npwx, nb, 2)).view(np.complex128)[..., 0]
     z[np.arange(npwx)[None, :] >= npw_list[:, None]] = 0.0
+    if env is not None:
+        z *= env[:, :, None]
     gram = np.conj(np.transpose(z, (0, 2, 1))) @ z
     L = np.linalg.cholesky(gram)
     # Q^H = L^-1 Z^H
@@ -222,13 +230,13 @@ def _coeff_block(seed_seq: np.random.SeedSequence, nb: int, npw_list, npwx: int)
 
 
 def make_coefficients(npw: np.ndarray, nbnd: int, npwx: int, seed: int, tag: int, threads: int = 0,
-                      only=None, out: np.ndarray | None = None):
+                      only=None, out: np.ndarray | None = None, env: np.ndarray | None = None):
     """Orthonormal N(0,1) coefficient blocks, seeded per chunk of 64 k-points.
 
     ``only``: IBZ indices (0-based) whose blocks are needed; the chunks holding
     them are generated (with the same values as a full build) and the rest
     stay zero.  ``out``: preallocated (nks, nbnd, npwx) complex array (e.g.
-    page-locked host memory)."""
+    page-locked host memory).  ``env``: (nks, npwx) plane-wave envelope."""
     nks = npw.size
     chunk = 64
     starts = list(range(0, nks, chunk))
@@ -240,7 +248,8 @@ def make_coefficients(npw: np.ndarray, nbnd: int, npwx: int, seed: int, tag: int
     want = None if only is None else set(int(k) // chunk for k in only)
     nth = threads or min(16, os.cpu_count() or 1)
     with _cf.ThreadPoolExecutor(max_workers=nth) as ex:
-        futs = {ex.submit(_coeff_block, ss[i], nbnd, npw[s:s + chunk], npwx): s for i, s in enumerate(starts)
+        futs = {ex.submit(_coeff_block, ss[i], nbnd, npw[s:s + chunk], npwx,
+                          None if env is None else env[s:s + chunk]): s for i, s in enumerate(starts)
                 if want is None or i in want}
         for fu in _cf.as_completed(futs):
             s = futs[fu]
@@ -332,7 +341,16 @@ def build(cfg: SynthConfig, coeff_only=None, coeff_out: np.ndarray | None = None
         only = np.unique(np.concatenate([K1[ko] - 1, K2[ko] - 1]))
     if coeff_out is not None and coeff_out.shape != (nks, cfg.nbnd, npwx):
         raise ValueError(f"coeff_out must have shape {(nks, cfg.nbnd, npwx)}")
-    coeff = make_coefficients(npw, cfg.nbnd, npwx, cfg.seed, 11, cfg.threads, only=only, out=coeff_out)
+    env = None
+    if cfg.env_decades > 0:
+        # |k+G|^2 of every basis plane wave; exp(-x / 2 sigma^2) = 10^-decades at x = ecutw
+        inv2s2 = cfg.env_decades * math.log(10.0) / ecutw
+        env = np.zeros((nks, npwx))
+        for i in range(nks):
+            gi = (igk[i, :npw[i]] - 1) if igk is not None else np.arange(npw[i])
+            kg = G[gi] + kpts[i][None, :]
+            env[i, :npw[i]] = np.exp(-inv2s2 * np.einsum("ij,ij->i", kg, kg))
+    coeff = make_coefficients(npw, cfg.nbnd, npwx, cfg.seed, 11, cfg.threads, only=only, out=coeff_out, env=env)
 
     # local fields (genGlfandParity, Sloss.f90:824-881), in G-list order:
     # lf='z' keeps G_par = 0 vectors, lf='xyz' the first nlf vectors of the list

@@ -115,3 +115,26 @@ def test_w_equals_v_times_inverse_epsilon(orc):
         assert np.allclose(E @ eps, np.eye(n), atol=1e-10)
         VE = Vm @ E
         assert np.max(np.abs(W - VE)) <= 1e-10 * np.max(np.abs(W))
+
+
+def test_dyson_conditioning_on_decayed_basis(synth, orc, rpa):
+    """On a basis whose coefficients fall by 8 decades to the cutoff, the
+    Dyson step (eps = 1 - chi0 V, gjel, W = V + V chi V; Sloss.f90:452-481)
+    amplifies a relative error of chi0 several hundred times: scaling the
+    oracle's chi0 by 1 + 1e-6 moves W by more than 1e-4 (normwise) and Im
+    eps^-1_00 by more than 1e-4 at some frequency above 1e-3 of its maximum,
+    while on the flat basis the same change moves both by a few 1e-6.  This is
+    the FP64 oracle alone (no GPU), so it is a property of the problem: any
+    chi0 carrying ~1e-6 relative error gives W errors of this size there."""
+    out = {}
+    for dec in (0.0, 8.0):
+        s = synth.build(synth.config_grid24(env_decades=dec))
+        chio = orc.kk_sloss(orc.sloss_s0(orc.Bound(s)), s.domega)
+        V = orc.genV(s)
+        W0, E0, rc0 = orc.dyson(chio, V, fast_wt=True)
+        W1, E1, rc1 = orc.dyson(np.ascontiguousarray(chio * (1.0 + 1e-6)), V, fast_wt=True)
+        assert rc0 == 0 and rc1 == 0
+        out[dec] = (rpa.errstats(W1, W0)["normwise"],
+                    rpa.errstats(E1[0, 0].imag, E0[0, 0].imag, floor=1e-3)["elem_max"])
+    assert out[0.0][0] < 1e-5 and out[0.0][1] < 1e-5
+    assert out[8.0][0] > 1e-4 and out[8.0][1] > 1e-4

@@ -60,6 +60,9 @@ def config_of(name: str, q_steps: int):
         return synth.config_grid24()
     if name == "small":
         return synth.config_small(q_steps=q_steps)
+    if name == "dyson301":  # a small k-grid with the large-W Dyson size: NGloc 301, nw 701 (profiling case)
+        return synth.config_small(nk=8, nbnd=16, nocc=6, npw=600, nlf=301, lf="xyz", no=701, omax_ev=50.0,
+                                  eta_ev=0.05, q_steps=q_steps)
     raise SystemExit(f"unknown config {name}")
 
 
@@ -138,18 +141,42 @@ class ClockSampler:
 
 # ---------------------------------------------------------------------------
 def run_step(ctx, s, rpa, host=None):
-    """One q-point: Optabs xx, Optabs zz, Sloss + Dyson.  host: dict of output buffers."""
+    """One q-point: Optabs xx, Optabs zz, Sloss + Dyson.  host: None (outputs
+    stay on the device), {} (new host arrays) or the dict alloc_outputs()
+    returns (caller-owned buffers, reused from step to step, as a driver
+    reuses its S0 / chi0 / WT arrays)."""
     want = host is not None
+    bufs = host if host else None
     out = {}
     for pol in ("xx", "zz"):
-        S0, Q = ctx.chi0(rpa.MODE_CURRENT, want=want, **rpa.optabs_args(s, pol))
-        chi = ctx.kk(rpa.KK_OPTABS_COMPLEX, want=want)
+        b = bufs[pol] if bufs else None
+        S0, Q = ctx.chi0(rpa.MODE_CURRENT, want=want, out=b[:2] if b else None, **rpa.optabs_args(s, pol))
+        chi = ctx.kk(rpa.KK_OPTABS_COMPLEX, want=want, out=b[2] if b else None)
         out[pol] = (S0, Q, chi)
-    S0, _ = ctx.chi0(rpa.MODE_CHARGE, want=want, **rpa.sloss_args(s))
-    chi = ctx.kk(rpa.KK_SLOSS_REAL, want=want)
-    WT, _, head = ctx.dyson(s.c0, s.cfg.eps, want_wt=want, want_epsinv=False, want_head=want)
+    b = bufs["loss"] if bufs else None
+    S0, _ = ctx.chi0(rpa.MODE_CHARGE, want=want, out=(b[0], None) if b else None, **rpa.sloss_args(s))
+    chi = ctx.kk(rpa.KK_SLOSS_REAL, want=want, out=b[1] if b else None)
+    WT, _, head = ctx.dyson(s.c0, s.cfg.eps, want_wt=want, want_epsinv=False, want_head=want,
+                            out=(b[2], None, b[3]) if b else None)
     out["loss"] = (S0, chi, WT, head)
     return out
+
+
+def alloc_outputs(s, pinned: bool = True):
+    """Host output buffers of one step (page-locked when pinned)."""
+    import torch
+
+    def buf(shape, dt):
+        tdt = {np.complex128: torch.complex128, np.float64: torch.float64}[dt]
+        if pinned:
+            return torch.empty(shape, dtype=tdt, pin_memory=True).numpy()
+        return np.empty(shape, dtype=dt)
+    n, no = s.nlf, s.no
+    cur = lambda: (buf((n, n, 2 * no + 1), np.complex128), buf((n, n), np.complex128),  # noqa: E731
+                   buf((n, n, no - 1), np.complex128))
+    return {"xx": cur(), "zz": cur(),
+            "loss": (buf((n, n, no), np.float64), buf((n, n, no - 1), np.complex128),
+                     buf((n, n, no - 1), np.complex128), buf((no - 1,), np.complex128))}
 
 
 def step_work(ctx, s, rpa):
@@ -192,52 +219,97 @@ def step_work(ctx, s, rpa):
     return {"acc_flops": tot_acc, "vertex_flops": tot_vert, "vertex_bytes": vbytes, "stage_ms": t, "stats": work}
 
 
-def cpu_sample(cfg_name: str, q_steps: int, budget_s: float):
-    """Times the CPU restatement (oracle, all host threads) on a k / frequency
-    sample of one q-point and extrapolates to the whole q-point (seconds)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    synth = pkg("synth")
-    cfg = config_of(cfg_name, q_steps)
-    ntot = cfg.nk * cfg.nk
-    nthreads = os.cpu_count() or 1
-    # k sample: evenly spaced FBZ points, sized from a short probe
-    rng_k = np.linspace(0, ntot - 1, num=min(ntot, 4 * nthreads)).astype(int)
-    s = synth.build(cfg, coeff_only=rng_k)
-    parts = {}
-    per_k = 0.0
-    for name, pol in (("optabs_xx", "xx"), ("optabs_zz", "zz"), ("sloss", None)):
-        b = O.Bound(s, nthreads=nthreads, klist=rng_k, pol=pol or "xx")
+class CpuSampler:
+    """The CPU restatement (oracle, all host threads) timed on samples of one
+    q-point of a workload and extrapolated to the whole q-point.
+
+    The basis is built once, holding the coefficient blocks of every k-point
+    that a sample of the run can draw; sample i times nk FBZ k-points evenly
+    spaced over the grid with an offset that moves from sample to sample (so
+    successive samples cover different k-points) for each of S0 xx / zz /
+    loss (scaled by Ntot / nk), the KK transforms on an nb x nb block of the
+    (G, G') pairs (scaled by NGloc^2 / nb^2) and the Dyson solve with the
+    reference's 4-deep W loop on nthreads frequencies (scaled by nw / nws)."""
+
+    def __init__(self, cfg_name: str, q_steps: int, nk: int | None = None, nsamples: int = 1,
+                 full: bool = False):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        self.O = O
+        synth = pkg("synth")
+        cfg = config_of(cfg_name, q_steps)
+        self.ntot = cfg.nk * cfg.nk
+        self.nthreads = os.cpu_count() or 1
+        self.full = full
+        self.nk = self.ntot if full else min(self.ntot, nk or 2 * self.nthreads)
+        self.stride = max(1, self.ntot // self.nk)
+        ks = np.unique(np.concatenate([self.klist(i) for i in range(nsamples)]))
+        self.s = synth.build(cfg, coeff_only=None if full else ks)
+
+    def klist(self, i: int) -> np.ndarray:
+        if self.full:
+            return np.arange(self.ntot)
+        return np.sort((np.arange(self.nk) * self.stride + 7 * i) % self.ntot)
+
+    def run(self, i: int = 0):
+        """(extrapolated seconds per q-point, parts, sample text, threads, wall seconds of the sample)."""
+        O, s, nthreads = self.O, self.s, self.nthreads
+        ks = self.klist(i)
+        parts = {}
+        w0 = time.perf_counter()
+        for name, pol in (("optabs_xx", "xx"), ("optabs_zz", "zz"), ("sloss", None)):
+            b = O.Bound(s, nthreads=nthreads, klist=ks, pol=pol or "xx")
+            t0 = time.perf_counter()
+            if pol:
+                O.optabs_s0(b)
+            else:
+                O.sloss_s0(b)
+            parts[name] = (time.perf_counter() - t0) / ks.size * self.ntot
+        nb = s.nlf if self.full else min(8, s.nlf)
+        So = np.random.default_rng(0).standard_normal((nb, nb, 2 * s.no + 1)) * (1 + 0j)
         t0 = time.perf_counter()
-        if pol:
-            O.optabs_s0(b)
-        else:
-            O.sloss_s0(b)
-        dt = time.perf_counter() - t0
-        parts[name] = dt / rng_k.size * ntot
-        per_k += dt / rng_k.size
-    # KK over a block of (G,G') pairs, scaled to nlf^2
-    nb = min(8, s.nlf)
-    So = np.random.default_rng(0).standard_normal((nb, nb, 2 * s.no + 1)) * (1 + 0j)
-    t0 = time.perf_counter()
-    O.kk_optabs(So, s.domega)
-    parts["kk_optabs_x2"] = 2 * (time.perf_counter() - t0) * (s.nlf ** 2) / (nb * nb)
-    Sl = np.random.default_rng(1).standard_normal((nb, nb, s.no))
-    t0 = time.perf_counter()
-    chi_blk = O.kk_sloss(Sl, s.domega)
-    parts["kk_sloss"] = (time.perf_counter() - t0) * (s.nlf ** 2) / (nb * nb)
-    # Dyson with the reference's 4-deep W loop on a frequency sample
-    nws = min(s.no - 1, nthreads)
-    chi = np.random.default_rng(2).standard_normal((s.nlf, s.nlf, nws + 0)) * 1e-3 + 0j
-    V = O.genV(s)
-    t0 = time.perf_counter()
-    O.dyson(np.ascontiguousarray(chi), V, fast_wt=False, nthreads=nthreads)
-    parts["dyson"] = (time.perf_counter() - t0) * (s.no - 1) / nws
-    total = sum(parts.values())
-    sample = (f"{rng_k.size} of {ntot} FBZ k-points for each of S0 xx/zz/loss (scaled by Ntot), "
-              f"KK on {nb}x{nb} of {s.nlf}x{s.nlf} (G,G') pairs, Dyson (4-deep WT loop) on {nws} of "
-              f"{s.no - 1} frequencies; extrapolated linearly")
-    return total, parts, sample, nthreads
+        O.kk_optabs(So, s.domega)
+        parts["kk_optabs_x2"] = 2 * (time.perf_counter() - t0) * (s.nlf ** 2) / (nb * nb)
+        Sl = np.random.default_rng(1).standard_normal((nb, nb, s.no))
+        t0 = time.perf_counter()
+        O.kk_sloss(Sl, s.domega)
+        parts["kk_sloss"] = (time.perf_counter() - t0) * (s.nlf ** 2) / (nb * nb)
+        nws = s.no - 1 if self.full else min(s.no - 1, nthreads)
+        chi = np.random.default_rng(2).standard_normal((s.nlf, s.nlf, nws)) * 1e-3 + 0j
+        V = O.genV(s)
+        t0 = time.perf_counter()
+        O.dyson(np.ascontiguousarray(chi), V, fast_wt=False, nthreads=nthreads)
+        parts["dyson"] = (time.perf_counter() - t0) * (s.no - 1) / nws
+        wall = time.perf_counter() - w0
+        total = sum(parts.values())
+        sample = (f"{ks.size} of {self.ntot} FBZ k-points for each of S0 xx/zz/loss (scaled by Ntot; offset "
+                  f"moves per sample), KK on {nb}x{nb} of {s.nlf}x{s.nlf} (G,G') pairs, Dyson (4-deep WT loop) "
+                  f"on {nws} of {s.no - 1} frequencies; extrapolated linearly")
+        return total, parts, sample, nthreads, wall
+
+
+def cpu_sample(cfg_name: str, q_steps: int, budget_s: float = 0.0):
+    """One sample of CpuSampler: (extrapolated s per q, parts, sample, threads, system)."""
+    cs = CpuSampler(cfg_name, q_steps, nk=4 * (os.cpu_count() or 1))
+    total, parts, sample, nthreads, _ = cs.run(0)
+    return total, parts, sample, nthreads, cs.s
+
+
+def cpu_validate(cfg_name: str, nsamples: int = 3):
+    """The sampled CPU estimate against a full run of the same q-point."""
+    est = []
+    cs = CpuSampler(cfg_name, 1, nsamples=nsamples)
+    for i in range(nsamples):
+        est.append(cs.run(i))
+    del cs
+    full = CpuSampler(cfg_name, 1, full=True)
+    tf, pf, sf, thr, wall = full.run(0)
+    te = float(np.mean([e[0] for e in est]))
+    return {"config": cfg_name, "threads": thr, "full_s": tf, "full_parts_s": pf, "sampled_estimate_s": te,
+            "sampled_estimates_s": [e[0] for e in est], "sample_wall_s": [e[4] for e in est],
+            "estimate_error": te / tf - 1.0,
+            "parts_error": {k: float(np.mean([e[1][k] for e in est]) / pf[k] - 1.0) for k in pf},
+            "sample": est[0][2]}
 
 
 # ---------------------------------------------------------------------------
@@ -334,8 +406,8 @@ def dispersion_path(nk: int, n_q: int):
     return [pts[i] for i in idx]
 
 
-def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, fp64_sample=(0, 31, 63), no: int = 701,
-                   eta_ev: float = 0.05):
+def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, fp64_sample=(0, 9, 18, 27, 36, 45, 54, 63),
+                   no: int = 701, eta_ev: float = 0.05, floor: float = 1e-3):
     """64-q loss-function dispersion (W and Im eps^-1 per q) on the resident
     grid120 basis: NGloc rising from 31 to 151 along the path, nw = 701 on
     0-30 eV, eta = 50 meV.  All q-points are submitted at once to a server of
@@ -368,7 +440,7 @@ def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, fp64_sample=(0, 31
     srv.close()
     # FP64 GPU sample: the same requests, one at a time on an FP64 shared context
     c64 = rpa.shared_context(parent, rpa.PREC_FP64)
-    t64, tmix_one, errs = 0.0, 0.0, []
+    t64, tmix_one, errs, stages = 0.0, 0.0, [], []
     cm = rpa.shared_context(parent)
     for qi in fp64_sample:
         r = reqs[qi]
@@ -387,10 +459,11 @@ def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, fp64_sample=(0, 31
             else:
                 tmix_one += dt
             outs.append(head)
-        d = np.abs(outs[0].imag - outs[1].imag)
+            stages.append({"wall_ms": round(1e3 * dt, 2),
+                           **{k: round(v, 2) for k, v in c.stage_times().items()}})
+        e = pkg("rpa").errstats(outs[0].imag, outs[1].imag, floor=floor)
         errs.append({"q_index": qi, "q_2pi_over_a": info[qi][0], "ngloc": info[qi][1],
-                     "max_rel_Im_epsinv": float(d.max() / np.abs(outs[1].imag).max()),
-                     "rms_rel_Im_epsinv": float(np.sqrt((d ** 2).mean()) / np.sqrt((outs[1].imag ** 2).mean()))})
+                     "Im_epsinv_00": e, "mixed_ms": stages[-2], "fp64_ms": stages[-1]})
     c64.close()
     cm.close()
     if own:
@@ -401,11 +474,17 @@ def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, fp64_sample=(0, 31
                         f"to {nslots} shared contexts",
             "n_q": n_q, "mixed_s": t_mixed, "value": n_q / t_mixed, "unit": "q-spectra/s",
             "mean_service_s": float(np.mean([x[1][2] for x in res])),
-            "fp64_sample": {"q_indices": list(fp64_sample), "fp64_s": t64, "mixed_s_one_at_a_time": tmix_one,
+            "fp64_sample": {"q_indices": list(fp64_sample), "ngloc": [info[i][1] for i in fp64_sample],
+                            "fp64_s": t64, "mixed_s_one_at_a_time": tmix_one,
                             "fp64_q_spectra_s_est": len(fp64_sample) / t64,
                             "mixed_over_fp64_same_q": t64 / tmix_one,
                             "mixed_batched_over_fp64": (n_q / t_mixed) / (len(fp64_sample) / t64),
-                            "note": "FP64 rate from the sampled q-points (NGloc 31, 91, 151), not all 64"},
+                            "note": f"FP64 rate from {len(fp64_sample)} q-points evenly spaced along the path "
+                                    f"(NGloc {info[fp64_sample[0]][1]}-{info[fp64_sample[-1]][1]}), run one at "
+                                    f"a time; the mixed rate is the batched 64-q run"},
+            "max_elem_rel_Im_epsinv_00": max(x["Im_epsinv_00"]["elem_max"] or 0.0 for x in errs),
+            "error_floor": f"element-wise relative error over frequencies with |Im eps^-1_00| >= {floor:g} "
+                           f"x its maximum; normwise = max|a-b| / max|b|; rms = ||a-b|| / ||b||",
             "errors_vs_fp64_gpu": errs}
 
 
@@ -460,10 +539,13 @@ def kmap_run(nk: int = 120, oracle_sample: int = 24):
                                        f"{ktot.shape[0]} FBZ points, scaled by the point count"}}
 
 
-def c5_run(n_q: int = 16, nk_full: int = 96, nk_check: int = 24, q_check=(1, 8), autotune: bool = True):
+def c5_run(n_q: int = 16, nk_full: int = 96, nk_check: int = 24, q_check=(1, 8), autotune: bool = True,
+           floor: float = 1e-3):
     """W(q, w) for 16 q-points at full size on the mixed path (timed), and the
-    mixed-vs-FP64 comparison (time ratio, per-q max / RMS error of Im W) on
-    the same workload with a 24x24 k-grid."""
+    mixed-vs-FP64 comparison (time ratio, per-q normwise / RMS / element-wise
+    error of Im W and Im eps^-1_00) on the q-points q_check of the same
+    workload on an nk_check x nk_check k-grid (nk_check = nk_full: the full
+    size itself, on the same resident basis)."""
     rpa, synth = pkg("rpa"), pkg("synth")
 
     def w_chain(c, s, steps):
@@ -475,26 +557,32 @@ def c5_run(n_q: int = 16, nk_full: int = 96, nk_check: int = 24, q_check=(1, 8),
         WT, _, head = c.dyson(s.c0, s.cfg.eps, want_wt=True)
         return WT, head
 
-    # mixed vs FP64 on the 24x24 grid
-    s = synth.build(c5_config(nk_check))
-    cm = rpa.Context(precision=rpa.PREC_MIXED)
-    cm.load_system(s)
-    c64 = rpa.shared_context(cm, rpa.PREC_FP64)
-    errs, tm, t64 = [], 0.0, 0.0
-    for st in q_check:
-        t = time.perf_counter()
-        Wm, hm = w_chain(cm, s, st)
-        tm += time.perf_counter() - t
-        t = time.perf_counter()
-        W6, h6 = w_chain(c64, s, st)
-        t64 += time.perf_counter() - t
-        d = np.abs(Wm.imag - W6.imag)
-        errs.append({"q_steps": st, "max_rel_Im_W": float(d.max() / np.abs(W6.imag).max()),
-                     "rms_rel_Im_W": float(np.sqrt((d ** 2).mean()) / np.sqrt((W6.imag ** 2).mean())),
-                     "max_rel_Im_epsinv": float(np.abs(hm.imag - h6.imag).max() / np.abs(h6.imag).max())})
-    c64.close()
-    cm.close()
-    del s
+    def check(cm, s):
+        c64 = rpa.shared_context(cm, rpa.PREC_FP64)
+        errs, tm, t64 = [], 0.0, 0.0
+        for st in q_check:
+            t = time.perf_counter()
+            Wm, hm = w_chain(cm, s, st)
+            tm += time.perf_counter() - t
+            t = time.perf_counter()
+            W6, h6 = w_chain(c64, s, st)
+            t64 += time.perf_counter() - t
+            errs.append({"q_steps": st, "Im_W": rpa.errstats(Wm.imag, W6.imag, floor=floor),
+                         "Im_W_00": rpa.errstats(Wm[0, 0].imag, W6[0, 0].imag, floor=floor),
+                         "Im_epsinv_00": rpa.errstats(hm.imag, h6.imag, floor=floor)})
+        c64.close()
+        return {"grid": f"{s.cfg.nk}x{s.cfg.nk}", "mixed_s": tm, "fp64_s": t64, "mixed_over_fp64": t64 / tm,
+                "errors_vs_fp64_gpu": errs,
+                "error_floor": f"element-wise relative error where |b| >= {floor:g} max|b|"}
+
+    chk = None
+    if nk_check != nk_full:
+        s = synth.build(c5_config(nk_check))
+        cm = rpa.Context(precision=rpa.PREC_MIXED)
+        cm.load_system(s)
+        chk = check(cm, s)
+        cm.close()
+        del s
     # full size, mixed path
     t0 = time.perf_counter()
     s = synth.build(c5_config(nk_full))
@@ -516,14 +604,14 @@ def c5_run(n_q: int = 16, nk_full: int = 96, nk_check: int = 24, q_check=(1, 8),
         w_chain(cm, s, st)
     t_full = time.perf_counter() - t
     st_times = cm.stage_times()
+    if nk_check == nk_full:
+        chk = check(cm, s)
     cm.close()
     return {"workload": f"large W: {nk_full}x{nk_full} k-grid, 80 bands (13 occ), ~4000 coefficients, "
                         f"NGloc=301, nw=701 on 0-50 eV, eta=50 meV, {n_q} q-points (1..{n_q} grid steps along "
                         f"Gamma-M); loss chain per q (S0, KK, FP64 Dyson, W)",
             "n_q": n_q, "mixed_s": t_full, "value": n_q / t_full, "unit": "q-spectra/s", "setup_s": t_setup,
-            "last_q_stage_ms": st_times, "autotune": tune,
-            "check": {"grid": f"{nk_check}x{nk_check}", "mixed_s": tm, "fp64_s": t64, "mixed_over_fp64": t64 / tm,
-                      "errors_vs_fp64_gpu": errs}}
+            "last_q_stage_ms": st_times, "autotune": tune, "check": chk}
 
 
 def main():
@@ -537,16 +625,20 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison step")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-validate", default=None, metavar="CONFIG",
+                    help="time the CPU restatement on a full q-point of CONFIG and compare it with its sampled estimate")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop (serving) measurement")
     ap.add_argument("--c5", action="store_true",
                     help="also run the large-W workload (96x96, 80 bands, 4000 coefficients, NGloc 301; adds minutes)")
+    ap.add_argument("--c5-check-nk", type=int, default=24,
+                    help="k-grid of the C5 mixed-vs-FP64 check (96: the full size, two q-points, ~15 min)")
     ap.add_argument("--serve-c4", action="store_true",
                     help="also run the request loop on the MoS2-like 72x72 / 40-band / 2500-coefficient basis")
     ap.add_argument("--kmap", action="store_true",
                     help="also time the k-point bookkeeping (genFBZ / findKinIBZ / findKQinBZ) on a 120x120 C6v grid")
-    ap.add_argument("--dispersion", action="store_true",
-                    help="also run the 64-q loss-function dispersion on the resident basis (adds ~2 min)")
+    ap.add_argument("--no-dispersion", action="store_true",
+                    help="skip the 64-q loss-function dispersion (mixed path batched, FP64 GPU path on 8 q-points)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -557,21 +649,34 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("gloo" if args.impl == "reference" else "nccl")
 
+    if args.cpu_validate:
+        print(json.dumps(cpu_validate(args.cpu_validate)), flush=True)
+        return
+
     if args.impl == "reference":
         if rank != 0:
             return
-        vals = []
+        cs = CpuSampler(args.config, 1, nsamples=args.warmup + args.steps)
+        vals, walls = [], []
         for i in range(args.warmup + args.steps):
-            tq, parts, sample, cores = cpu_sample(args.config, 1, args.cpu_budget)
+            tq, parts, sample, cores, wall = cs.run(i)
             if i >= args.warmup:
                 vals.append(1.0 / tq)
+                walls.append(wall)
+        s = cs.s
         v = float(np.median(vals))
-        cfg = config_of(args.config, 1)
+        cfgd = workload_desc(s, args.config)
+        cfgd.update({"l2": "n/a (CPU; per-k working sets far below the host caches' size are not the bound)",
+                     "parallelism": f"OpenMP over FBZ k-points, {cores} host threads",
+                     "precision_path": "fp64 (oracle restatement of the reference loops)"})
+        # a step is one bounded sample (a fraction of the q-point); value is the
+        # extrapolated whole-q-point rate, ms_per_step the sample's wall time
         line = {"metric": "q-point chi/W spectra/sec", "value": v, "unit": "q-spectra/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.median(walls)),
+                "q_fraction_per_step": float(np.median(walls)) * v, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
                 "impl": "reference",
-                "config": {"workload": f"{args.config} (see bench.py docstring)", "l2": "n/a (CPU)"},
+                "config": cfgd,
                 "cpu_baseline": {"value": v, "unit": "q-spectra/s", "cores": cores, "kind": "port",
                                  "sample": sample},
                 "e2e": {"value": v, "unit": "q-spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -619,41 +724,55 @@ def main():
     value = world * 1000.0 / ms
 
     e2e = None
+    out = None
     if not args.no_e2e:
+        # the basis comes from page-locked host memory every step; the step's
+        # spectra go to caller-owned page-locked buffers allocated once (as a
+        # driver reuses its output arrays from q-point to q-point)
         pinned = torch.empty(s.coeff.shape, dtype=torch.complex128, pin_memory=True)
         pc = pinned.numpy()
         pc[...] = s.coeff
-        e2e_ms = []
+        bufs = alloc_outputs(s, pinned=True)
         h2d = pc.nbytes + s.E.nbytes + s.npw.nbytes + (s.igk.nbytes if s.igk is not None else 0) + \
             s.ktot.nbytes + 5 * s.K1.nbytes + s.q.nbytes + s.ilf.nbytes + s.parG.nbytes
-        d2h = 0
+        d2h = sum(a.nbytes for v in bufs.values() for a in v)
+        e2e_ms, parts = [], {"load_basis": [], "kmap_set_q": [], "step": []}
         for i in range(1 + args.steps):
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
+            h0 = time.perf_counter()
             ctx.load_basis(s.npw, s.igk, pc, s.E)
+            h1 = time.perf_counter()
             ctx.kmap(s.ktot, s.K1, s.R1, s.K2, s.R2, s.iG0)
             ctx.set_q(s.q, s.ilf, s.parG)
-            out = run_step(ctx, s, rpa, host={})
+            h2 = time.perf_counter()
+            out = run_step(ctx, s, rpa, host=bufs)
+            h3 = time.perf_counter()
             e1.record(stream)
             torch.cuda.synchronize()
             if i > 0:
                 e2e_ms.append(e0.elapsed_time(e1))
-            if i == 0:
-                for v in out.values():
-                    for a in v:
-                        if a is not None:
-                            d2h += a.nbytes
+                for k, v in (("load_basis", h1 - h0), ("kmap_set_q", h2 - h1), ("step", h3 - h2)):
+                    parts[k].append(1e3 * v)
         ems = max_over_ranks(dist, float(np.median(e2e_ms)))
         e2e = {"value": world * 1000.0 / ems, "unit": "q-spectra/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": ems}
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": ems,
+               "parts_ms": {k: round(float(np.median(v)), 1) for k, v in parts.items()},
+               "host_buffers": "inputs and outputs page-locked, outputs allocated once and reused"}
+        # the same step once with fresh pageable output arrays (np.zeros per call,
+        # first touch of every page during the read-back): for comparison only
+        torch.cuda.synchronize()
+        h0 = time.perf_counter()
+        run_step(ctx, s, rpa, host={})
+        e2e["pageable_fresh_outputs_step_ms"] = round(1e3 * (time.perf_counter() - h0), 1)
 
     # plain FP64 GPU path on the same inputs: its time per q-point and the
     # mixed path's errors against it (one step, host outputs)
     fp64 = None
-    if args.precision == "mixed" and not args.no_fp64 and e2e is not None:
-        mixed_out = out
+    if args.precision == "mixed" and not args.no_fp64 and out is not None:
+        mixed_out = {k: tuple(None if a is None else a.copy() for a in v) for k, v in out.items()}
         ctx.close()
         ctx64 = rpa.Context(device=local, precision=rpa.PREC_FP64)
         ctx64.load_system(s)
@@ -668,13 +787,11 @@ def main():
         ms64 = f0.elapsed_time(f1)
         ctx64.close()
 
-        def err(a, b):
-            d = np.abs(a - b)
-            return {"max_rel": float(d.max() / np.abs(b).max()),
-                    "rms_rel": float(np.sqrt(np.mean(d ** 2)) / np.sqrt(np.mean(np.abs(b) ** 2)))}
+        err = rpa.errstats
         errs = {"S0_xx": err(mixed_out["xx"][0], ref["xx"][0]), "chi0_xx": err(mixed_out["xx"][2], ref["xx"][2]),
                 "S0_zz": err(mixed_out["zz"][0], ref["zz"][0]), "chi0_zz": err(mixed_out["zz"][2], ref["zz"][2]),
                 "S0_loss": err(mixed_out["loss"][0], ref["loss"][0]), "W": err(mixed_out["loss"][2], ref["loss"][2]),
+                "Im_W": err(mixed_out["loss"][2].imag, ref["loss"][2].imag),
                 "Im_epsinv_00": err(mixed_out["loss"][3].imag, ref["loss"][3].imag)}
         fp64 = {"ms_per_step": ms64, "value": 1000.0 / ms64, "unit": "q-spectra/s",
                 "mixed_over_fp64": ms64 / ms, "errors_vs_fp64_gpu": errs}
@@ -733,14 +850,14 @@ def main():
 
     cpu = None
     if not args.no_cpu and rank == 0:
-        tq, parts, sample, cores = cpu_sample(args.config, q_steps, args.cpu_budget)
+        tq, parts, sample, cores, _ = cpu_sample(args.config, q_steps, args.cpu_budget)
         cpu = {"value": 1.0 / tq, "unit": "q-spectra/s", "cores": cores, "kind": "port", "sample": sample,
                "parts_s": {k: round(v, 3) for k, v in parts.items()}}
 
     serving = disp = None
     if rank == 0 and not args.no_serve and args.precision == "mixed":
         serving = serving_run()
-    if rank == 0 and args.dispersion and args.precision == "mixed":
+    if rank == 0 and not args.no_dispersion and args.precision == "mixed" and args.config == "grid120":
         disp = dispersion_run(ctx, s)
     kmap = kmap_run() if rank == 0 and args.kmap else None
     serving_c4 = None
@@ -751,7 +868,7 @@ def main():
         if ctx is not None:
             ctx.close()
             ctx = None
-        c5 = c5_run()
+        c5 = c5_run(nk_check=args.c5_check_nk)
 
     if rank == 0:
         cfgd = workload_desc(s, args.config)

@@ -28,109 +28,11 @@
 // timeout the CTA records an error, waits (bounded) for its own MMAs, frees
 // its TMEM and returns.
 
-#include <cuda_bf16.h>
-#include <cuda_fp16.h>
+#include <algorithm>
 
-#include <cmath>
-#include <cstring>
-
-#include "rpa_internal.cuh"
-#include "tc05.cuh"
+#include "k_accum_ws.cuh"
 
 namespace rpa {
-
-struct AccTcCtx {
-  const Trans* rec;     // window-sorted interband records
-  const float2* M;      // vertices in sorted order [n_inter][nlf]
-  const float2* M2;
-  float2* Sdf;          // double-float S0 [nw][np][ncomp] (hi, lo)
-  int* status;
-  int nlf, nw, obase, wmax, n_inter;
-  double domega, eta, cut_over_eta;
-  double scaleA;        // power of two folded into w
-  float scaleB;         // power of two folded into M2
-  float inv_scale;      // 1 / (scaleA scaleB)
-  float inv_src;        // 1 / (scale of the pre-split A-side tile)
-  int nht;              // 96-row tiles of the local fields
-  int sym;              // 1: S0 is Hermitian (complex) or symmetric (real) -- M2 = M --, so only the
-                        // tile pairs gi <= gj are computed (blockIdx.y enumerates them) and the
-                        // conversion to FP64 mirrors the others
-  long long a_chunk, a_tile;  // A-side source: bytes per chunk and per tile
-  int a_lo;             // A-side source: offset of the lo rows
-  int n_rows;           // rows of M / M2 (n_inter rounded up to a multiple of 32, zero padded)
-  int seg;              // chunks accumulated in one TMEM segment before it is read back
-};
-
-constexpr int TC_TT = 32;       // transitions per chunk (K = 64 16-bit values)
-constexpr int TC_GA = 128;      // G rows per tile (MMA M)
-constexpr int TC_GB = 96;       // G' rows per tile
-constexpr int TC_FLUSH = 32;    // chunks summed in FP32 before a double-float flush
-constexpr uint32_t TC_SPINS = 1u << 16;  // suspending polls: about 1.3 s at most
-
-template <bool F16>
-__device__ __forceinline__ void split8(const float* x, uint4& hi, uint4& lo) {
-  uint32_t h[4], l[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    if (F16) {
-      __half2 hh = __floats2half2_rn(x[2 * i], x[2 * i + 1]);
-      float2 f = __half22float2(hh);
-      __half2 ll = __floats2half2_rn(x[2 * i] - f.x, x[2 * i + 1] - f.y);
-      h[i] = *reinterpret_cast<uint32_t*>(&hh);
-      l[i] = *reinterpret_cast<uint32_t*>(&ll);
-    } else {
-      __nv_bfloat162 hh = __floats2bfloat162_rn(x[2 * i], x[2 * i + 1]);
-      float2 f = __bfloat1622float2(hh);
-      __nv_bfloat162 ll = __floats2bfloat162_rn(x[2 * i] - f.x, x[2 * i + 1] - f.y);
-      h[i] = *reinterpret_cast<uint32_t*>(&hh);
-      l[i] = *reinterpret_cast<uint32_t*>(&ll);
-    }
-  }
-  hi = make_uint4(h[0], h[1], h[2], h[3]);
-  lo = make_uint4(l[0], l[1], l[2], l[3]);
-}
-
-__device__ __forceinline__ void st16(unsigned char* tile, int row, int chunk, uint4 v) {
-  *reinterpret_cast<uint4*>(tile + row * 128 + ((chunk ^ (row & 7)) << 4)) = v;
-}
-
-__device__ __forceinline__ double lorentz_tc(const AccTcCtx& A, int r, double e1, double e2, bool* in) {
-  double o = __dmul_rn((double)(r + A.obase), A.domega);
-  double dE = __dadd_rn(__dadd_rn(o, e1), -e2);
-  double den = __dadd_rn(__dmul_rn(dE, dE), __dmul_rn(A.eta, A.eta));
-  double L = __ddiv_rn(A.eta, den);
-  *in = L >= A.cut_over_eta;
-  return L;
-}
-
-__device__ int lb_lo(const Trans* rec, int n, int key) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (rec[mid].lo < key) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-
-// (hi, lo) += v in double-float arithmetic (TwoSum then Fast2Sum).
-__device__ __forceinline__ float2 df_add(float2 a, float v) {
-  float s = __fadd_rn(a.x, v);
-  float bb = __fsub_rn(s, a.x);
-  float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(v, bb));
-  float lo = __fadd_rn(a.y, e);
-  float h = __fadd_rn(s, lo);
-  float l = __fsub_rn(lo, __fsub_rn(h, s));
-  return make_float2(h, l);
-}
-
-// Pre-split B tiles of one 32-transition chunk, laid out exactly as the
-// 128-byte-swizzled K-major shared-memory tiles the MMA reads, so that a CTA
-// fetches them with one bulk copy:
-//   tile 0/1: B1 hi/lo, row G' = [ Re b | Im b ]          (b = sB * M2_t(G'))
-//   tile 2/3: B2 hi/lo, row G' = [ -Im b | Re b ]         (complex S0 only)
-// 96 rows per tile (rows >= nlf are zero), 12 KB per tile.
-constexpr uint32_t TC_TILE = TC_GB * 128;
 
 template <bool F16, bool CPLX>
 __global__ void k_presplit(const float2* __restrict__ M2, int nlf, int nchunks, int nht, float scaleB,
@@ -440,400 +342,6 @@ __global__ void __launch_bounds__(256, 1) k_accum_tc(AccTcCtx A, const unsigned 
 // No barrier in the steady state: every hand-off is an mbarrier.  Every wait
 // is bounded and gives up early once a timeout has been recorded in the shared
 // abort flag.
-constexpr int WS_SIMT_WARPS = 12;
-constexpr int WS_SIMT = 32 * WS_SIMT_WARPS;
-constexpr int WS_THREADS = WS_SIMT + 128;
-constexpr uint32_t WS_POLLS = 1u << 16;
-// register split: 384 x 152 + 128 x 56 = 65536 = 512 x 128 registers at launch (and per SM
-// sub-partition 3 x 152 x 32 + 56 x 32 = 16384)
-constexpr int WS_REG_SIMT = 152, WS_REG_PROD = 56;
-
-// Bounded wait with a growing sleep between polls, so that waiting warps give
-// their issue slots to the warps that form operands.
-__device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
-  uint32_t ns = 32;
-  for (uint32_t i = 0; i < WS_POLLS; ++i) {
-    if (tc::mbar_try_wait_ns(bar, parity, 20000u)) return true;
-    if (*abort_flag) return false;
-    __nanosleep(ns);
-    ns = ns < 256 ? 2 * ns : 256;
-  }
-  *abort_flag = 1;
-  return false;
-}
-
-template <int NIO, bool CPLX, bool SEPA>
-struct WsCfg {
-  static constexpr uint32_t A_BYTES = TC_GA * 128;                  // one 16-bit A tile
-  static constexpr uint32_t BROWS = CPLX ? 2 * TC_GB : TC_GB;       // [B1; B2] or B1
-  static constexpr uint32_t BHALF = BROWS * 128;                    // hi (or lo) rows of B
-  static constexpr uint32_t BSRC = 2 * BHALF;                       // hi, then lo
-  static constexpr uint32_t ASRC = 2 * TC_TILE;                     // separate A-side tiles (M2 != M)
-  static constexpr uint32_t REC_OFF = BSRC + (SEPA ? ASRC : 0);
-  static constexpr uint32_t DATA = (REC_OFF + TC_TT * sizeof(Trans) + 1023) / 1024 * 1024;
-  static constexpr uint32_t FORMED = NIO * 2 * A_BYTES;             // (Ah, Al) x NIO
-  static constexpr int S0 = (int)((232448 - 2 * FORMED - 1024 - 3072) / DATA);
-  static constexpr int S = S0 > 6 ? 6 : S0;
-  static constexpr size_t SMEM = (size_t)S * DATA + 2 * FORMED + 1024;
-};
-
-template <int NIO, bool CPLX, bool SEPA>
-__global__ void __launch_bounds__(WS_THREADS, 1)
-    k_accum_ws(AccTcCtx A, const unsigned char* __restrict__ tiles, const unsigned char* __restrict__ tilesA) {
-  using Cfg = WsCfg<NIO, CPLX, SEPA>;
-  constexpr int S = Cfg::S;
-  constexpr uint32_t DATA = Cfg::DATA, FORMED = Cfg::FORMED, A_BYTES = Cfg::A_BYTES;
-  constexpr uint32_t DCOLS = (CPLX ? 2 : 1) * NIO * TC_GB;  // accumulator columns per TMEM buffer
-  constexpr int CW = DCOLS / 3;                                // columns per formation thread
-  constexpr uint32_t NCOL = 2 * DCOLS <= 256 ? 256 : 512;
-  static_assert(S >= 2, "shared-memory ring too shallow");
-  static_assert(CW % 32 == 0, "accumulator layout");
-
-  extern __shared__ unsigned char smraw[];
-  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
-  unsigned char* fbase = base + S * DATA;  // formed slots
-  __shared__ uint64_t dfull[S], dfree[S], formed[2], mdone[2], tfree[2], wready[2];
-  __shared__ uint32_t tslot;
-  __shared__ __align__(16) float wtab[2][NIO][TC_TT];
-  __shared__ int range[2];
-  __shared__ volatile int abort_flag;
-
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int r0 = blockIdx.x * NIO;
-  // G tile (A rows) and G' tile (B rows), 96 local fields each
-  int gi = blockIdx.y, gj = blockIdx.z;
-  if (A.sym) {
-    // blockIdx.y enumerates the pairs gi <= gj row by row
-    int p = blockIdx.y;
-    gi = 0;
-    while (p >= A.nht - gi) {
-      p -= A.nht - gi;
-      ++gi;
-    }
-    gj = gi + p;
-  }
-  const int nrowA = min(TC_GB, A.nlf - gi * TC_GB);
-  const size_t np = (size_t)A.nlf * A.nlf;
-
-  if (warp == 0) {
-    tc::tmem_alloc(&tslot, NCOL);
-    tc::tmem_relinquish();
-  }
-  if (tid == 0) {
-    for (int i = 0; i < S; ++i) {
-      tc::mbar_init(&dfull[i], 1);
-      tc::mbar_init(&dfree[i], WS_SIMT_WARPS + 2);  // formation warps, the weights warp, the MMA commit
-    }
-    for (int i = 0; i < 2; ++i) {
-      tc::mbar_init(&formed[i], WS_SIMT_WARPS);
-      tc::mbar_init(&mdone[i], 1);
-      tc::mbar_init(&tfree[i], WS_SIMT_WARPS);
-      tc::mbar_init(&wready[i], 1);
-    }
-    tc::fence_mbar_init();
-    abort_flag = 0;
-    range[0] = lb_lo(A.rec, A.n_inter, r0 - A.wmax + 1) & ~(TC_TT - 1);
-    range[1] = lb_lo(A.rec, A.n_inter, r0 + NIO);
-  }
-  // A padding rows (G >= nlf) stay zero for the whole kernel
-  for (uint32_t e = tid; e < 2 * FORMED / 16; e += WS_THREADS)
-    reinterpret_cast<uint4*>(fbase)[e] = make_uint4(0, 0, 0, 0);
-  tc::fence_async_smem();
-  tc::tc_fence_before();
-  __syncthreads();
-  tc::tc_fence_after();
-  const uint32_t taddr = tslot;
-  const int ta = range[0], tb = range[1];
-  const int nchunks = (tb - ta + TC_TT - 1) / TC_TT;
-  const int chunk0 = ta / TC_TT;
-  // Step c of every CTA handles the chunk of its range congruent to c modulo
-  // the range length, so CTAs of neighbouring frequency rows (whose ranges
-  // overlap almost entirely) read each chunk at the same time and it is
-  // fetched from DRAM about once per wave.
-  const int rot = nchunks > 0 ? ((-chunk0) % nchunks + nchunks) % nchunks : 0;
-  auto phys = [&](int c) { const int p = c + rot; return p >= nchunks ? p - nchunks : p; };
-
-  auto stage = [&](int c) { return base + (size_t)(c % S) * DATA; };
-  auto slot = [&](int c) { return fbase + (size_t)(c & 1) * FORMED; };
-  bool ok = true;
-
-  if (warp >= WS_SIMT_WARPS) {
-    // ---------------- producer / MMA issuer ----------------
-    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(WS_REG_PROD));
-    if (warp == WS_SIMT_WARPS + 2 && lane == 0) {
-      // ---------------- loads: a stage is refilled as soon as it is released ----------------
-      constexpr uint32_t bytes = Cfg::BSRC + (SEPA ? Cfg::ASRC : 0) + TC_TT * sizeof(Trans);
-      int loaded = 0;
-      for (; loaded < nchunks && ok; ++loaded) {
-        if (loaded >= S) ok = ws_wait(&dfree[loaded % S], ((loaded / S) - 1) & 1, &abort_flag);
-        if (!ok) break;
-        unsigned char* st = stage(loaded);
-        uint64_t* b = &dfull[loaded % S];
-        tc::mbar_arrive_expect_tx(b, bytes);
-        const int pc = phys(loaded);
-        tc::bulk_g2s(st, tiles + ((size_t)(chunk0 + pc) * A.nht + gj) * Cfg::BSRC, Cfg::BSRC, b);
-        if (SEPA) {
-          const unsigned char* as = tilesA + (size_t)(chunk0 + pc) * A.a_chunk + (size_t)gi * A.a_tile;
-          tc::bulk_g2s(st + Cfg::BSRC, as, TC_TILE, b);
-          tc::bulk_g2s(st + Cfg::BSRC + TC_TILE, as + A.a_lo, TC_TILE, b);
-        }
-        tc::bulk_g2s(st + Cfg::REC_OFF, A.rec + ta + (size_t)pc * TC_TT, TC_TT * sizeof(Trans), b);
-      }
-      if (!ok) {
-        abort_flag = 1;
-        // bounded wait for the copies in flight before shared memory is released
-        for (int c = (loaded > S ? loaded - S : 0); c < loaded; ++c) tc::mbar_wait(&dfull[c % S], (c / S) & 1, 1024);
-      }
-    }
-    if (warp == WS_SIMT_WARPS && lane == 0) {
-      // ---------------- MMA issue ----------------
-      int issued = 0;
-      const uint32_t idesc = tc::idesc_bf16(TC_GA, CPLX ? 2 * TC_GB : TC_GB, true);
-      for (int c = 0; c < nchunks && ok; ++c) {
-        ok = ws_wait(&formed[c & 1], (c >> 1) & 1, &abort_flag);
-        // an even chunk opens segment c / 2 in TMEM buffer (c / 2) % 2, whose
-        // previous segment must have been read back
-        if (ok && (c & 1) == 0 && c >= 4) {
-          const int sg = (c >> 1) - 2;
-          ok = ws_wait(&tfree[sg & 1], (sg >> 1) & 1, &abort_flag);
-        }
-        if (!ok) break;
-        tc::tc_fence_after();
-        const uint32_t bh = tc::smem_u32(stage(c)), bl = bh + Cfg::BHALF;
-        const uint32_t as = tc::smem_u32(slot(c));
-        const uint32_t d0 = taddr + (uint32_t)(((c >> 1) & 1) * DCOLS);
-        const uint32_t first = (c & 1) ? 1u : 0u;
-#pragma unroll
-        for (int j = 0; j < NIO; ++j) {
-          const uint32_t ah = as + j * 2 * A_BYTES, al = ah + A_BYTES;
-          const uint32_t d = d0 + (uint32_t)(j * TC_GB);
-          // cross products first, the large hi * hi products last
-#pragma unroll
-          for (int ks = 0; ks < 4; ++ks) {
-            const uint32_t ko = ks * 32;
-            tc::mma_bf16(d, tc::desc_sw128(ah + ko), tc::desc_sw128(bl + ko), idesc, ks > 0 ? 1u : first);
-            tc::mma_bf16(d, tc::desc_sw128(al + ko), tc::desc_sw128(bh + ko), idesc, 1u);
-          }
-#pragma unroll
-          for (int ks = 0; ks < 4; ++ks) {
-            const uint32_t ko = ks * 32;
-            tc::mma_bf16(d, tc::desc_sw128(ah + ko), tc::desc_sw128(bh + ko), idesc, 1u);
-          }
-        }
-        tc::mma_commit(&mdone[c & 1]);
-        tc::mma_commit(&dfree[c % S]);
-        issued = c + 1;
-      }
-      if (!ok) {
-        atomicExch(A.status, 1);
-        abort_flag = 1;
-        // bounded drain of this CTA's own MMAs
-        if (issued > 0) tc::mbar_wait(&mdone[(issued - 1) & 1], ((issued - 1) >> 1) & 1, 1024);
-      }
-    }
-    if (warp == WS_SIMT_WARPS + 1) {
-      // ---------------- Lorentzian weights ----------------
-      for (int c = 0; c < nchunks && ok; ++c) {
-        ok = ws_wait(&dfull[c % S], (c / S) & 1, &abort_flag);
-        if (ok && c >= 2) ok = ws_wait(&formed[c & 1], ((c - 2) >> 1) & 1, &abort_flag);  // wtab[c % 2] read
-        ok = __all_sync(0xffffffffu, ok);
-        if (!ok) break;
-        const Trans* rec = reinterpret_cast<const Trans*>(stage(c) + Cfg::REC_OFF);
-        const int t = ta + phys(c) * TC_TT + lane;
-        const Trans& R = rec[lane];
-        const double dE0 = R.e1 - R.e2;
-        const float cs = (float)(R.c * A.scaleA) * A.inv_src;
-        const float eta = (float)A.eta;
-#pragma unroll
-        for (int j = 0; j < NIO; ++j) {
-          // window membership is the exact [lo, hi] of the record
-          const int r = r0 + j;
-          float w = 0.f;
-          if (t < tb && r < A.nw && r >= R.lo && r <= R.hi) {
-            const float dE = (float)fma((double)(r + A.obase), A.domega, dE0);
-            w = cs * (eta / fmaf(dE, dE, eta * eta));
-          }
-          wtab[c & 1][j][lane] = w;
-        }
-        __syncwarp();
-        if (lane == 0) {
-          tc::mbar_arrive(&wready[c & 1]);
-          tc::mbar_arrive(&dfree[c % S]);
-        }
-      }
-      if (!ok) abort_flag = 1;
-    }
-  } else {
-    // ---------------- read-back, weights, A formation ----------------
-    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(WS_REG_SIMT));
-    // accumulator slice: TMEM lane quadrant wq, columns cg * CW .. cg * CW + CW - 1
-    const int wq = warp & 3, cg = warp >> 2;
-    const int grow = wq * 32 + lane;       // row of the G tile
-    const int gG = gi * TC_GB + grow;      // G
-    float acc[CW];
-#pragma unroll
-    for (int i = 0; i < CW; ++i) acc[i] = 0.f;
-    int consumed = 0;
-    auto consume = [&](int buf) {
-      const uint32_t a0 = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)(buf * DCOLS + cg * CW);
-#pragma unroll
-      for (int p = 0; p < CW / 32; ++p) {
-        float v[32];
-        tc::tmem_ld32(a0 + 32 * p, v);
-        tc::tmem_ld_wait();
-#pragma unroll
-        for (int i = 0; i < 32; ++i) acc[32 * p + i] += v[i];
-      }
-    };
-    // column col of the accumulator = (part, G'): part = Re / Im (complex) or
-    // the frequency row of the pair (real)
-    auto flush = [&]() {
-      if (grow < TC_GB && gG < A.nlf) {
-        const int ncomp = CPLX ? 2 : 1;
-#pragma unroll
-        for (int j0 = 0; j0 < CW; j0 += 4) {
-          float2* dst[4];
-          float2 old[4];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int col = cg * CW + j0 + j, part = col / TC_GB, gp = gj * TC_GB + col - part * TC_GB;
-            const int io = CPLX ? r0 : r0 + part, comp = CPLX ? part : 0;
-            dst[j] = (gp < A.nlf && io < A.nw)
-                         ? A.Sdf + ((size_t)io * np + (size_t)gG + (size_t)A.nlf * gp) * ncomp + comp
-                         : nullptr;
-            if (dst[j]) old[j] = *dst[j];
-          }
-#pragma unroll
-          for (int j = 0; j < 4; ++j)
-            if (dst[j]) *dst[j] = df_add(old[j], acc[j0 + j] * A.inv_scale);
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < CW; ++j) acc[j] = 0.f;
-    };
-    for (int c = 0; c < nchunks; ++c) {
-      ok = ws_wait(&dfull[c % S], (c / S) & 1, &abort_flag);
-      if (ok && c >= 2) ok = ws_wait(&mdone[c & 1], ((c - 2) >> 1) & 1, &abort_flag);
-      ok = __all_sync(0xffffffffu, ok);
-      unsigned char* st = stage(c);
-      unsigned char* fs = slot(c);
-      // chunk c-2 done: its slot is free, and for odd c it closed segment
-      // (c - 3) / 2, which is read back now
-      if (ok && c >= 3 && (c & 1)) {
-        const int sg = (c - 3) >> 1;
-        tc::tc_fence_after();
-        consume(sg & 1);
-        tc::tc_fence_before();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&tfree[sg & 1]);
-        if (++consumed % TC_FLUSH == 0) flush();
-      }
-      if (ok) ok = __all_sync(0xffffffffu, ws_wait(&wready[c & 1], (c >> 1) & 1, &abort_flag));
-      if (!ok) break;
-      // A tiles: A = w * (hi + lo) of the staged vertex tile (B1 rows, or the
-      // separate A-side tile), re-split
-      const unsigned char* srch = st + (SEPA ? Cfg::BSRC : 0);
-      const unsigned char* srcl = srch + (SEPA ? TC_TILE : Cfg::BHALF);
-#pragma unroll 2
-      for (int e = tid; e < nrowA * 8; e += WS_SIMT) {
-        const int row = e >> 3, ch = e & 7;
-        const uint32_t off = (uint32_t)row * 128u + ((uint32_t)(ch ^ (row & 7)) << 4);
-        const uint4 h = *reinterpret_cast<const uint4*>(srch + off);
-        const uint4 l = *reinterpret_cast<const uint4*>(srcl + off);
-        float x[8];
-        const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {l.x, l.y, l.z, l.w};
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const float2 fh = __half22float2(*reinterpret_cast<const __half2*>(&hw[i]));
-          const float2 fl = __half22float2(*reinterpret_cast<const __half2*>(&lw[i]));
-          x[2 * i] = fh.x + fl.x;
-          x[2 * i + 1] = fh.y + fl.y;
-        }
-        const int tt0 = (ch & 3) * 8;
-#pragma unroll
-        for (int j = 0; j < NIO; ++j) {
-          const float4 w0 = *reinterpret_cast<const float4*>(&wtab[c & 1][j][tt0]);
-          const float4 w1 = *reinterpret_cast<const float4*>(&wtab[c & 1][j][tt0 + 4]);
-          const float y[8] = {x[0] * w0.x, x[1] * w0.y, x[2] * w0.z, x[3] * w0.w,
-                              x[4] * w1.x, x[5] * w1.y, x[6] * w1.z, x[7] * w1.w};
-          uint4 hi, lo;
-          split8<true>(y, hi, lo);
-          *reinterpret_cast<uint4*>(fs + j * 2 * A_BYTES + off) = hi;
-          *reinterpret_cast<uint4*>(fs + j * 2 * A_BYTES + A_BYTES + off) = lo;
-        }
-      }
-      tc::fence_async_smem();
-      __syncwarp();
-      if (lane == 0) {
-        tc::mbar_arrive(&formed[c & 1]);
-        tc::mbar_arrive(&dfree[c % S]);
-      }
-    }
-    // drain: read back the segments the loop did not reach
-    if (ok) {
-      const int nseg = (nchunks + 1) / 2, ncons = nchunks >= 3 ? (nchunks - 2) / 2 : 0;
-      for (int sg = ncons; sg < nseg && ok; ++sg) {
-        const int cl = min(2 * sg + 1, nchunks - 1);
-        ok = __all_sync(0xffffffffu, ws_wait(&mdone[cl & 1], (cl >> 1) & 1, &abort_flag));
-        if (!ok) break;
-        tc::tc_fence_after();
-        consume(sg & 1);
-      }
-      if (ok) flush();
-    }
-    if (!ok) {
-      atomicExch(A.status, 1);
-      abort_flag = 1;
-    }
-  }
-  tc::tc_fence_before();
-  __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
-}
-
-// Pre-split B operand of the warp-specialised kernel, per chunk and 96-row
-// tile of G': the hi rows, then the lo rows; rows 0-95 = [Re b | Im b] (B1),
-// rows 96-191 = [-Im b | Re b] (B2, complex S0 only), b = scale * M(G'),
-// rows with G' >= nlf zero.
-template <bool CPLX>
-__global__ void k_presplit_ws(const float2* __restrict__ M, int nlf, int nchunks, int nht, float scale,
-                              unsigned char* __restrict__ tiles) {
-  constexpr uint32_t BROWS = CPLX ? 2 * TC_GB : TC_GB, BHALF = BROWS * 128;
-  const long long ntask = (long long)nchunks * nht * TC_GB * 4;
-  for (long long task = blockIdx.x * (long long)blockDim.x + threadIdx.x; task < ntask;
-       task += (long long)gridDim.x * blockDim.x) {
-    const long long cht = task / (TC_GB * 4);
-    const int rem = (int)(task % (TC_GB * 4));
-    const int ch = (int)(cht / nht), ht = (int)(cht % nht);
-    // the four 16-byte groups of a row on neighbouring threads: every warp
-    // store fills whole 32-byte sectors of eight rows
-    const int row = rem >> 2, grp = rem & 3, g = ht * TC_GB + row;
-    float re[8], im[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      float2 m = g < nlf ? M[((size_t)ch * TC_TT + grp * 8 + q) * nlf + g] : make_float2(0.f, 0.f);
-      re[q] = m.x * scale;
-      im[q] = m.y * scale;
-    }
-    unsigned char* t = tiles + (size_t)cht * 2 * BHALF;
-    uint4 rh, rl, ih, il;
-    split8<true>(re, rh, rl);
-    split8<true>(im, ih, il);
-    st16(t, row, grp, rh);
-    st16(t + BHALF, row, grp, rl);
-    st16(t, row, 4 + grp, ih);
-    st16(t + BHALF, row, 4 + grp, il);
-    if (CPLX) {
-      const uint32_t sg = 0x80008000u;  // split(-x) = -split(x)
-      const int r2 = TC_GB + row;
-      st16(t, r2, grp, make_uint4(ih.x ^ sg, ih.y ^ sg, ih.z ^ sg, ih.w ^ sg));
-      st16(t + BHALF, r2, grp, make_uint4(il.x ^ sg, il.y ^ sg, il.z ^ sg, il.w ^ sg));
-      st16(t, r2, 4 + grp, rh);
-      st16(t + BHALF, r2, 4 + grp, rl);
-    }
-  }
-}
-
 __global__ void k_cmax(const Trans* __restrict__ rec, int n, unsigned long long* cmax) {
   double mx = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) mx = fmax(mx, fabs(rec[i].c));
@@ -886,26 +394,6 @@ static int launch_tc(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char*
   return RPA_OK;
 }
 
-template <int NIO, bool CPLX, bool SEPA>
-static int launch_ws(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char* tiles, const unsigned char* tilesA) {
-  using Cfg = WsCfg<NIO, CPLX, SEPA>;
-  auto kern = k_accum_ws<NIO, CPLX, SEPA>;
-  RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
-  dim3 grid((nw + NIO - 1) / NIO, A.sym ? A.nht * (A.nht + 1) / 2 : A.nht, A.sym ? 1 : A.nht);
-  kern<<<grid, WS_THREADS, Cfg::SMEM, c->stream>>>(A, tiles, tilesA);
-  RPA_CUDA(c, cudaGetLastError());
-  ++c->launches;
-  return RPA_OK;
-}
-
-template <bool CPLX>
-static int launch_presplit_ws(rpa_ctx* c, const float2* M, int nchunks, int nht, float scale, unsigned char* tiles) {
-  k_presplit_ws<CPLX><<<4096, 256, 0, c->stream>>>(M, c->nlf, nchunks, nht, scale, tiles);
-  RPA_CUDA(c, cudaGetLastError());
-  ++c->launches;
-  return RPA_OK;
-}
-
 template <bool F16, bool CPLX>
 static int launch_presplit(rpa_ctx* c, const float2* M2, int nchunks, float scaleB, unsigned char* tiles) {
   const int nht = (c->nlf + TC_GB - 1) / TC_GB;
@@ -915,7 +403,57 @@ static int launch_presplit(rpa_ctx* c, const float2* M2, int nchunks, float scal
   return RPA_OK;
 }
 
+
 static double pow2_floor(double x) { return std::ldexp(1.0, (int)std::floor(std::log2(x))); }
+
+// Cost model of a tile variant, in issue cycles per chunk summed over the
+// CTAs of one launch: per CTA and 32-transition chunk the MMAs take ~6 cycles
+// per accumulator column (three split products, four K steps of N = NC GB per
+// row) and the formation ~8 cycles per valid A row per row, overlapped, plus
+// ~200 cycles of hand-off; a launch has ceil(nw / NIO) x (tile pairs) CTAs.
+static double acc_model_cost(bool cplx, int nlf, int nw, AccVariant v) {
+  const int nht = (nlf + v.gb - 1) / v.gb;
+  v.nio = ws_fit_nio(v.nio, cplx, nht > 1, v.gb);
+  const double pairs = nht > 1 ? 0.5 * nht * (nht + 1) : 1.0;
+  const double rows_avg = (double)nlf / nht;
+  const double mma = 6.0 * v.nio * (cplx ? 2 : 1) * v.gb, form = 8.0 * v.nio * std::min<double>(v.gb, rows_avg);
+  return std::ceil((double)nw / v.nio) * pairs * (std::max(mma, form) + 200.0);
+}
+
+// Tile variant of an accumulation: forced for the context (opts.reserved[2] or
+// the autotuner's trial), the autotuner's table entry for (S0 kind, NGloc,
+// nw / 64), else the cheapest variant of the cost model.  The yz / zy pair
+// (M2 != M) keeps the default 96-row tiles.
+static AccVariant acc_variant(rpa_ctx* c, int nw, bool cplx, bool two) {
+  if (two) return {TC_GB, 1};
+  if (c->acc_force.gb > 0) return {c->acc_force.gb, c->acc_force.nio};
+  const auto it = c->acc_table.find(acc_tune_key(cplx, c->nlf, nw));
+  if (it != c->acc_table.end()) return {it->second.gb, it->second.nio};
+  const AccVariant* list = cplx ? ACC_VARIANTS_COMPLEX : ACC_VARIANTS_REAL;
+  const int n = cplx ? (int)(sizeof ACC_VARIANTS_COMPLEX / sizeof(AccVariant))
+                     : (int)(sizeof ACC_VARIANTS_REAL / sizeof(AccVariant));
+  AccVariant best = list[0];
+  double bc = acc_model_cost(cplx, c->nlf, nw, best);
+  for (int i = 1; i < n; ++i) {
+    const double k = acc_model_cost(cplx, c->nlf, nw, list[i]);
+    if (k < 0.9 * bc) {  // the default unless a variant is clearly cheaper
+      bc = k;
+      best = list[i];
+    }
+  }
+  return best;
+}
+
+int acc_variant_list(bool cplx, int* gb, int* nio, int cap) {
+  const AccVariant* list = cplx ? ACC_VARIANTS_COMPLEX : ACC_VARIANTS_REAL;
+  const int n = cplx ? (int)(sizeof ACC_VARIANTS_COMPLEX / sizeof(AccVariant))
+                     : (int)(sizeof ACC_VARIANTS_REAL / sizeof(AccVariant));
+  for (int i = 0; i < n && i < cap; ++i) {
+    gb[i] = list[i].gb;
+    nio[i] = list[i].nio;
+  }
+  return n;
+}
 
 // Interband accumulation of one k-chunk into the double-float S0 (d_Sdf).
 int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const float2* Mf, const float2* Mf2,
@@ -949,21 +487,22 @@ int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const fl
   const int nht = (c->nlf + TC_GB - 1) / TC_GB;
   const bool two = Mf2 != Mf;
   if (f16 && A.seg == 1) {
-    // warp-specialised kernel on 96-row tiles of G and G'.  The A side reads
-    // the B1 rows of the same stage when there is one tile and M2 = M, else
-    // its own pre-split source tile (the B tiles of tile gi, or a pre-split
-    // copy of M for the yz / zy pair).
-    const size_t bsrc = (size_t)(cplx ? 4 : 2) * TC_TILE;
-    RPA_TRY(ensure(c, c->d_tiles, (size_t)nch * nht * bsrc));
+    // warp-specialised kernel on G-tiles of v.gb rows.  The A side reads the
+    // B1 rows of the same stage when there is one tile and M2 = M, else its
+    // own pre-split source tile (the B tiles of tile gi, or a pre-split copy
+    // of M for the yz / zy pair, which keeps the 96-row default tile).
+    const AccVariant v = acc_variant(c, P.nw, cplx, two);
+    const int gb = v.gb, nhv = (c->nlf + gb - 1) / gb;
+    const size_t tile = (size_t)gb * 128, bsrc = (size_t)(cplx ? 4 : 2) * tile;
+    RPA_TRY(ensure(c, c->d_tiles, (size_t)nch * nhv * bsrc));
     unsigned char* tiles = c->d_tiles.as<unsigned char>();
-    RPA_TRY(cplx ? launch_presplit_ws<true>(c, Mf2, nch, nht, A.scaleB, tiles)
-                 : launch_presplit_ws<false>(c, Mf2, nch, nht, A.scaleB, tiles));
+    RPA_TRY(presplit_ws_tiles(c, cplx, gb, Mf2, nch, nhv, A.scaleB, tiles));
     const unsigned char* tilesA = tiles;
-    A.nht = nht;
+    A.nht = nhv;
     A.inv_src = 1.0f / A.scaleB;
-    A.a_chunk = (long long)nht * bsrc;
+    A.a_chunk = (long long)nhv * bsrc;
     A.a_tile = (long long)bsrc;
-    A.a_lo = (cplx ? 2 : 1) * TC_TILE;
+    A.a_lo = (cplx ? 2 : 1) * (int)tile;
     if (two) {
       const double amS = (double)amaxM * 1.5;
       const float sM = amS > 0 ? (float)(16384.0 / pow2_floor(amS)) : 1.0f;
@@ -975,11 +514,14 @@ int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const fl
       A.a_tile = 2 * TC_TILE;
       A.a_lo = TC_TILE;
     }
-    const bool sepa = two || nht > 1;
-    A.sym = (!two && nht > 1) ? 1 : 0;
+    const bool sepa = two || nhv > 1;
+    A.sym = (!two && nhv > 1) ? 1 : 0;
     c->s_sym = A.sym != 0;
-    if (cplx) return sepa ? launch_ws<1, true, true>(c, A, P.nw, tiles, tilesA) : launch_ws<1, true, false>(c, A, P.nw, tiles, tilesA);
-    return sepa ? launch_ws<1, false, true>(c, A, P.nw, tiles, tilesA) : launch_ws<2, false, false>(c, A, P.nw, tiles, tilesA);
+    c->s_gb = gb;
+    c->acc_last_gb = gb;
+    c->acc_last_nio = ws_fit_nio(v.nio, cplx, sepa, gb);
+    return cplx ? launch_ws_complex(c, A, P.nw, sepa, gb, v.nio, tiles, tilesA)
+                : launch_ws_real(c, A, P.nw, sepa, gb, v.nio, tiles, tilesA);
   }
   const size_t tbytes = (size_t)nch * nht * (cplx ? 4 : 2) * TC_TILE;
   RPA_TRY(ensure(c, c->d_tiles, tbytes));
@@ -1059,10 +601,10 @@ int df_to_f64(rpa_ctx* c, size_t n, int nw, bool cplx) {
   if (c->s_sym) {
     if (cplx)
       k_df_to_f64_sym<true><<<2048, 256, 0, c->stream>>>(c->d_Sdf.as<float2>(), c->d_S.as<double>(), nw, c->nlf,
-                                                         TC_GB);
+                                                         c->s_gb);
     else
       k_df_to_f64_sym<false><<<2048, 256, 0, c->stream>>>(c->d_Sdf.as<float2>(), c->d_S.as<double>(), nw, c->nlf,
-                                                          TC_GB);
+                                                          c->s_gb);
   } else {
     k_df_to_f64<<<2048, 256, 0, c->stream>>>(c->d_Sdf.as<float2>(), c->d_S.as<double>(), n);
   }

@@ -290,6 +290,10 @@ int rpa_create(rpa_ctx** out, const rpa_opts* opts) {
   c->split_f16 = opts ? opts->split == 0 : true;
   c->tc_seg = (opts && opts->reserved[0] > 0) ? opts->reserved[0] : 1;
   c->vertex_kind = (opts && opts->reserved[1] == 1) ? 1 : 0;
+  if (opts && opts->reserved[2] > 0) {
+    c->acc_force.gb = opts->reserved[2] & 255;
+    c->acc_force.nio = opts->reserved[2] >> 8;
+  }
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete c;
@@ -324,6 +328,8 @@ int rpa_create_shared(rpa_ctx** out, rpa_ctx* parent, int precision) {
   c->tc_seg = parent->tc_seg;
   c->vertex_kind = parent->vertex_kind;
   c->vt_table = parent->vt_table;
+  c->acc_table = parent->acc_table;
+  c->acc_force = parent->acc_force;
   c->nbp = parent->nbp;
   c->ng = parent->ng;
   c->h_miller = parent->h_miller;
@@ -678,6 +684,7 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
   const size_t s_bytes = (size_t)P.nw * np * (cplx ? 16 : 8);
   RPA_TRY(ensure(c, c->d_S, s_bytes));
   c->s_sym = false;
+  c->acc_last_gb = c->acc_last_nio = 0;
   RPA_TRY(ensure(c, c->d_Q, sizeof(double2) * np));
   RPA_CUDA(c, cudaMemsetAsync(c->d_S.p, 0, s_bytes, c->stream));
   if (c->precision == RPA_PREC_MIXED) {
@@ -929,6 +936,13 @@ int rpa_kk_matrix(int variant, int no, double domega, double* K) {
 int rpa_stage_times(const rpa_ctx* c, double* ms6) {
   if (!c || !ms6) return RPA_EINVAL;
   for (int i = 0; i < 6; ++i) ms6[i] = c->stage_ms[i];
+  return RPA_OK;
+}
+
+int rpa_accum_tile(const rpa_ctx* c, int* gb, int* nio) {
+  if (!c || !gb || !nio) return RPA_EINVAL;
+  *gb = c->acc_last_gb;
+  *nio = c->acc_last_nio;
   return RPA_OK;
 }
 

@@ -126,6 +126,17 @@ struct rpa_ctx {
   VtxTune vt_cur;
   bool vt_forced = false;
   std::map<long long, VtxTune> vt_table;
+  // mixed-path accumulation tile (G-tile rows gb, frequency rows per CTA nio):
+  // forced for every call (opts.reserved[2], or the autotuner's trial; gb = 0:
+  // not forced) and the table rpa_autotune fills, keyed by (S0 kind, NGloc,
+  // nw / 64); the variant the last accumulation used
+  struct AccTune {
+    int gb = 0, nio = 0;
+    double ms = 0.0;
+  };
+  AccTune acc_force;
+  std::map<long long, AccTune> acc_table;
+  int acc_last_gb = 0, acc_last_nio = 0;
   // fixed KK kernels on the device, one slot per variant (Optabs, Sloss): FP64
   // and FP32 copies and the (no, domega) each was built for (no = 0: empty)
   int kk_key_no[2] = {0, 0};
@@ -135,6 +146,7 @@ struct rpa_ctx {
   // the mixed-path accumulation of the running rpa_chi0 computed only the tile
   // pairs gi <= gj of S0 (M2 = M); the conversion to FP64 mirrors the rest
   bool s_sym = false;
+  int s_gb = 96;  // G-tile rows of that accumulation
   double stage_ms[6] = {0, 0, 0, 0, 0, 0};
   long long launches = 0;  // kernels launched by this context
   double stats[4] = {0, 0, 0, 0};
@@ -187,6 +199,15 @@ struct Chi0Plan {
 };
 
 int build_gfast(rpa_ctx* c, int ik, int nsum_legacy, int* out);
+
+// tile variants (G-tile rows, frequency rows per CTA) of the warp-specialised
+// accumulation for the complex or real S0; returns their number
+int acc_variant_list(bool cplx, int* gb, int* nio, int cap);
+
+// key of the accumulation tuning table: (S0 kind, NGloc, nw / 64)
+inline long long acc_tune_key(bool cplx, int nlf, int nw) {
+  return (long long)(cplx ? 1 : 0) | ((long long)nlf << 1) | ((long long)(nw / 64) << 16);
+}
 
 // key of the vertex tuning table: (mode, nbnd, nocc, NGloc / 32)
 inline long long vtx_tune_key(int mode, int nbnd, int nocc, int nlf) {

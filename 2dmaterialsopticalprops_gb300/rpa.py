@@ -24,7 +24,7 @@ KK_OPTABS_COMPLEX, KK_SLOSS_REAL = 1, 2
 
 EXPORTS = ["rpa_create", "rpa_destroy", "rpa_last_error", "rpa_set_gvectors", "rpa_set_symmetry",
            "rpa_load_basis", "rpa_kmap", "rpa_set_q", "rpa_chi0", "rpa_kk", "rpa_dyson", "rpa_gfast",
-           "rpa_init_igk", "rpa_kk_matrix", "rpa_stage_times", "rpa_chi0_stats", "rpa_dyson_noalloc", "rpa_selftest", "rpa_launch_count", "rpa_get_stream", "rpa_synchronize",
+           "rpa_init_igk", "rpa_kk_matrix", "rpa_stage_times", "rpa_chi0_stats", "rpa_accum_tile", "rpa_dyson_noalloc", "rpa_selftest", "rpa_launch_count", "rpa_get_stream", "rpa_synchronize",
            "rpa_basis_info", "rpa_create_shared", "rpa_server_create", "rpa_server_submit", "rpa_server_wait",
            "rpa_server_last_error", "rpa_server_destroy", "rpa_pi", "rpa_kk_w", "rpa_gen_fbz",
            "rpa_find_k_ibz", "rpa_find_kq", "rpa_qe_read_gvectors", "rpa_qe_wfc_info", "rpa_qe_read_wfc",
@@ -91,6 +91,7 @@ def load_library(path: str = LIB_PATH):
     L.rpa_kk_matrix.argtypes = [ip, ip, dp, vp]
     L.rpa_stage_times.argtypes = [vp, vp]
     L.rpa_chi0_stats.argtypes = [vp, vp]
+    L.rpa_accum_tile.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.rpa_dyson_noalloc.argtypes = [vp, vp, ip, ip, vp, vp, vp, C.POINTER(C.c_int)]
     L.rpa_selftest.argtypes = [ip, C.POINTER(C.c_double)]
     L.rpa_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
@@ -240,7 +241,7 @@ class Context:
     """One rpa_ctx: resident basis + per-q state, Fortran-layout I/O."""
 
     def __init__(self, device: int = 0, precision: int = PREC_FP64, verbose: int = 0, split: int = 0,
-                 tc_seg: int = 0, vertex_simt: bool = False):
+                 tc_seg: int = 0, vertex_simt: bool = False, acc_tile: tuple | None = None):
         self.L = load_library()
         self.h = C.c_void_p()
         opts = RpaOpts(device=device, precision=precision, verbose=verbose, split=split)
@@ -249,6 +250,11 @@ class Context:
         # explicitly, the FP32 CUDA-core kernel (bases beyond 32767 plane waves
         # or 181 bands per k-point)
         opts.reserved[1] = 1 if vertex_simt else 0
+        # mixed-path S0 accumulation tile (gb local fields per G-tile, nio
+        # frequency rows per CTA) for every call with M2 = M; None: the
+        # autotuner's table, else the library's cost model
+        if acc_tile is not None:
+            opts.reserved[2] = int(acc_tile[0]) | (int(acc_tile[1]) << 8)
         rc = self.L.rpa_create(C.byref(self.h), C.byref(opts))
         if rc != RPA_OK:
             raise RpaError(rc, self.L.rpa_last_error(None).decode())
@@ -454,6 +460,12 @@ class Context:
     def tune_import(self, text: str):
         self._chk(self.L.rpa_tune_import(self.h, text.encode()))
 
+    def accum_tile(self) -> tuple:
+        """(gb, nio) of the last mixed-path accumulation, (0, 0) if none."""
+        gb, nio = C.c_int(), C.c_int()
+        self._chk(self.L.rpa_accum_tile(self.h, C.byref(gb), C.byref(nio)))
+        return gb.value, nio.value
+
     def chi0_stats(self):
         out = np.zeros(4)
         self._chk(self.L.rpa_chi0_stats(self.h, _p(out)))
@@ -566,6 +578,12 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# S0 accumulation tile variants of the mixed path, (gb, nio) as the library
+# lists them (opts.reserved[2] in include/rpa_gpu.h); the first is the default
+ACC_VARIANTS = {"complex": [(96, 1), (64, 1), (32, 2)],
+                "real": [(96, 2), (128, 1), (64, 2), (48, 2), (32, 2)]}
 
 
 def sloss_args(s) -> dict:

@@ -39,9 +39,11 @@ PKG = "2dmaterialsopticalprops_gb300"
 
 
 ACC_DRAM_BYTES_PER_PAIR = 30.4e9 / 54.6e6
-# DRAM bytes per FBZ k-point of one current-vertex launch (k_vertex_mn<32, current>):
-# ncu measured 16.0 + 0.55 GB for the 1600 k-points of the 40x40 case
-VTX_DRAM_BYTES_PER_K = 16.56e9 / 1600
+# DRAM bytes per FBZ k-point of the vertex launches (k_vertex_mn): ncu measured
+# 16.0 + 0.55 GB (current, xx) and 1.30 + 0.18 GB (charge) for the 1600
+# k-points of the 40x40 case
+VTX_DRAM_BYTES_PER_K_CURRENT = 16.56e9 / 1600
+VTX_DRAM_BYTES_PER_K_CHARGE = 1.48e9 / 1600
 
 
 def pkg(name):
@@ -460,7 +462,8 @@ def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, fp64_sample=(0, 9,
                 tmix_one += dt
             outs.append(head)
             stages.append({"wall_ms": round(1e3 * dt, 2),
-                           **{k: round(v, 2) for k, v in c.stage_times().items()}})
+                           **{k: round(v, 2) for k, v in c.stage_times().items()},
+                           **({"accum_tile": list(c.accum_tile())} if c is cm else {})})
         e = pkg("rpa").errstats(outs[0].imag, outs[1].imag, floor=floor)
         errs.append({"q_index": qi, "q_2pi_over_a": info[qi][0], "ngloc": info[qi][1],
                      "Im_epsinv_00": e, "mixed_ms": stages[-2], "fp64_ms": stages[-1]})
@@ -827,9 +830,10 @@ def main():
                     "flops_per_step": work["acc_flops"], "flop_count": "8*NGloc^2*sum_t N_win(t)"}
     else:
         roof_vtx.update({"kernel": "k_vertex_mn (Optabs xx, zz: current; Sloss: charge), 3 launches per step",
-                         "traffic": VTX_DRAM_BYTES_PER_K * s.ntot,
-                         "traffic_basis": "DRAM bytes of one current launch, per k-point from an ncu capture "
-                                          "of the 40x40 case, times this workload's FBZ k-points"})
+                         "traffic": (2 * VTX_DRAM_BYTES_PER_K_CURRENT + VTX_DRAM_BYTES_PER_K_CHARGE) * s.ntot,
+                         "traffic_basis": "DRAM bytes of the step's three vertex launches (xx, zz current; charge), "
+                                          "per k-point from an ncu capture of the 40x40 case, times this "
+                                          "workload's FBZ k-points (the passes bytes_per_step counts)"})
         pk = peaks.get("bf16_tflops_sustained", 1700.0)
         # DRAM bytes of one complex (Optabs) accumulation launch: ncu measured
         # 30.4 GB for 54.6 M (transition, frequency) pairs on the 60x60 case,

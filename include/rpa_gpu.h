@@ -55,7 +55,13 @@ typedef struct rpa_opts {
                       reserved[1]: mixed-path vertex kernel, 0 = tensor cores with
                       MN-major operands (default; at most 32767 plane waves and
                       181 bands per k-point, else rpa_load_basis returns
-                      RPA_EINVAL), 1 = FP32 CUDA cores (any basis size) */
+                      RPA_EINVAL), 1 = FP32 CUDA cores (any basis size).
+                      reserved[2]: mixed-path S0 accumulation tile for every
+                      call with M2 = M, gb | nio << 8 (gb local fields per
+                      G-tile, nio frequency rows per CTA; 0 = the autotuner's
+                      table, else a cost model).  Variants: complex S0 (96, 1)
+                      (64, 1) (32, 2); real S0 (96, 2) (128, 1) (64, 2) (48, 2)
+                      (32, 2); another value makes rpa_chi0 return RPA_EINVAL. */
 } rpa_opts;
 
 /* Arguments of one chi0 accumulation (the namelist values the drivers use).
@@ -147,21 +153,25 @@ int rpa_find_k_ibz(rpa_ctx* ctx, int ntot, const double* ktot, int nki, const do
 int rpa_find_kq(rpa_ctx* ctx, int ntot, const double* ktot, int nki, const double* kI, const double* q, double eps,
                 int* iG0, int* R2, int* K2);
 
-/* ---- Vertex tile autotuner (mixed path; no counterpart in the reference) ------
+/* ---- Tile autotuner (mixed path; no counterpart in the reference) -----------
  * Runs the chi0 call of args on the current k map and q once per candidate
  * tensor-core vertex configuration (band-window width of the sequential side;
  * for charge vertices also the gathered side) and keeps the fastest for later
  * rpa_chi0 calls with the same (mode, nbnd, nocc, NGloc / 32); *best_ms (may be
- * NULL) = its vertex-stage time.  Shared contexts start with their parent's
- * table.  RPA_ESTATE on an FP64 context or with reserved[1] != 0. */
+ * NULL) = its vertex-stage time.  Then, with that vertex configuration, it runs
+ * every S0 accumulation tile variant (see opts.reserved[2]; S0 with M2 = M)
+ * and keeps the fastest accumulation stage for calls with the same (S0 kind,
+ * NGloc, nw / 64).  Shared contexts start with their parent's tables.
+ * RPA_ESTATE on an FP64 context or with reserved[1] != 0. */
 int rpa_autotune(rpa_ctx* ctx, const rpa_chi0_args* args, double* best_ms);
 
-/* The table as JSON text ({"vertex": [{"mode", "nbnd", "nocc", "nlf32", "ymax",
- * "swap", "ms"}, ...]}); *len = bytes needed including the NUL (buf may be NULL
- * to query it). */
+/* The tables as JSON text ({"vertex": [{"mode", "nbnd", "nocc", "nlf32", "ymax",
+ * "swap", "ms"}, ...], "accum": [{"cplx", "nlf", "nw64", "gb", "nio", "ms"},
+ * ...]}); *len = bytes needed including the NUL (buf may be NULL to query it). */
 int rpa_tune_export(const rpa_ctx* ctx, char* buf, int cap, int* len);
 
-/* Replaces the table by the one in json (as written by rpa_tune_export). */
+/* Replaces the tables by the ones in json (as written by rpa_tune_export; the
+ * "accum" list may be absent). */
 int rpa_tune_import(rpa_ctx* ctx, const char* json);
 
 /* ---- On-disk formats (host only, no context; errors via rpa_last_error(NULL)) --
@@ -318,6 +328,12 @@ int rpa_stage_times(const rpa_ctx* ctx, double* ms6);
  * [1] sum over transitions of window lengths (N_win), [2] vertex complex MACs,
  * [3] accumulation launches. */
 int rpa_chi0_stats(const rpa_ctx* ctx, double* out4);
+
+/* The S0 accumulation tile the last rpa_chi0 of a mixed context used: *gb
+ * local fields per G-tile and *nio frequency rows per CTA (0, 0 on the FP64
+ * path or when no interband transition contributed).  Diagnostic; no
+ * counterpart in the reference. */
+int rpa_accum_tile(const rpa_ctx* ctx, int* gb, int* nio);
 
 /* On-device self-test of the tensor-core building blocks on the current
  * device: which = 0, 1, 2 runs a 128 x N x 192 bf16 tcgen05 GEMM (N = 192,

@@ -520,9 +520,30 @@ int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const fl
     c->s_gb = gb;
     c->acc_last_gb = gb;
     c->acc_last_nio = ws_fit_nio(v.nio, cplx, sepa, gb);
+    if (c->defer_acc) {
+      // batch mode: describe the launch instead of making it
+      AccGroupItem it;
+      std::memset(&it, 0, sizeof it);
+      it.A = A;
+      it.tiles = tiles;
+      it.tilesA = tilesA;
+      it.nrb = (P.nw + c->acc_last_nio - 1) / c->acc_last_nio;
+      it.npy = A.sym ? nhv * (nhv + 1) / 2 : nhv;
+      it.npz = A.sym ? 1 : nhv;
+      static_assert(sizeof(AccGroupItem) <= sizeof(c->deferred_item), "deferred item storage");
+      std::memcpy(c->deferred_item, &it, sizeof it);
+      c->deferred = true;
+      c->deferred_gb = gb;
+      c->deferred_nio = v.nio;
+      c->deferred_nw = P.nw;
+      c->deferred_sepa = sepa;
+      c->deferred_cplx = cplx;
+      return RPA_OK;
+    }
     return cplx ? launch_ws_complex(c, A, P.nw, sepa, gb, v.nio, tiles, tilesA)
                 : launch_ws_real(c, A, P.nw, sepa, gb, v.nio, tiles, tilesA);
   }
+  if (c->defer_acc) return fail(c, RPA_EINVAL, "accumulation: a deferred (batched) accumulation needs the default fp16 split and TMEM segments");
   const size_t tbytes = (size_t)nch * nht * (cplx ? 4 : 2) * TC_TILE;
   RPA_TRY(ensure(c, c->d_tiles, tbytes));
   unsigned char* tiles = c->d_tiles.as<unsigned char>();

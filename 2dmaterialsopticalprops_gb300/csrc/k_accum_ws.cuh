@@ -90,9 +90,11 @@ struct WsCfg {
   static_assert(DCOLS % 32 == 0 && DCOLS <= 192, "accumulator layout");
 };
 
+// The work of one CTA: frequency rows bx * NIO.., tile (pair) by, bz as the
+// grid of k_accum_ws numbers them.
 template <int NIO, bool CPLX, bool SEPA, int GB>
-__global__ void __launch_bounds__(WS_THREADS, 1)
-    k_accum_ws(AccTcCtx A, const unsigned char* __restrict__ tiles, const unsigned char* __restrict__ tilesA) {
+__device__ __forceinline__ void accum_ws_cta(const AccTcCtx& A, const unsigned char* __restrict__ tiles,
+                                             const unsigned char* __restrict__ tilesA, int bx, int by, int bz) {
   using Cfg = WsCfg<NIO, CPLX, SEPA, GB>;
   constexpr int S = Cfg::S;
   constexpr uint32_t DATA = Cfg::DATA, FORMED = Cfg::FORMED, A_BYTES = Cfg::A_BYTES;
@@ -112,12 +114,12 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
   __shared__ volatile int abort_flag;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int r0 = blockIdx.x * NIO;
+  const int r0 = bx * NIO;
   // G tile (A rows) and G' tile (B rows), 96 local fields each
-  int gi = blockIdx.y, gj = blockIdx.z;
+  int gi = by, gj = bz;
   if (A.sym) {
-    // blockIdx.y enumerates the pairs gi <= gj row by row
-    int p = blockIdx.y;
+    // by enumerates the pairs gi <= gj row by row
+    int p = by;
     gi = 0;
     while (p >= A.nht - gi) {
       p -= A.nht - gi;
@@ -408,6 +410,55 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
 }
 
 
+template <int NIO, bool CPLX, bool SEPA, int GB>
+__global__ void __launch_bounds__(WS_THREADS, 1)
+    k_accum_ws(AccTcCtx A, const unsigned char* __restrict__ tiles, const unsigned char* __restrict__ tilesA) {
+  accum_ws_cta<NIO, CPLX, SEPA, GB>(A, tiles, tilesA, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// One item of a grouped launch: the accumulation of one q-point (its launch
+// context and pre-split tiles) and the first CTA of the grouped grid that
+// works on it; its CTAs are numbered as k_accum_ws's grid (nrb row blocks x
+// npy x npz tiles).
+struct AccGroupItem {
+  AccTcCtx A;
+  const unsigned char* tiles;
+  const unsigned char* tilesA;
+  long long cta0;
+  int nrb, npy, npz, pad;
+};
+
+// Grouped-tile launch: the S0 accumulations of several q-points (same tile
+// shape, each with its own NGloc, nw, transitions and buffers) as one grid.
+// A CTA finds its item by binary search over cta0 and copies its context to
+// shared memory.
+template <int NIO, bool CPLX, bool SEPA, int GB>
+__global__ void __launch_bounds__(WS_THREADS, 1)
+    k_accum_ws_group(const AccGroupItem* __restrict__ items, int nitems) {
+  __shared__ __align__(16) AccGroupItem it;
+  __shared__ int sidx;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = nitems - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (items[mid].cta0 <= (long long)blockIdx.x) lo = mid;
+      else hi = mid - 1;
+    }
+    sidx = lo;
+  }
+  __syncthreads();
+  {
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(items + sidx);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(&it);
+    for (int i = threadIdx.x; i < (int)(sizeof(AccGroupItem) / 8); i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  const long long local = (long long)blockIdx.x - it.cta0;
+  const int bx = (int)(local % it.nrb);
+  const long long rest = local / it.nrb;
+  accum_ws_cta<NIO, CPLX, SEPA, GB>(it.A, it.tiles, it.tilesA, bx, (int)(rest % it.npy), (int)(rest / it.npy));
+}
+
 // Pre-split B operand of the warp-specialised kernel, per chunk and GB-row
 // tile of G': the hi rows, then the lo rows; rows 0..GB-1 = [Re b | Im b] (B1),
 // rows GB..2GB-1 = [-Im b | Re b] (B2, complex S0 only), b = scale * M(G'),
@@ -465,6 +516,18 @@ static int launch_ws(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char*
 }
 
 
+// nctas = 0: only raises the kernel's shared-memory limit (done before a
+// stream capture, so the captured launch makes no attribute call).
+template <int NIO, bool CPLX, bool SEPA, int GB>
+static cudaError_t launch_ws_group(cudaStream_t s, int device, const AccGroupItem* items, int nitems,
+                                   long long nctas) {
+  using Cfg = WsCfg<NIO, CPLX, SEPA, GB>;
+  auto kern = k_accum_ws_group<NIO, CPLX, SEPA, GB>;
+  if (nctas == 0) return allow_dynamic_smem(kern, device);
+  kern<<<(unsigned)nctas, WS_THREADS, Cfg::SMEM, s>>>(items, nitems);
+  return cudaGetLastError();
+}
+
 template <bool CPLX, int GB>
 static int launch_presplit_ws(rpa_ctx* c, const float2* M, int nchunks, int nht, float scale, unsigned char* tiles) {
   k_presplit_ws<CPLX, GB><<<4096, 256, 0, c->stream>>>(M, c->nlf, nchunks, nht, scale, tiles);
@@ -492,6 +555,11 @@ int launch_ws_complex(rpa_ctx* c, const AccTcCtx& A, int nw, bool sepa, int gb, 
                       const unsigned char* tilesA);
 int launch_ws_real(rpa_ctx* c, const AccTcCtx& A, int nw, bool sepa, int gb, int nio, const unsigned char* tiles,
                    const unsigned char* tilesA);
+// Grouped launch of the real-S0 variant (gb, nio) over nitems items (device
+// array) with nctas CTAs in all (k_accum_ws_r.cu); nctas = 0 sets the
+// kernel's shared-memory attribute only.
+cudaError_t launch_ws_group_real(cudaStream_t s, int device, bool sepa, int gb, int nio, const AccGroupItem* items,
+                                 int nitems, long long nctas);
 // Pre-split B tiles of GB rows for nchunks chunks and nht tiles.
 int presplit_ws_tiles(rpa_ctx* c, bool cplx, int gb, const float2* M, int nchunks, int nht, float scale,
                       unsigned char* tiles);

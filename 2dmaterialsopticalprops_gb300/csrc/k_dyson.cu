@@ -239,19 +239,38 @@ __global__ void __launch_bounds__(256) k_dyson_fp64(DysonArgs D) {
   }
 }
 
-int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singular, int* n_zero,
-               const double2** head_dev) {
+static int dyson_grid(rpa_ctx* c, int nwo, int* grid) {
+  int dev_sms = 0;
+  RPA_CUDA(c, cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
+  *grid = nwo < 2 * dev_sms ? nwo : 2 * dev_sms;
+  return RPA_OK;
+}
+
+// Uploads V and sizes every buffer of the Dyson step of the current chi0, so
+// that dyson_enqueue allocates nothing.
+int dyson_prepare(rpa_ctx* c, const double* V_host, bool want_epsinv) {
   const int n = c->nlf, nn = n * n, nwo = c->last_no - 1;
   RPA_TRY(ensure(c, c->d_V, sizeof(double) * nn));
   RPA_CUDA(c, cudaMemcpyAsync(c->d_V.p, V_host, sizeof(double) * nn, cudaMemcpyHostToDevice, c->stream));
-  int dev_sms = 0;
-  RPA_CUDA(c, cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
-  int grid = nwo < 2 * dev_sms ? nwo : 2 * dev_sms;
+  int grid = 0;
+  RPA_TRY(dyson_grid(c, nwo, &grid));
   RPA_TRY(ensure(c, c->d_WT, sizeof(double2) * (size_t)nwo * nn));
   if (want_epsinv) RPA_TRY(ensure(c, c->d_eps, sizeof(double2) * (size_t)nwo * nn));
   RPA_TRY(ensure(c, c->d_tmp, sizeof(double2) * (size_t)grid * 3 * nn + sizeof(double2) * (nwo + 1)));
   RPA_TRY(ensure(c, c->d_flags, sizeof(int) * 4));
-  RPA_CUDA(c, cudaMemsetAsync(c->d_flags.p, 0, sizeof(int) * 4, c->stream));
+  if (c->precision == RPA_PREC_MIXED) RPA_CUDA(c, allow_dynamic_smem(k_dyson_fp64<true>, c->device));
+  else RPA_CUDA(c, allow_dynamic_smem(k_dyson_fp64<false>, c->device));
+  return RPA_OK;
+}
+
+// The Dyson kernel on the context's stream (no allocation, no host wait):
+// clears the singular / zero-pivot counters (flags[0..1]; the accumulation's
+// status in flags[2..3] is kept) and solves every frequency.
+int dyson_enqueue(rpa_ctx* c, bool want_epsinv, const double2** head_dev) {
+  const int n = c->nlf, nn = n * n, nwo = c->last_no - 1;
+  int grid = 0;
+  RPA_TRY(dyson_grid(c, nwo, &grid));
+  RPA_CUDA(c, cudaMemsetAsync(c->d_flags.p, 0, sizeof(int) * 2, c->stream));
   DysonArgs D;
   D.chi0 = c->d_chi0.as<double2>();
   D.V = c->d_V.as<double>();
@@ -263,21 +282,25 @@ int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singul
   D.n = n;
   D.nwo = nwo;
   size_t smem = ((3 * (size_t)n * sizeof(int) + 15) & ~(size_t)15) + sizeof(double2) * n;
-  if (c->precision == RPA_PREC_MIXED) {
-    RPA_CUDA(c, allow_dynamic_smem(k_dyson_fp64<true>, c->device));
+  if (c->precision == RPA_PREC_MIXED)
     k_dyson_fp64<true><<<grid, 256, smem, c->stream>>>(D);
-  } else {
-    RPA_CUDA(c, allow_dynamic_smem(k_dyson_fp64<false>, c->device));
+  else
     k_dyson_fp64<false><<<grid, 256, smem, c->stream>>>(D);
-  }
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
+  if (head_dev) *head_dev = D.head;
+  return RPA_OK;
+}
+
+int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singular, int* n_zero,
+               const double2** head_dev) {
+  RPA_TRY(dyson_prepare(c, V_host, want_epsinv));
+  RPA_TRY(dyson_enqueue(c, want_epsinv, head_dev));
   int fl[4];
   RPA_CUDA(c, cudaMemcpyAsync(fl, c->d_flags.p, sizeof(int) * 4, cudaMemcpyDeviceToHost, c->stream));
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
   *n_singular = fl[0];
   *n_zero = fl[1];
-  if (head_dev) *head_dev = D.head;
   return RPA_OK;
 }
 

@@ -261,12 +261,13 @@ int kk_apply_real_fp64(rpa_ctx* c, DevBuf& buf, const std::vector<double>& K, in
   return RPA_OK;
 }
 
-int kk_run(rpa_ctx* c, int variant, int no, double domega) {
+// The fixed kernel of (variant, no, domega) on the device and the chi0 buffer
+// sized, so that kk_run then only launches.
+int kk_prepare(rpa_ctx* c, int variant, int no, double domega) {
   // the fixed kernel depends on (variant, no, domega) only: built on the host and
   // copied once per variant slot, then reused by every transform with the same grid
   const int sl = variant == RPA_KK_OPTABS_COMPLEX ? 0 : 1;
   const bool cached = c->kk_key_no[sl] == no && c->kk_key_domega[sl] == domega;
-  const int nw = variant == RPA_KK_OPTABS_COMPLEX ? 2 * no + 1 : no;
   const int nrow = no - 1, np = c->nlf * c->nlf;
   DevBuf& dk = c->d_kk[sl];
   DevBuf& dkf = c->d_kkf[sl];
@@ -288,6 +289,16 @@ int kk_run(rpa_ctx* c, int variant, int no, double domega) {
     c->kk_key_domega[sl] = domega;
   }
   RPA_TRY(ensure(c, c->d_chi0, sizeof(double2) * (size_t)nrow * np));
+  return RPA_OK;
+}
+
+int kk_run(rpa_ctx* c, int variant, int no, double domega) {
+  RPA_TRY(kk_prepare(c, variant, no, domega));
+  const int sl = variant == RPA_KK_OPTABS_COMPLEX ? 0 : 1;
+  const int nw = variant == RPA_KK_OPTABS_COMPLEX ? 2 * no + 1 : no;
+  const int nrow = no - 1, np = c->nlf * c->nlf;
+  DevBuf& dk = c->d_kk[sl];
+  DevBuf& dkf = c->d_kkf[sl];
   const bool cplx = variant == RPA_KK_OPTABS_COMPLEX;
   const int ncols = cplx ? 2 * np : np;
   dim3 grid((ncols + 63) / 64, (nrow + 31) / 32);

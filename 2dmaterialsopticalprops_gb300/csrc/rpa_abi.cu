@@ -251,6 +251,10 @@ static void genV_host(const rpa_ctx* c, double Gcar, double c0, double eps, std:
   }
 }
 
+// V of the current q-point and local fields (genV, Sloss.f90:1173-1208) for
+// the batch driver.
+void genV_of(const rpa_ctx* c, double c0, double eps, std::vector<double>& V) { genV_host(c, c->last_Gcar, c0, eps, V); }
+
 struct EvTimer {
   rpa_ctx* c;
   int a, b;
@@ -685,6 +689,9 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
   RPA_TRY(ensure(c, c->d_S, s_bytes));
   c->s_sym = false;
   c->acc_last_gb = c->acc_last_nio = 0;
+  c->deferred = false;
+  if (c->defer_acc && c->precision != RPA_PREC_MIXED)
+    return fail(c, RPA_EINVAL, "rpa_chi0: a deferred accumulation needs the mixed path");
   RPA_TRY(ensure(c, c->d_Q, sizeof(double2) * np));
   RPA_CUDA(c, cudaMemsetAsync(c->d_S.p, 0, s_bytes, c->stream));
   if (c->precision == RPA_PREC_MIXED) {
@@ -722,6 +729,8 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
     int k1 = k0;
     while (k1 < c->ntot && (size_t)(tot + counts[k1]) <= max_trans) tot += counts[k1++];
     if (k1 == k0) return fail(c, RPA_EINVAL, "rpa_chi0: one k-point exceeds the transition budget");
+    if (c->defer_acc && (k0 > 0 || k1 < c->ntot))
+      return fail(c, RPA_EINVAL, "rpa_chi0: a deferred accumulation needs the transitions of all k-points in one chunk");
     int nk = k1 - k0;
     std::vector<long long> off(nk + 1, 0);
     for (int i = 0; i < nk; ++i) off[i + 1] = off[i] + counts[k0 + i];
@@ -786,7 +795,7 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
     }
     k0 = k1;
   }
-  if (c->precision == RPA_PREC_MIXED) RPA_TRY(df_to_f64(c, s_bytes / sizeof(double), P.nw, cplx));
+  if (c->precision == RPA_PREC_MIXED && !c->defer_acc) RPA_TRY(df_to_f64(c, s_bytes / sizeof(double), P.nw, cplx));
   cudaEventRecord(c->ev[5], c->stream);
   RPA_CUDA(c, cudaStreamSynchronize(c->stream));
   {

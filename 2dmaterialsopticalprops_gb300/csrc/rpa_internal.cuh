@@ -146,6 +146,14 @@ struct rpa_ctx {
   // the mixed-path accumulation of the running rpa_chi0 computed only the tile
   // pairs gi <= gj of S0 (M2 = M); the conversion to FP64 mirrors the rest
   bool s_sym = false;
+  // deferred S0 accumulation (batch mode, batch.cu): with defer_acc set,
+  // rpa_chi0 stops after the B-tile pre-split and leaves the accumulation's
+  // launch description (an AccGroupItem) here for a grouped launch
+  bool defer_acc = false;
+  bool deferred = false;
+  alignas(16) unsigned char deferred_item[256];
+  int deferred_gb = 0, deferred_nio = 0, deferred_nw = 0;
+  bool deferred_sepa = false, deferred_cplx = false;
   int s_gb = 96;  // G-tile rows of that accumulation
   double stage_ms[6] = {0, 0, 0, 0, 0, 0};
   long long launches = 0;  // kernels launched by this context
@@ -220,6 +228,8 @@ int kk_apply_real_fp64(rpa_ctx* c, DevBuf& buf, const std::vector<double>& K, in
 // the page-locked ring when dst is pageable; basis upload overlapping copies
 // and transposes; release of the ring, threads and copy stream
 int copy_d2h(rpa_ctx* c, void* dst, const void* src, size_t bytes);
+// V (genV) of the context's q-point and local fields, real (nlf, nlf) column-major
+void genV_of(const rpa_ctx* c, double c0, double eps, std::vector<double>& V);
 int upload_basis(rpa_ctx* c, const double* coeff, int nks, int nbnd, int npwx, double2* dst);
 int host_io_prepare(rpa_ctx* c);
 void host_io_release(rpa_ctx* c);

@@ -29,7 +29,8 @@ EXPORTS = ["rpa_create", "rpa_destroy", "rpa_last_error", "rpa_set_gvectors", "r
            "rpa_server_last_error", "rpa_server_destroy", "rpa_pi", "rpa_kk_w", "rpa_gen_fbz",
            "rpa_find_k_ibz", "rpa_find_kq", "rpa_qe_read_gvectors", "rpa_qe_wfc_info", "rpa_qe_read_wfc",
            "rpa_write_corrfun", "rpa_read_corrfun", "rpa_write_wt", "rpa_autotune",
-           "rpa_tune_export", "rpa_tune_import"]
+           "rpa_tune_export", "rpa_tune_import", "rpa_batch_create", "rpa_batch_run", "rpa_batch_info", "rpa_batch_launch", "rpa_batch_wait",
+           "rpa_batch_last_error", "rpa_batch_destroy"]
 
 
 class RpaOpts(C.Structure):
@@ -119,9 +120,16 @@ def load_library(path: str = LIB_PATH):
     L.rpa_server_wait.argtypes = [vp, C.c_longlong, vp]
     L.rpa_server_last_error.argtypes = [vp]
     L.rpa_server_destroy.argtypes = [vp]
+    L.rpa_batch_create.argtypes = [C.POINTER(vp), vp, ip]
+    L.rpa_batch_run.argtypes = [vp, ip, vp, vp]
+    L.rpa_batch_launch.argtypes = [vp, ip, vp, vp]
+    L.rpa_batch_wait.argtypes = [vp]
+    L.rpa_batch_info.argtypes = [vp, vp, C.POINTER(ip), C.POINTER(C.c_longlong)]
+    L.rpa_batch_last_error.argtypes = [vp]
+    L.rpa_batch_destroy.argtypes = [vp]
     for name in EXPORTS:
-        if name == "rpa_server_last_error":
-            L.rpa_server_last_error.restype = C.c_char_p
+        if name in ("rpa_server_last_error", "rpa_batch_last_error"):
+            getattr(L, name).restype = C.c_char_p
             continue
         if name != "rpa_last_error":
             getattr(L, name).restype = C.c_int
@@ -501,6 +509,112 @@ def shared_context(parent: Context, precision: int | None = None) -> Context:
     return c
 
 
+def _make_request(*, kind: int, kmap: dict, ilf, parG, args: dict, mode: int, kk_variant: int,
+                  c0: float = 0.0, eps: float = 1e-4, want_s0: bool = False, want_chi0: bool = True,
+                  want_wt: bool = False, want_head: bool = True):
+    """An RpaRequest and the arrays it points to (kept alive by the caller)."""
+    keep = {}
+
+    def arr(x, dt):
+        a = np.ascontiguousarray(x, dtype=dt)
+        keep[id(a)] = a
+        return a
+
+    ktot = arr(kmap["ktot"], np.float64)
+    ints = [arr(kmap[k], np.int32) for k in ("K1", "R1", "K2", "R2", "iG0")]
+    ilf_a = arr(ilf, np.int32)
+    par_a = arr(parG, np.int32)
+    nlf, no = ilf_a.size, int(args["no"])
+    a = dict(args)
+    pol = POL[a.pop("pol", "xx")]
+    ca = RpaChi0Args(mode=mode, pol=pol, **{k: v for k, v in a.items()})
+    outs = {}
+    if want_s0:
+        outs["S0"] = (np.zeros((nlf, nlf, 2 * no + 1), dtype=np.complex128) if mode == MODE_CURRENT
+                      else np.zeros((nlf, nlf, no), dtype=np.float64))
+    if want_chi0:
+        outs["chi0"] = np.zeros((nlf, nlf, no - 1), dtype=np.complex128)
+    if kind == REQ_W and want_wt:
+        outs["WT"] = np.zeros((nlf, nlf, no - 1), dtype=np.complex128)
+    if kind == REQ_W and want_head:
+        outs["head"] = np.zeros(no - 1, dtype=np.complex128)
+    r = RpaRequest(kind=kind, kk_variant=kk_variant, ntot=ktot.shape[0], ktot=_p(ktot),
+                   K1=_p(ints[0]), R1=_p(ints[1]), K2=_p(ints[2]), R2=_p(ints[3]), iG0=_p(ints[4]),
+                   nlf=nlf, ilf=_p(ilf_a), parG=_p(par_a), args=ca, c0=c0, eps=eps,
+                   S0_out=_p(outs.get("S0")), Qeff_out=None, chi0_out=_p(outs.get("chi0")),
+                   WT_out=_p(outs.get("WT")), head_out=_p(outs.get("head")))
+    for i in range(3):
+        r.q[i] = float(kmap["q"][i])
+    return r, keep, outs
+
+
+class Batch:
+    """rpa_batch: up to max_q W requests per run on shared contexts of parent,
+    their S0 accumulations as grouped-tile launches and the conversion, KK and
+    Dyson stages of all of them in one CUDA graph."""
+
+    def __init__(self, parent: Context, max_q: int):
+        self.L = parent.L
+        self.h = C.c_void_p()
+        rc = self.L.rpa_batch_create(C.byref(self.h), parent.h, int(max_q))
+        if rc != RPA_OK:
+            raise RpaError(rc, "rpa_batch_create failed")
+        self.max_q = int(max_q)
+        self._pending = None
+
+    def run(self, requests: list, want_wt: bool = False):
+        """requests: dicts with kmap, ilf, parG, args, c0, eps (W requests).
+        Returns a list of (status, {"head": ..., "WT": ...})."""
+        self.launch(requests, want_wt)
+        return self.wait()
+
+    def launch(self, requests: list, want_wt: bool = False):
+        """The per-request part and the graph launch; returns without waiting
+        for the graph (wait() collects the results)."""
+        built = [_make_request(kind=REQ_W, mode=MODE_CHARGE, kk_variant=KK_SLOSS_REAL, want_chi0=False,
+                               want_wt=want_wt, **{k: r[k] for k in ("kmap", "ilf", "parG", "args", "c0", "eps")})
+                 for r in requests]
+        arr = (RpaRequest * len(built))(*[b[0] for b in built])
+        st = np.zeros(len(built), dtype=np.int32)
+        rc = self.L.rpa_batch_launch(self.h, len(built), C.cast(arr, C.c_void_p), _p(st))
+        if rc != RPA_OK:
+            raise RpaError(rc, self.L.rpa_batch_last_error(self.h).decode())
+        self._pending = (built, arr, st)
+
+    def wait(self):
+        if self._pending is None:
+            rc = self.L.rpa_batch_wait(self.h)
+            raise RpaError(rc, self.L.rpa_batch_last_error(self.h).decode())
+        built, arr, st = self._pending
+        self._pending = None
+        rc = self.L.rpa_batch_wait(self.h)
+        if rc != RPA_OK and not np.any(st != RPA_OK):
+            raise RpaError(rc, self.L.rpa_batch_last_error(self.h).decode())
+        return [(int(s), b[2]) for s, b in zip(st, built)]
+
+    def info(self) -> dict:
+        t = np.zeros(4)
+        g = C.c_int()
+        n = C.c_longlong()
+        self.L.rpa_batch_info(self.h, _p(t), C.byref(g), C.byref(n))
+        return {"setup_s": t[0], "capture_s": t[1], "graph_s": t[2], "readback_s": t[3], "groups": g.value,
+                "graph_nodes": n.value}
+
+    def last_error(self) -> str:
+        return self.L.rpa_batch_last_error(self.h).decode()
+
+    def close(self):
+        if self.h:
+            self.L.rpa_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Server:
     """rpa_server: requests of any q, local-field set and frequency grid on
     one resident basis, run by nslots shared contexts with continuous
@@ -519,38 +633,9 @@ class Server:
     def submit(self, *, kind: int, kmap: dict, ilf, parG, args: dict, mode: int, kk_variant: int,
                c0: float = 0.0, eps: float = 1e-4, want_s0: bool = False, want_chi0: bool = True,
                want_wt: bool = False, want_head: bool = True) -> int:
-        keep = {}
-
-        def arr(x, dt):
-            a = np.ascontiguousarray(x, dtype=dt)
-            keep[id(a)] = a
-            return a
-
-        ktot = arr(kmap["ktot"], np.float64)
-        ints = [arr(kmap[k], np.int32) for k in ("K1", "R1", "K2", "R2", "iG0")]
-        ilf_a = arr(ilf, np.int32)
-        par_a = arr(parG, np.int32)
-        nlf, no = ilf_a.size, int(args["no"])
-        a = dict(args)
-        pol = POL[a.pop("pol", "xx")]
-        ca = RpaChi0Args(mode=mode, pol=pol, **{k: v for k, v in a.items()})
-        outs = {}
-        if want_s0:
-            outs["S0"] = (np.zeros((nlf, nlf, 2 * no + 1), dtype=np.complex128) if mode == MODE_CURRENT
-                          else np.zeros((nlf, nlf, no), dtype=np.float64))
-        if want_chi0:
-            outs["chi0"] = np.zeros((nlf, nlf, no - 1), dtype=np.complex128)
-        if kind == REQ_W and want_wt:
-            outs["WT"] = np.zeros((nlf, nlf, no - 1), dtype=np.complex128)
-        if kind == REQ_W and want_head:
-            outs["head"] = np.zeros(no - 1, dtype=np.complex128)
-        r = RpaRequest(kind=kind, kk_variant=kk_variant, ntot=ktot.shape[0], ktot=_p(ktot),
-                       K1=_p(ints[0]), R1=_p(ints[1]), K2=_p(ints[2]), R2=_p(ints[3]), iG0=_p(ints[4]),
-                       nlf=nlf, ilf=_p(ilf_a), parG=_p(par_a), args=ca, c0=c0, eps=eps,
-                       S0_out=_p(outs.get("S0")), Qeff_out=None, chi0_out=_p(outs.get("chi0")),
-                       WT_out=_p(outs.get("WT")), head_out=_p(outs.get("head")))
-        for i in range(3):
-            r.q[i] = float(kmap["q"][i])
+        r, keep, outs = _make_request(kind=kind, kmap=kmap, ilf=ilf, parG=parG, args=args, mode=mode,
+                                      kk_variant=kk_variant, c0=c0, eps=eps, want_s0=want_s0, want_chi0=want_chi0,
+                                      want_wt=want_wt, want_head=want_head)
         rid = C.c_longlong()
         rc = self.L.rpa_server_submit(self.h, C.byref(r), C.byref(rid))
         if rc != RPA_OK:

@@ -417,6 +417,43 @@ const char* rpa_server_last_error(const rpa_server* srv);
 /* Finishes the queued requests, stops the workers, destroys the contexts. */
 int rpa_server_destroy(rpa_server* srv);
 
+/* ---- Batched W requests in one CUDA graph (no counterpart in the reference) --
+ * A batch owns max_q shared contexts on parent's resident basis (parent must be
+ * RPA_PREC_MIXED).  rpa_batch_run solves nq <= max_q W requests (RPA_REQ_W,
+ * RPA_MODE_CHARGE, RPA_KK_SLOSS_REAL; outputs head_out and WT_out, host, or
+ * NULL) as the Sloss q loop (Sloss.f90:292-481) would for each, in two parts:
+ *   - per request, on its context: k map and q, pairs, windows, sort,
+ *     tensor-core vertices, B-tile pre-split (the host decisions of a q-chain:
+ *     transition counts, the window bound, operand scales), V, the KK matrix;
+ *   - one CUDA graph, launched once: per S0 tile shape one grouped-tile launch
+ *     of the S0 accumulation over every request of that shape (each request
+ *     keeps its own NGloc, nw, transitions and buffers), then per request, as
+ *     parallel branches, S0 to FP64, KK and the FP64 Dyson solve.
+ * status[i] = the request's own result code; the call returns RPA_OK or the
+ * first failing request's code (rpa_batch_last_error gives its message).  Each
+ * request needs all its transitions in one k-chunk (RPA_EINVAL otherwise) and
+ * the default split / segment options.  Arrays of reqs must stay valid during
+ * the call.  The results equal rpa_chi0 + rpa_kk + rpa_dyson on a mixed
+ * context to the mixed path's rounding. */
+typedef struct rpa_batch rpa_batch;
+int rpa_batch_create(rpa_batch** out, rpa_ctx* parent, int max_q);
+int rpa_batch_run(rpa_batch* b, int nq, const rpa_request* reqs, int* status);
+/* rpa_batch_run in two halves: launch does the per-request part and launches
+ * the graph without waiting for it (reqs, status and the requests' arrays must
+ * stay valid until the wait); wait blocks until the graph is done and fills
+ * status and the outputs.  Two batches on the same parent can alternate, the
+ * per-request part of one overlapping the graph of the other. */
+int rpa_batch_launch(rpa_batch* b, int nq, const rpa_request* reqs, int* status);
+int rpa_batch_wait(rpa_batch* b);
+/* Of the last rpa_batch_run: times4 (may be NULL) = seconds of [0] the
+ * per-request part, [1] graph capture and instantiation, [2] the graph's
+ * execution, [3] the read-back; the number of grouped launches (tile shapes)
+ * and of graph nodes. */
+int rpa_batch_info(const rpa_batch* b, double* times4, int* groups, long long* nodes);
+const char* rpa_batch_last_error(const rpa_batch* b);
+/* Destroys the batch's contexts (before rpa_destroy(parent)). */
+int rpa_batch_destroy(rpa_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

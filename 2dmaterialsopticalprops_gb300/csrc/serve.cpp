@@ -9,6 +9,12 @@
 // larger than the whole budget runs alone).  Each context has its own stream,
 // so the kernels of running requests overlap on the GPU, and a request that
 // arrives while others run starts without waiting for them to finish.
+// rpa_server_create_batched adds one batching worker with an rpa_batch: when
+// it is free and the queue starts with W requests (charge mode, Sloss KK), it
+// takes up to batch_q of them that fit the budget and runs them as one batch
+// (per-request setup, then one CUDA graph with the grouped-tile S0 launches
+// and every request's KK and Dyson); the slot workers keep serving the queue
+// meanwhile, so requests of any kind still start as soon as any worker is free.
 
 #include <chrono>
 #include <condition_variable>
@@ -43,6 +49,9 @@ double seconds(clock_type::time_point a, clock_type::time_point b) {
 
 struct rpa_server {
   rpa_ctx* parent = nullptr;
+  rpa_batch* batch = nullptr;  // the batching worker's batch (rpa_server_create_batched)
+  int batch_q = 0;
+  long long batched = 0;       // requests completed through the batch
   std::vector<rpa_ctx*> slots;
   std::vector<std::thread> workers;
   std::mutex mu;
@@ -117,9 +126,99 @@ void worker(rpa_server* s, int slot) {
   }
 }
 
+bool batchable(const rpa_request& r) {
+  return r.kind == RPA_REQ_W && r.args.mode == RPA_MODE_CHARGE && r.kk_variant == RPA_KK_SLOSS_REAL &&
+         !r.S0_out && !r.Qeff_out && !r.chi0_out;
+}
+
+void batch_worker(rpa_server* s) {
+  std::vector<long long> ids;
+  std::vector<rpa_request> reqs;
+  std::vector<int> status;
+  for (;;) {
+    double fp = 0;
+    ids.clear();
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      // the oldest queued W request that fits next to the running ones
+      auto first = [&]() -> std::deque<long long>::iterator {
+        for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
+          const Job& j = s->jobs[*it];
+          if (batchable(j.req)) return (s->running == 0 || s->in_use + j.footprint <= s->budget) ? it : s->queue.end();
+        }
+        return s->queue.end();
+      };
+      s->cv.wait(lk, [&] { return s->stop || first() != s->queue.end(); });
+      if (first() == s->queue.end()) return;  // stopping: the slot workers finish what is queued
+      // up to batch_q W requests in arrival order (other kinds stay queued for
+      // the slot workers), as long as they fit the budget
+      for (auto it = first(); it != s->queue.end() && (int)ids.size() < s->batch_q;) {
+        Job& j = s->jobs[*it];
+        if (!batchable(j.req)) {
+          ++it;
+          continue;
+        }
+        if (!ids.empty() && s->in_use + fp + j.footprint > s->budget) break;
+        ids.push_back(*it);
+        fp += j.footprint;
+        j.t_start = clock_type::now();
+        it = s->queue.erase(it);
+      }
+      s->in_use += fp;
+      ++s->running;
+      reqs.clear();
+      for (long long id : ids) reqs.push_back(s->jobs[id].req);
+    }
+    status.assign(ids.size(), RPA_OK);
+    const int rc = rpa_batch_run(s->batch, (int)ids.size(), reqs.data(), status.data());
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      const auto now = clock_type::now();
+      for (size_t i = 0; i < ids.size(); ++i) {
+        Job& j = s->jobs[ids[i]];
+        j.t_end = now;
+        j.status = status[i] != RPA_OK ? status[i] : (rc != RPA_OK && rc != RPA_ESINGULAR ? rc : RPA_OK);
+        if (j.status != RPA_OK) j.error = rpa_batch_last_error(s->batch);
+        j.done = true;
+      }
+      s->in_use -= fp;
+      --s->running;
+      s->completed += (long long)ids.size();
+      s->batched += (long long)ids.size();
+    }
+    s->cv.notify_all();
+  }
+}
+
 }  // namespace
 
 extern "C" {
+
+int rpa_server_create_batched(rpa_server** out, rpa_ctx* parent, int nslots, double mem_bytes, int batch_q) {
+  if (!out || batch_q < 1) return RPA_EINVAL;
+  rpa_batch* b = nullptr;
+  int rc = rpa_batch_create(&b, parent, batch_q);
+  if (rc != RPA_OK) return rc;
+  rc = rpa_server_create(out, parent, nslots, mem_bytes);
+  if (rc != RPA_OK) {
+    rpa_batch_destroy(b);
+    return rc;
+  }
+  rpa_server* s = *out;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->batch = b;
+    s->batch_q = batch_q;
+  }
+  s->workers.emplace_back(batch_worker, s);
+  return RPA_OK;
+}
+
+int rpa_server_batched_count(const rpa_server* s, long long* n) {
+  if (!s || !n) return RPA_EINVAL;
+  *n = s->batched;
+  return RPA_OK;
+}
 
 int rpa_server_create(rpa_server** out, rpa_ctx* parent, int nslots, double mem_bytes) {
   if (!out || !parent || nslots < 1 || nslots > 64 || !(mem_bytes > 0)) return RPA_EINVAL;
@@ -195,6 +294,7 @@ int rpa_server_destroy(rpa_server* s) {
   s->cv.notify_all();
   for (auto& t : s->workers) t.join();
   int rc = RPA_OK;
+  if (s->batch) rpa_batch_destroy(s->batch);
   for (rpa_ctx* c : s->slots) {
     const int r = rpa_destroy(c);
     if (r != RPA_OK) rc = r;

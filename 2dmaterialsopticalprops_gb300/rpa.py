@@ -30,6 +30,7 @@ EXPORTS = ["rpa_create", "rpa_destroy", "rpa_last_error", "rpa_set_gvectors", "r
            "rpa_find_k_ibz", "rpa_find_kq", "rpa_qe_read_gvectors", "rpa_qe_wfc_info", "rpa_qe_read_wfc",
            "rpa_write_corrfun", "rpa_read_corrfun", "rpa_write_wt", "rpa_autotune",
            "rpa_tune_export", "rpa_tune_import", "rpa_batch_create", "rpa_batch_run", "rpa_batch_info", "rpa_batch_launch", "rpa_batch_wait",
+           "rpa_server_create_batched", "rpa_server_batched_count",
            "rpa_batch_last_error", "rpa_batch_destroy"]
 
 
@@ -121,6 +122,8 @@ def load_library(path: str = LIB_PATH):
     L.rpa_server_last_error.argtypes = [vp]
     L.rpa_server_destroy.argtypes = [vp]
     L.rpa_batch_create.argtypes = [C.POINTER(vp), vp, ip]
+    L.rpa_server_create_batched.argtypes = [C.POINTER(vp), vp, ip, dp, ip]
+    L.rpa_server_batched_count.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.rpa_batch_run.argtypes = [vp, ip, vp, vp]
     L.rpa_batch_launch.argtypes = [vp, ip, vp, vp]
     L.rpa_batch_wait.argtypes = [vp]
@@ -621,11 +624,16 @@ class Server:
     batching.  submit() returns an id; wait(id) returns the outputs and
     (latency, queue, service) seconds."""
 
-    def __init__(self, parent: Context, nslots: int, mem_bytes: float):
+    def __init__(self, parent: Context, nslots: int, mem_bytes: float, batch_q: int = 0):
+        """batch_q > 0: also a batching worker that runs up to batch_q queued W
+        requests as one rpa_batch (rpa_server_create_batched)."""
         self.L = parent.L
         self.parent = parent
         self.h = C.c_void_p()
-        rc = self.L.rpa_server_create(C.byref(self.h), parent.h, nslots, float(mem_bytes))
+        if batch_q > 0:
+            rc = self.L.rpa_server_create_batched(C.byref(self.h), parent.h, nslots, float(mem_bytes), int(batch_q))
+        else:
+            rc = self.L.rpa_server_create(C.byref(self.h), parent.h, nslots, float(mem_bytes))
         if rc != RPA_OK:
             raise RpaError(rc, "rpa_server_create failed")
         self.live = {}
@@ -642,6 +650,15 @@ class Server:
             raise RpaError(rc, "rpa_server_submit failed")
         self.live[rid.value] = (keep, outs, r)
         return rid.value
+
+    def batched_count(self) -> int:
+        n = C.c_longlong()
+        self._chk_srv(self.L.rpa_server_batched_count(self.h, C.byref(n)))
+        return n.value
+
+    def _chk_srv(self, rc):
+        if rc != RPA_OK:
+            raise RpaError(rc, "server")
 
     def wait(self, rid: int):
         t = np.zeros(3)

@@ -326,7 +326,7 @@ SERVE_MIXES = {
 
 
 def serving_run(n_req: int = 32, rate: float = 200.0, nslots: int = 4, mem_gb: float = 40.0, seed: int = 5,
-                mix: str = "grid60"):
+                mix: str = "grid60", batch_q: int = 0):
     """Request loop on a resident basis (mixed path): seeded Poisson arrivals of
     W (loss-function) and chi0 (Optabs xx) requests with the q, NGloc and nw
     ranges of SERVE_MIXES[mix], served by nslots shared contexts with
@@ -352,14 +352,14 @@ def serving_run(n_req: int = 32, rate: float = 200.0, nslots: int = 4, mem_gb: f
         if i % 2 == 0:
             args = dict(no=no, domega=domega, eta=s.eta, Vcell=s.Vcell, Gcar=s.Gcar, nocc=s.nocc)
             return dict(kind=rpa.REQ_W, kmap=km, ilf=ilf, parG=par, args=args, mode=rpa.MODE_CHARGE,
-                        kk_variant=rpa.KK_SLOSS_REAL, c0=s.c0, eps=s.cfg.eps), (ilf.size, no, "W")
+                        kk_variant=rpa.KK_SLOSS_REAL, c0=s.c0, eps=s.cfg.eps, want_chi0=False), (ilf.size, no, "W")
         a = rpa.optabs_args(s, "xx")
         a.update(no=no, domega=domega)
         return dict(kind=rpa.REQ_CHI0, kmap=km, ilf=ilf, parG=par, args=a, mode=rpa.MODE_CURRENT,
                     kk_variant=rpa.KK_OPTABS_COMPLEX), (ilf.size, no, "chi")
 
     reqs = [make(i) for i in range(n_req + 4)]
-    srv = rpa.Server(parent, nslots=nslots, mem_bytes=mem_gb * 1e9)
+    srv = rpa.Server(parent, nslots=nslots, mem_bytes=mem_gb * 1e9, batch_q=batch_q)
     # warm-up: one request per slot at once, so that every slot's device
     # buffers reach their sizes before the timed stream
     for i in [srv.submit(**r) for r, _ in reqs[:4]]:
@@ -383,6 +383,7 @@ def serving_run(n_req: int = 32, rate: float = 200.0, nslots: int = 4, mem_gb: f
     th.join()
     res = [srv.wait(i)[1] for i in ids]
     t_end = time.perf_counter()
+    n_batched = srv.batched_count()
     srv.close()
     parent.close()
     lat = np.array([r[0] for r in res])
@@ -394,6 +395,7 @@ def serving_run(n_req: int = 32, rate: float = 200.0, nslots: int = 4, mem_gb: f
                         f"nw {M['no'][0]}-{M['no'][1] - 1}; {nslots} slots, {mem_gb:g} GB admission budget",
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
             "mean_queue_s": float(queue.mean()), "mean_service_s": float(serv.mean()),
+            "batching_worker": {"batch_q": batch_q, "requests_batched": n_batched} if batch_q else None,
             "throughput_req_s": n_req / (t_end - t0), "n_requests": n_req, "slots": nslots,
             "ngloc_range": [int(min(r[1][0] for r in reqs)), int(max(r[1][0] for r in reqs))],
             "nw_range": [int(min(r[1][1] for r in reqs)), int(max(r[1][1] for r in reqs))]}
@@ -408,8 +410,8 @@ def dispersion_path(nk: int, n_q: int):
     return [pts[i] for i in idx]
 
 
-def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, fp64_sample=(0, 9, 18, 27, 36, 45, 54, 63),
-                   no: int = 701, eta_ev: float = 0.05, floor: float = 1e-3):
+def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, n_fp64: int = 8, no: int = 701,
+                   eta_ev: float = 0.05, floor: float = 1e-3):
     """64-q loss-function dispersion (W and Im eps^-1 per q) on the resident
     grid120 basis: NGloc rising from 31 to 151 along the path, nw = 701 on
     0-30 eV, eta = 50 meV.  All q-points are submitted at once to a server of
@@ -422,6 +424,9 @@ def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, fp64_sample=(0, 9,
         parent.load_system(s)
     path = dispersion_path(s.cfg.nk, n_q)
     n_q = len(path)
+    # the q-points of the FP64 comparison: n_fp64 evenly spaced along the path
+    # (0, 9, 18, ..., 63 for 64 q-points)
+    fp64_sample = tuple(sorted({int(round(x)) for x in np.linspace(0, n_q - 1, n_fp64)}))
     domega = s.domega * (s.no - 1) / (no - 1)
     eta = eta_ev / 27.211386245988
     reqs, info = [], []
@@ -455,13 +460,18 @@ def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, fp64_sample=(0, 9,
         chunks = [breqs[i:i + bq] for i in range(0, len(breqs), bq)]
         out, info = [], []
         t = time.perf_counter()
-        objs[0].launch(chunks[0])
-        for j in range(1, len(chunks)):
-            objs[j % nobj].launch(chunks[j])
-            out += objs[(j - 1) % nobj].wait()
-            info.append(objs[(j - 1) % nobj].info())
-        out += objs[(len(chunks) - 1) % nobj].wait()
-        info.append(objs[(len(chunks) - 1) % nobj].info())
+        pending = []  # objects with a launched batch, in launch order
+        for j, ch in enumerate(chunks):
+            o = objs[j % nobj]
+            if o in pending:  # its previous batch (j - nobj) is the oldest pending one
+                out += pending.pop(0).wait()
+                info.append(o.info())
+            o.launch(ch)
+            pending.append(o)
+        while pending:
+            o = pending.pop(0)
+            out += o.wait()
+            info.append(o.info())
         dt = time.perf_counter() - t
         for o in objs:
             o.close()
@@ -472,13 +482,11 @@ def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, fp64_sample=(0, 9,
                 "per_batch": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in x.items()} for x in info],
                 "max_rel_diff_head_vs_server": diff}
 
-    serial = batched_run(16, 1)
-    piped = batched_run(8, 2)
-    batched = dict(piped, serial_16=serial,
-                   note="per-request setup (pairs, sort, vertices, B split) then one graph launch per batch: "
-                        "grouped-tile S0 launches per tile shape, S0 -> FP64, KK and Dyson of every request; "
-                        "value: two batches of 8 alternating (setup of one overlaps the other's graph); "
-                        "serial_16: one batch of 16 at a time")
+    batched = batched_run(16, 1)
+    batched["alternating_2x8"] = {k: v for k, v in batched_run(8, 2).items() if k != "per_batch"}
+    batched["note"] = ("per-request setup (pairs, sort, vertices, B split) then one graph launch per batch of 16: "
+                       "grouped-tile S0 launches per tile shape, S0 -> FP64, KK and Dyson of every request; "
+                       "alternating_2x8: two batches of 8, the setup of one overlapping the other's graph")
     # FP64 GPU sample: the same requests, one at a time on an FP64 shared context
     c64 = rpa.shared_context(parent, rpa.PREC_FP64)
     t64, tmix_one, errs, stages = 0.0, 0.0, [], []
@@ -512,15 +520,20 @@ def dispersion_run(parent, s, n_q: int = 64, nslots: int = 4, fp64_sample=(0, 9,
         parent.close()
     return {"workload": f"{n_q} q-points along Gamma-M-K (|q| {info[0][0]:.4f}-{info[-1][0]:.3f} 2pi/a) on the "
                         f"grid120 basis; loss chain per q (S0, KK, FP64 Dyson, W, Im eps^-1), NGloc 31-151 rising "
-                        f"along the path, nw={no}, eta={eta_ev * 1000:.0f} meV; mixed path: all q submitted at once "
-                        f"to {nslots} shared contexts",
-            "n_q": n_q, "mixed_s": t_mixed, "value": n_q / t_mixed, "unit": "q-spectra/s", "graph_batched": batched,
+                        f"along the path, nw={no}, eta={eta_ev * 1000:.0f} meV; mixed path: rpa_batch, batches of "
+                        f"16 q-points (one CUDA graph each); also all 64 submitted at once to {nslots} shared contexts",
+            "n_q": n_q, "value": batched["value"], "unit": "q-spectra/s", "mixed_s": batched["s"],
+            "path": "rpa_batch: batches of 16 q-points, one CUDA graph each (graph_batched)",
+            "graph_batched": batched,
+            "server_concurrent": {"value": n_q / t_mixed, "s": t_mixed,
+                                  "note": f"all 64 submitted at once to a server of {nslots} shared contexts"},
             "mean_service_s": float(np.mean([x[1][2] for x in res])),
             "fp64_sample": {"q_indices": list(fp64_sample), "ngloc": [info[i][1] for i in fp64_sample],
                             "fp64_s": t64, "mixed_s_one_at_a_time": tmix_one,
                             "fp64_q_spectra_s_est": len(fp64_sample) / t64,
                             "mixed_over_fp64_same_q": t64 / tmix_one,
-                            "mixed_batched_over_fp64": (n_q / t_mixed) / (len(fp64_sample) / t64),
+                            "mixed_batched_over_fp64": batched["value"] / (len(fp64_sample) / t64),
+                            "mixed_server_over_fp64": (n_q / t_mixed) / (len(fp64_sample) / t64),
                             "note": f"FP64 rate from {len(fp64_sample)} q-points evenly spaced along the path "
                                     f"(NGloc {info[fp64_sample[0]][1]}-{info[fp64_sample[-1]][1]}), run one at "
                                     f"a time; the mixed rate is the batched 64-q run"},
@@ -681,6 +694,8 @@ def main():
                     help="also time the k-point bookkeeping (genFBZ / findKinIBZ / findKQinBZ) on a 120x120 C6v grid")
     ap.add_argument("--no-dispersion", action="store_true",
                     help="skip the 64-q loss-function dispersion (mixed path batched, FP64 GPU path on 8 q-points)")
+    ap.add_argument("--dispersion", action="store_true",
+                    help="run the dispersion on --config's basis too (it runs on grid120 by default)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -900,7 +915,9 @@ def main():
     serving = disp = None
     if rank == 0 and not args.no_serve and args.precision == "mixed":
         serving = serving_run()
-    if rank == 0 and not args.no_dispersion and args.precision == "mixed" and args.config == "grid120":
+        serving["with_batching_worker"] = serving_run(batch_q=8)
+    if rank == 0 and not args.no_dispersion and args.precision == "mixed" and (args.config == "grid120" or
+                                                                              args.dispersion):
         disp = dispersion_run(ctx, s)
     kmap = kmap_run() if rank == 0 and args.kmap else None
     serving_c4 = None

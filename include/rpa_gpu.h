@@ -417,6 +417,17 @@ const char* rpa_server_last_error(const rpa_server* srv);
 /* Finishes the queued requests, stops the workers, destroys the contexts. */
 int rpa_server_destroy(rpa_server* srv);
 
+/* A server as rpa_server_create plus one batching worker (no counterpart in
+ * the reference): when free, it takes up to batch_q queued W requests (charge
+ * mode, Sloss KK, no S0 / Qeff / chi0 outputs) in arrival order, as many as fit
+ * the budget next to the running requests, and runs them as one rpa_batch
+ * (per-request setup, then one CUDA graph with the grouped-tile S0 launches and
+ * every request's KK and Dyson).  The slot workers keep taking requests of
+ * any kind.  parent must be RPA_PREC_MIXED (the batch's contexts are mixed). */
+int rpa_server_create_batched(rpa_server** out, rpa_ctx* parent, int nslots, double mem_bytes, int batch_q);
+/* Requests completed through the batching worker so far. */
+int rpa_server_batched_count(const rpa_server* srv, long long* n);
+
 /* ---- Batched W requests in one CUDA graph (no counterpart in the reference) --
  * A batch owns max_q shared contexts on parent's resident basis (parent must be
  * RPA_PREC_MIXED).  rpa_batch_run solves nq <= max_q W requests (RPA_REQ_W,

@@ -72,6 +72,35 @@ def test_results_same_alone_and_in_the_mix(parent, rpa, synth):
             assert rel(outs[k], ref[k]) <= TOL_SAME, k
 
 
+def test_batching_worker_results_same_as_alone(parent, rpa, synth):
+    """rpa_server_create_batched: the W requests (without chi0 output) that the
+    batching worker runs as one rpa_batch give the W and eps^-1_11 of the
+    same requests served one at a time, and the chi0 requests are still
+    served by the slot workers."""
+    s, ctx = parent
+    reqs = _requests(rpa, synth, s)
+    for r in reqs:
+        if r["kind"] == rpa.REQ_W:
+            r["want_chi0"] = False
+    alone = []
+    srv = rpa.Server(ctx, nslots=1, mem_bytes=1e9)
+    for r in reqs:
+        alone.append(srv.wait(srv.submit(**r))[0])
+    srv.close()
+    # one slot worker that is kept busy by a first chi0 request, so the W
+    # requests queued behind it go to the batching worker
+    srv = rpa.Server(ctx, nslots=1, mem_bytes=1e9, batch_q=4)
+    ids = [srv.submit(**r) for r in reqs]
+    mixed = [srv.wait(i)[0] for i in ids]
+    n_batched = srv.batched_count()
+    srv.close()
+    assert n_batched >= 1
+    for outs, ref in zip(mixed, alone):
+        assert set(outs) == set(ref)
+        for k in ref:
+            assert rel(outs[k], ref[k]) <= TOL_SAME, k
+
+
 def test_server_request_equals_a_context_call(parent, rpa, synth):
     s, ctx = parent
     r = _requests(rpa, synth, s)[2]  # W request, q = 3 grid steps

@@ -7,9 +7,11 @@
 // the TMEM read-back before the accumulation kernels rely on them.
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "rpa_internal.cuh"
 #include "tc05.cuh"
@@ -124,6 +126,129 @@ int selftest_umma(int which, double* result) {
     k_umma_selftest<256><<<1, 128, smem>>>(nchunks, 12345u, out, ref, status);
   }
   e = cudaDeviceSynchronize();
+  std::vector<float> ho(n), hr(n);
+  int st = 0;
+  if (e == cudaSuccess) {
+    cudaMemcpy(ho.data(), out, n * 4, cudaMemcpyDeviceToHost);
+    cudaMemcpy(hr.data(), ref, n * 4, cudaMemcpyDeviceToHost);
+    cudaMemcpy(&st, status, 4, cudaMemcpyDeviceToHost);
+  }
+  cudaFree(out);
+  cudaFree(ref);
+  cudaFree(status);
+  if (e != cudaSuccess) return RPA_ECUDA;
+  if (st) return RPA_ETIMEOUT;
+  double mx = 0, mref = 0;
+  for (size_t i = 0; i < n; ++i) {
+    mx = std::max(mx, (double)std::fabs(ho[i] - hr[i]));
+    mref = std::max(mref, (double)std::fabs(hr[i]));
+  }
+  *result = mref > 0 ? mx / mref : mx;
+  return RPA_OK;
+}
+
+// The same GEMM with A in tensor memory (tcgen05.mma with an [a_tmem]
+// operand, kind::f16 with f16 inputs): each warp writes the rows of its lane
+// quadrant, two f16 of K per 32-bit column (K = 64 per chunk: 32 columns);
+// B stays a 128-byte-swizzled K-major tile in shared memory.  Checks the A
+// layout in TMEM before a kernel relies on it.
+template <int N>
+__global__ void __launch_bounds__(128) k_umma_ts_selftest(int nchunks, uint32_t seed, float* out, float* ref,
+                                                          int* status) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(sm) + 1023) & ~uintptr_t(1023));
+  unsigned char* B = base;  // N x 128 B
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tslot;
+  constexpr uint32_t NCOL = N + 32 <= 64 ? 64 : (N + 32 <= 128 ? 128 : (N + 32 <= 256 ? 256 : 512));
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) {
+    tc::tmem_alloc(&tslot, NCOL);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t taddr = tslot;
+  const uint32_t acol = (uint32_t)N;  // A columns follow the accumulator
+  bool ok = true;
+  const int row = warp * 32 + lane;
+  for (int c = 0; c < nchunks && ok; ++c) {
+    // A row `row`: K values c*64 .. c*64+63, packed two per column
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+      uint32_t v[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int k = g * 16 + 2 * i;
+        const __half2 h = __floats2half2_rn(hval(row, c * 64 + k, seed), hval(row, c * 64 + k + 1, seed));
+        v[i] = *reinterpret_cast<const uint32_t*>(&h);
+      }
+      tc::tmem_st8(taddr + ((uint32_t)(warp * 32) << 16) + acol + (uint32_t)(g * 8), v);
+    }
+    tc::tmem_st_wait();
+    for (int e = tid; e < N * 64; e += 128) {
+      int r = e >> 6, k = e & 63;
+      *reinterpret_cast<__half*>(B + tc::sw128_off(r, k)) = __float2half_rn(hval(1000 + r, c * 64 + k, seed));
+    }
+    tc::fence_async_smem();
+    tc::tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc::tc_fence_after();
+      const uint32_t idesc = tc::idesc_bf16(128, N, true);
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks)
+        tc::mma_ts(taddr, taddr + acol + (uint32_t)(ks * 8), tc::desc_sw128(tc::smem_u32(B) + ks * 32), idesc,
+                   (c > 0 || ks > 0) ? 1u : 0u);
+      tc::mma_commit(&bar);
+    }
+    ok = tc::mbar_wait(&bar, c & 1, 1u << 16);
+    if (!ok) atomicExch(status, 1);
+    tc::tc_fence_after();
+    __syncthreads();
+  }
+  if (ok) {
+    for (int c0 = 0; c0 < N; c0 += 32) {
+      float v[32];
+      tc::tmem_ld32(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      tc::tmem_ld_wait();
+#pragma unroll
+      for (int i = 0; i < 32; ++i)
+        if (c0 + i < N) out[row * N + c0 + i] = v[i];
+    }
+  }
+  for (int e = tid; e < 128 * N; e += 128) {
+    int r = e / N, n = e % N;
+    float s = 0.f;
+    for (int k = 0; k < nchunks * 64; ++k)
+      s += __half2float(__float2half_rn(hval(r, k, seed))) * __half2float(__float2half_rn(hval(1000 + n, k, seed)));
+    ref[e] = s;
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
+}
+
+int selftest_umma_ts(double* result) {
+  constexpr int N = 192;
+  const int nchunks = 3;
+  float *out = nullptr, *ref = nullptr;
+  int* status = nullptr;
+  size_t n = (size_t)128 * N;
+  if (cudaMalloc(&out, n * 4) != cudaSuccess || cudaMalloc(&ref, n * 4) != cudaSuccess ||
+      cudaMalloc(&status, 4) != cudaSuccess)
+    return RPA_ENOMEM;
+  cudaMemset(out, 0, n * 4);
+  cudaMemset(status, 0, 4);
+  size_t smem = 1024 + (size_t)N * 128;
+  cudaFuncSetAttribute(k_umma_ts_selftest<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_umma_ts_selftest<N><<<1, 128, smem>>>(nchunks, 4321u, out, ref, status);
+  cudaError_t e = cudaDeviceSynchronize();
   std::vector<float> ho(n), hr(n);
   int st = 0;
   if (e == cudaSuccess) {

@@ -40,6 +40,7 @@ int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singul
 void kk_matrix(int variant, int no, double domega, std::vector<double>& K, int* nw_out);
 int selftest_umma(int which, double* result);
 int selftest_wait(double* result);
+int selftest_umma_ts(double* result);
 int gk_sort_host(const double* k, int npwx, int ngm, const double* g, double ecut, int* ngk, int* igk, double* gk);
 
 static thread_local std::string g_create_err;
@@ -962,8 +963,9 @@ int rpa_chi0_stats(const rpa_ctx* c, double* out4) {
 }
 
 int rpa_selftest(int which, double* result) {
-  if (!result || which < 0 || which > 3) return RPA_EINVAL;
+  if (!result || which < 0 || which > 4) return RPA_EINVAL;
   if (which == 3) return selftest_wait(result);
+  if (which == 4) return selftest_umma_ts(result);
   return selftest_umma(which, result);
 }
 

@@ -342,7 +342,10 @@ int rpa_accum_tile(const rpa_ctx* ctx, int* gb, int* nio);
  * values.  Returns RPA_ETIMEOUT if the bounded completion wait gave up.
  * which = 3 waits on an mbarrier that nothing arrives on: the bounded wait
  * gives up (a few milliseconds) and the call returns RPA_ETIMEOUT with *result
- * = the cycles waited, leaving the device usable. */
+ * = the cycles waited, leaving the device usable.
+ * which = 4 runs the 128 x 192 x 192 GEMM with f16 inputs and A in tensor
+ * memory (tcgen05.mma with an [a_tmem] operand, two f16 of K per 32-bit
+ * column, rows in lanes), B from a swizzled shared-memory tile. */
 int rpa_selftest(int which, double* result);
 
 /* Number of CUDA kernels this context has launched so far (its own kernels;

@@ -19,3 +19,8 @@ def test_bounded_wait_times_out_and_the_device_stays_usable(rpa):
     assert L.rpa_selftest(3, C.byref(cycles)) == rpa.RPA_ETIMEOUT
     assert cycles.value > 0
     assert rpa.selftest(0) < 1e-5
+
+
+def test_umma_with_a_in_tensor_memory(rpa):
+    """tcgen05.mma with A in TMEM (rows in lanes, two f16 of K per column)."""
+    assert rpa.selftest(4) < 1e-5

@@ -48,12 +48,19 @@ constexpr uint32_t pow2_at_least(uint32_t x) {
   return p;
 }
 
+// Whether a shape forms its A tiles in tensor memory: the two TMEM
+// accumulator buffers (2 x NIO x NC x GB columns) and two A slots of NIO x
+// (hi, lo) x 32 columns (64 K values of 16 bits, two per column) fit the 512
+// columns.  Otherwise the A tiles are formed in shared memory.
+constexpr bool ws_atmem(int nio, bool cplx, int gb) { return 2 * nio * (cplx ? 2 : 1) * gb + 2 * nio * 64 <= 512; }
+
 // Shared-memory stages of the warp-specialised kernel's ring for a shape
-// (the bytes of one stage: pre-split B tiles, separate A-side tiles, records).
+// (the bytes of one stage: pre-split B tiles, separate A-side tiles, records;
+// beside them two A slots in shared memory unless they are in TMEM).
 constexpr int ws_stages(int nio, bool cplx, bool sepa, int gb) {
   const long long tile = (long long)gb * 128, bsrc = 2LL * (cplx ? 2 : 1) * tile;
   const long long data = (bsrc + (sepa ? 2 * tile : 0) + TC_TT * (long long)sizeof(Trans) + 1023) / 1024 * 1024;
-  const long long formed = (long long)nio * 2 * TC_GA * 128;
+  const long long formed = ws_atmem(nio, cplx, gb) ? 0 : (long long)nio * 2 * TC_GA * 128;
   return (int)((232448 - 2 * formed - 1024 - 3072) / data);
 }
 
@@ -77,14 +84,16 @@ struct WsCfg {
   static constexpr uint32_t ASRC = 2 * TILE;                        // separate A-side tiles (M2 != M)
   static constexpr uint32_t REC_OFF = BSRC + (SEPA ? ASRC : 0);
   static constexpr uint32_t DATA = (REC_OFF + TC_TT * sizeof(Trans) + 1023) / 1024 * 1024;
-  static constexpr uint32_t FORMED = NIO * 2 * A_BYTES;             // (Ah, Al) x NIO
+  static constexpr bool ATMEM = ws_atmem(NIO, CPLX, GB);            // A slots in TMEM
+  static constexpr uint32_t FORMED = ATMEM ? 0 : NIO * 2 * A_BYTES;  // (Ah, Al) x NIO in shared memory
   static constexpr int S0 = ws_stages(NIO, CPLX, SEPA, GB);
   static constexpr int S = S0 > 6 ? 6 : S0;
   static constexpr size_t SMEM = (size_t)S * DATA + 2 * FORMED + 1024;
   static constexpr uint32_t NMMA = NC * GB;                         // N of one MMA
   static constexpr uint32_t DCOLS = NIO * NMMA;                     // accumulator columns per TMEM buffer
   static constexpr int CW = (int)((DCOLS + 95) / 96 * 32);          // columns per formation thread
-  static constexpr uint32_t NCOL = pow2_at_least(2 * DCOLS);        // TMEM columns allocated
+  static constexpr uint32_t ACOL = 2 * DCOLS;                       // first TMEM column of the A slots
+  static constexpr uint32_t NCOL = pow2_at_least(2 * DCOLS + (ATMEM ? 2 * NIO * 64 : 0));  // TMEM columns allocated
   static_assert(GB % 16 == 0 && GB <= TC_GA, "G tile");
   static_assert(NMMA % 16 == 0 && NMMA <= 256, "MMA N");
   static_assert(DCOLS % 32 == 0 && DCOLS <= 192, "accumulator layout");
@@ -150,9 +159,11 @@ __device__ __forceinline__ void accum_ws_cta(const AccTcCtx& A, const unsigned c
     range[0] = lb_lo(A.rec, A.n_inter, r0 - A.wmax + 1) & ~(TC_TT - 1);
     range[1] = lb_lo(A.rec, A.n_inter, r0 + NIO);
   }
-  // A padding rows (G >= nlf) stay zero for the whole kernel
-  for (uint32_t e = tid; e < 2 * FORMED / 16; e += WS_THREADS)
-    reinterpret_cast<uint4*>(fbase)[e] = make_uint4(0, 0, 0, 0);
+  // A padding rows (G >= nlf) stay zero for the whole kernel (shared-memory A
+  // slots; TMEM A slots are written whole for every chunk)
+  if constexpr (!Cfg::ATMEM)
+    for (uint32_t e = tid; e < 2 * FORMED / 16; e += WS_THREADS)
+      reinterpret_cast<uint4*>(fbase)[e] = make_uint4(0, 0, 0, 0);
   tc::fence_async_smem();
   tc::tc_fence_before();
   __syncthreads();
@@ -215,9 +226,27 @@ __device__ __forceinline__ void accum_ws_cta(const AccTcCtx& A, const unsigned c
         if (!ok) break;
         tc::tc_fence_after();
         const uint32_t bh = tc::smem_u32(stage(c)), bl = bh + Cfg::BHALF;
-        const uint32_t as = tc::smem_u32(slot(c));
         const uint32_t d0 = taddr + (uint32_t)(((c >> 1) & 1) * DCOLS);
         const uint32_t first = (c & 1) ? 1u : 0u;
+        if constexpr (Cfg::ATMEM) {
+          // A slot c % 2 in TMEM: per row j, hi in columns 0-31, lo in 32-63
+          // (K step ks at column 8 ks)
+          const uint32_t a0 = taddr + Cfg::ACOL + (uint32_t)(c & 1) * (uint32_t)(NIO * 64);
+#pragma unroll
+          for (int j = 0; j < NIO; ++j) {
+            const uint32_t ah = a0 + (uint32_t)j * 64u, al = ah + 32u;
+            const uint32_t d = d0 + (uint32_t)j * NMMA;
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+              const uint32_t ko = ks * 32;
+              tc::mma_ts(d, ah + ks * 8, tc::desc_sw128(bl + ko), idesc, ks > 0 ? 1u : first);
+              tc::mma_ts(d, al + ks * 8, tc::desc_sw128(bh + ko), idesc, 1u);
+            }
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) tc::mma_ts(d, ah + ks * 8, tc::desc_sw128(bh + ks * 32), idesc, 1u);
+          }
+        } else {
+        const uint32_t as = tc::smem_u32(slot(c));
 #pragma unroll
         for (int j = 0; j < NIO; ++j) {
           const uint32_t ah = as + j * 2 * A_BYTES, al = ah + A_BYTES;
@@ -234,6 +263,7 @@ __device__ __forceinline__ void accum_ws_cta(const AccTcCtx& A, const unsigned c
             const uint32_t ko = ks * 32;
             tc::mma_bf16(d, tc::desc_sw128(ah + ko), tc::desc_sw128(bh + ko), idesc, 1u);
           }
+        }
         }
         tc::mma_commit(&mdone[c & 1]);
         tc::mma_commit(&dfree[c % S]);
@@ -352,6 +382,51 @@ __device__ __forceinline__ void accum_ws_cta(const AccTcCtx& A, const unsigned c
       // separate A-side tile), re-split
       const unsigned char* srch = st + (SEPA ? Cfg::BSRC : 0);
       const unsigned char* srcl = srch + (SEPA ? Cfg::TILE : Cfg::BHALF);
+      if constexpr (Cfg::ATMEM) {
+        // TMEM A slot c % 2: this thread forms row grow (its lane quadrant) for
+        // the 16-bit K chunks ch = cg, cg + 3, cg + 6 (8 K values, 4 columns
+        // each); rows >= nrowA are written as zeros
+        tc::tc_fence_after();  // the slot's previous MMAs (chunk c - 2) are done
+        const uint32_t arow = taddr + ((uint32_t)(wq * 32) << 16) + Cfg::ACOL + (uint32_t)(c & 1) * (uint32_t)(NIO * 64);
+        const bool rowok = grow < nrowA;
+#pragma unroll
+        for (int k3 = 0; k3 < 3; ++k3) {
+          const int ch = cg + 3 * k3;
+          if (ch < 8) {
+            float x[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) x[i] = 0.f;
+            if (rowok) {
+              const uint32_t off = (uint32_t)grow * 128u + ((uint32_t)(ch ^ (grow & 7)) << 4);
+              const uint4 h = *reinterpret_cast<const uint4*>(srch + off);
+              const uint4 l = *reinterpret_cast<const uint4*>(srcl + off);
+              const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+              for (int i = 0; i < 4; ++i) {
+                const float2 fh = __half22float2(*reinterpret_cast<const __half2*>(&hw[i]));
+                const float2 fl = __half22float2(*reinterpret_cast<const __half2*>(&lw[i]));
+                x[2 * i] = fh.x + fl.x;
+                x[2 * i + 1] = fh.y + fl.y;
+              }
+            }
+            const int tt0 = (ch & 3) * 8;
+#pragma unroll
+            for (int j = 0; j < NIO; ++j) {
+              const float4 w0 = *reinterpret_cast<const float4*>(&wtab[c & 1][j][tt0]);
+              const float4 w1 = *reinterpret_cast<const float4*>(&wtab[c & 1][j][tt0 + 4]);
+              const float y[8] = {x[0] * w0.x, x[1] * w0.y, x[2] * w0.z, x[3] * w0.w,
+                                  x[4] * w1.x, x[5] * w1.y, x[6] * w1.z, x[7] * w1.w};
+              uint4 hi, lo;
+              split8<true>(y, hi, lo);
+              const uint32_t col = arow + (uint32_t)j * 64u + (uint32_t)ch * 4u;
+              tc::tmem_st4(col, hi.x, hi.y, hi.z, hi.w);
+              tc::tmem_st4(col + 32u, lo.x, lo.y, lo.z, lo.w);
+            }
+          }
+        }
+        tc::tmem_st_wait();
+        tc::tc_fence_before();
+      } else {
 #pragma unroll 2
       for (int e = tid; e < nrowA * 8; e += WS_SIMT) {
         const int row = e >> 3, ch = e & 7;
@@ -379,6 +454,7 @@ __device__ __forceinline__ void accum_ws_cta(const AccTcCtx& A, const unsigned c
           *reinterpret_cast<uint4*>(fs + j * 2 * A_BYTES + off) = hi;
           *reinterpret_cast<uint4*>(fs + j * 2 * A_BYTES + A_BYTES + off) = lo;
         }
+      }
       }
       tc::fence_async_smem();
       __syncwarp();

@@ -81,3 +81,58 @@ def test_accumulation_tile_layout():
     assert np.abs(D[:nlf, :nlf] - ref.real).max() <= 2e-6 * scale
     assert np.abs(D[:nlf, GB:GB + nlf] - ref.imag).max() <= 2e-6 * scale
     assert np.abs(D[nlf:, :]).max() == 0 and np.abs(D[:, nlf:GB]).max() == 0
+
+
+def test_accumulation_with_a_in_tensor_memory():
+    """The A tile formed in tensor memory (shapes whose TMEM columns fit): row
+    G of the tile in lane G, the 16-bit K values of chunk ch (8 values) in the
+    four 32-bit columns 4 ch .. 4 ch + 3, two per column (even K in the low
+    half), hi in columns 0-31 and lo in 32-63 of the slot; the MMA of K step
+    ks reads columns 8 ks .. 8 ks + 7 of hi and of lo.  Against the B tiles of
+    k_presplit_ws read as the K-major descriptor reads them, the three split
+    products give the chunk's complex S0 contribution, as the shared-memory A
+    tile does."""
+    rng = np.random.default_rng(5)
+    nlf = 91
+    M = (rng.standard_normal((TT, nlf)) + 1j * rng.standard_normal((TT, nlf))).astype(np.complex64)
+    w = rng.standard_normal(TT).astype(np.float32)
+    B = {h: np.zeros((2 * GB, 64)) for h in ("hi", "lo")}
+    for rem in range(GB * 4):
+        row, grp = rem >> 2, rem & 3
+        b = M[grp * 8: grp * 8 + 8, row] if row < nlf else np.zeros(8, dtype=np.complex64)
+        rh, rl = _split(b.real)
+        ih, il = _split(b.imag)
+        _st16(B["hi"], row, grp, rh)
+        _st16(B["lo"], row, grp, rl)
+        _st16(B["hi"], row, 4 + grp, ih)
+        _st16(B["lo"], row, 4 + grp, il)
+        _st16(B["hi"], GB + row, grp, -ih)
+        _st16(B["lo"], GB + row, grp, -il)
+        _st16(B["hi"], GB + row, 4 + grp, rh)
+        _st16(B["lo"], GB + row, 4 + grp, rl)
+    # TMEM slot: lanes x 64 columns of two 16-bit values (column col holds K = 2 col, 2 col + 1)
+    tm = np.zeros((128, 64, 2))
+    for lane in range(128):
+        for ch in range(8):
+            part, grp = ch >> 2, ch & 3
+            if lane < nlf:
+                b = M[grp * 8: grp * 8 + 8, lane]
+                bh, bl = _split(b.imag if part else b.real)
+                x = (bh + bl).astype(np.float32) * w[grp * 8: grp * 8 + 8]
+            else:
+                x = np.zeros(8, dtype=np.float32)
+            ah, al = _split(x)
+            for q in range(4):  # column 4 ch + q holds K values 8 ch + 2q, 8 ch + 2q + 1
+                tm[lane, 4 * ch + q] = ah[2 * q: 2 * q + 2]
+                tm[lane, 32 + 4 * ch + q] = al[2 * q: 2 * q + 2]
+    D = np.zeros((128, 2 * GB))
+    for ks in range(4):
+        Ah = tm[:, 8 * ks: 8 * ks + 8].reshape(128, 16)
+        Al = tm[:, 32 + 8 * ks: 32 + 8 * ks + 8].reshape(128, 16)
+        Bh, Bl = _read(B["hi"], 2 * GB, ks), _read(B["lo"], 2 * GB, ks)
+        D += Ah @ Bl.T + Al @ Bh.T + Ah @ Bh.T
+    ref = ((M.T * w) @ M.conj()).astype(np.complex128)
+    scale = np.abs(ref).max()
+    assert np.abs(D[:nlf, :nlf] - ref.real).max() <= 2e-6 * scale
+    assert np.abs(D[:nlf, GB:GB + nlf] - ref.imag).max() <= 2e-6 * scale
+    assert np.abs(D[nlf:, :]).max() == 0

@@ -19,22 +19,30 @@
 // of bands.  The MMA operands are MN-major: a K row of the X tile holds 128
 // (G, band) rows, 8 bands per 16-byte chunk, so each gathered (G, plane wave,
 // plane) lands with 16-byte cp.async copies and no transposition.  K order in a
-// chunk of 32 plane waves: rows 0-31 real parts, 32-63 imaginary parts.  The Y
-// tile holds two column blocks, [y | y'] with y' = (-Im y rows 0-31, Re y rows
-// 32-63), so one MMA of N = 2 NYN per K step gives
-//     Re D = X . y  and  Im D = X . y' = X[Re] . (-Im y) + X[Im] . Re y
-// The threads that copy a y chunk write its y' image.  Per K step three MMAs
-// of N = 2 NYN into one accumulator, small products first: Xl . Yh, Xh . Yl,
-// Xh . Yh.  (The tensor core reads its operands from shared memory at 128
-// bytes per cycle: an N = 128 MMA just keeps up.)  The current factor separates,
-// f(G,i) = a(G) + b(i): the b(i) c block (precomputed per launch, split like the
-// coefficient planes) is a second column block of y, and a(G) multiplies the c
-// block at read-back: M = a(G) D[c] + D[b c].  Each local-field tile sweeps the plane waves in the
-// opposite direction of the previous one, so the coefficient rows read last
-// are read again first while they are still in L2.
+// chunk of 32 plane waves: rows 0-31 real parts, 32-63 imaginary parts, so
+//     Re D = X[Re] . Re y + X[Im] . Im y,   Im D = X[Im] . Re y - X[Re] . Im y
+// Current vertices: the factor separates, f(G,i) = a(G) + b(i), and the column
+// blocks of y are [c | b1 c | b2 c] (b c precomputed per launch, split like the
+// coefficient planes; b2 c only when two Cartesian components are wanted --
+// the yz / zy pair, or a second polarisation prefetched beside the first,
+// which then shares the gathers of X and the D[c] block); a(G) multiplies the
+// c block at read-back: M_mu = a_mu(G) D[c] + D[b_mu c].
+// One or two column blocks (charge; current, one component): the Y tile holds
+// [y | y'] with y' = (-Im y rows 0-31, Re y rows 32-63), written by the threads
+// that copy the y chunk, and three MMAs of N = 2 NYN per K step give
+// Re D = X . y and Im D = X . y'.  Three blocks: [y | y'] would not leave room
+// for three stages, so the Y tile holds y alone; per K step (16 rows) three
+// MMAs of N = NYN give Re D from the same K rows of X and Y, and three more
+// give Im D from X's rows and the other half of Y's K rows, negated
+// (instruction-descriptor bit) where X holds real parts.
+// Small products first: Xl . Yh, Xh . Yl, Xh . Yh.  (The tensor core reads its
+// operands from shared memory at 128 bytes per cycle: an N = 128 MMA just
+// keeps up.)  Each local-field tile sweeps the plane waves in the opposite
+// direction of the previous one, so the coefficient rows read last are read
+// again first while they are still in L2.
 // Each chunk goes into a fresh TMEM accumulator that the worker warps add to
-// FP32 registers; a ring of four accumulators keeps the MMA warp from waiting
-// for the read-back of the chunk before last.
+// FP32 registers; a ring of accumulators (four, two when 192 columns wide)
+// keeps the MMA warp from waiting for the read-back of the chunk before last.
 // Warp roles: 16 worker warps gather chunk t + S - 1 into the ring of S
 // shared-memory stages and read back chunk t - 1 from TMEM; warp 16 issues
 // the MMAs.  Every wait is bounded and ends in an error status.
@@ -59,19 +67,21 @@ struct VtxMnCtx {
   const int* npw;
   const __half* planes;   // [kibz][npwx][4][nbp]
   const __half* ybt;      // [k_local][nsum_max][4][nbp]: b(i) c split like the planes (current vertices)
+  const __half* ybt2;     // the same for the second Cartesian component (three column blocks)
   const int16_t* map;     // [k_local][nlf][nsum_max]: gathered-side position of (G, i), -1 none
   const Trans* trans;
   const long long* offsets;
   const int* pos_of;
   float2* M;
-  unsigned* amax;
+  float2* M2;             // vertex rows of the second component (three column blocks)
+  unsigned* amax;         // [2]: max |M|, max |M2| (float bits)
   int* status;
   int k0, nlf, npwx, nbp, nsum_max, legacy, nsum_legacy;
   int swap;               // 1: x = bands n of K1 (inverse map), y = bands m of K2
   int xs, xb, xo0, xo1;   // gathered window: first band, rows per G (multiple of 8), owned bands
   int ys, yo0, yo1;       // sequential window: first band (multiple of 8), owned bands
   int gpt;                // local fields per 128-row tile
-  int comp;
+  int comp, comp2;         // Cartesian components of b(i) c and b2(i) c
   double q0, q1, q2, Gcar;
   float a_scale, out_scale;
 };
@@ -83,11 +93,14 @@ constexpr uint32_t VM_SPINS = 1u << 16;         // suspending polls: about 1.3 s
 constexpr int VM_SMEM_MAX = 232448 - 1024;      // dynamic shared memory left beside the static part
 constexpr int VM_SMAX = 6;
 
-template <int NBY, bool CURRENT>
+// NB column blocks of y: 1 = charge (y), 2 = current (c, b c), 3 = current
+// with a second component (c, b1 c, b2 c).
+template <int NBY, int NB>
 struct VmCfg {
-  static constexpr int NY = CURRENT ? 2 : 1;
-  static constexpr int NYN = NY * NBY;                   // columns of one block (y or y')
-  static constexpr int NTA = (2 * NYN + 63) / 64;        // 64-wide atoms along N of one half (lo or hi) of Y
+  static constexpr bool IMG = NB <= 2;                   // y' images in the Y tile
+  static constexpr int NYN = NB * NBY;                   // columns of Re D (and of Im D)
+  static constexpr int NYT = IMG ? 2 * NYN : NYN;        // columns of the Y tile
+  static constexpr int NTA = (NYT + 63) / 64;            // 64-wide atoms along N of one half (lo or hi) of Y
   static constexpr uint32_t XH = 64 * 128 * 2;           // one half (hi or lo) of X
   static constexpr uint32_t YKG = (uint32_t)NTA * 2048;  // Y bytes per group of 8 K rows: hi atoms, then lo atoms
   static constexpr uint32_t YLO = (uint32_t)NTA * 1024;  // offset of the lo atoms in a K group
@@ -95,12 +108,14 @@ struct VmCfg {
   static constexpr uint32_t PTAB = 32 * NBY * 4;         // int32 [32][NBY]
   static constexpr int S0 = (int)((VM_SMEM_MAX - 1024 - (int)PTAB) / (int)STAGE);
   static constexpr int S = S0 > VM_SMAX ? VM_SMAX : S0;
-  static constexpr uint32_t N2 = 64 * NTA;                // accumulator columns (y and y', padded)
-  static constexpr int NBUF = 4;                         // TMEM accumulators in the ring
+  // accumulator columns: Re D then Im D (with images: one MMA of N = 64 NTA over both)
+  static constexpr uint32_t N2 = IMG ? 64 * NTA : 2 * NYN;
+  static constexpr int NBUF = N2 <= 128 ? 4 : 2;         // TMEM accumulators in the ring
   static constexpr uint32_t NCOL = NBUF * N2 <= 256 ? 256 : 512;
   static constexpr int CW = NBY / 4;                     // columns per thread per block
   static constexpr size_t SMEM = (size_t)S * STAGE + PTAB + 1024;
-  static_assert(NBY % 16 == 0 && NTA <= 2, "window too wide");
+  static_assert(NBY % 16 == 0 && NTA <= 2 && NYN <= 256, "window too wide");
+  static_assert(NBUF * N2 <= 512, "accumulator ring beyond TMEM");
   static_assert(S >= 3, "shared-memory ring too shallow");
 };
 
@@ -146,9 +161,11 @@ __device__ __forceinline__ void tmem_ld_n(uint32_t addr, float* v) {
 }
 
 // One CTA per FBZ k-point of the launch.
-template <int NBY, bool CURRENT>
+template <int NBY, int NB>
 __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
-  using Cfg = VmCfg<NBY, CURRENT>;
+  using Cfg = VmCfg<NBY, NB>;
+  constexpr bool CURRENT = NB > 1, IMG = Cfg::IMG;
+  constexpr int NP = CURRENT ? NB - 1 : 1;  // vertex sets written
   constexpr int S = Cfg::S, NYN = Cfg::NYN, CW = Cfg::CW;
   constexpr uint32_t XH = Cfg::XH, YKG = Cfg::YKG, YLO = Cfg::YLO, STAGE = Cfg::STAGE;
 
@@ -204,8 +221,12 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
     // ---------------------------------------------------------------- MMA warp
     if (lane == 0) {
       constexpr uint32_t N2 = Cfg::N2;
-      constexpr int NB = Cfg::NBUF;
-      const uint32_t id = tc::idesc_f16_mn(128, N2, false);
+      constexpr int NBF = Cfg::NBUF;
+      constexpr uint64_t YG2 = 2 * (YKG >> 4);  // descriptor step of 16 K rows of Y
+      // with images: one MMA over [y | y'];  three blocks: N = NYN for Re D, the
+      // same with B negated for the -X[Re] . Im y part of Im D
+      const uint32_t id = tc::idesc_f16_mn(128, IMG ? N2 : (uint32_t)NYN, false);
+      const uint32_t idn = tc::idesc_f16_mn(128, IMG ? N2 : (uint32_t)NYN, true);
       // descriptors of stage 0; a chunk adds its byte offsets / 16 to the start-address field
       const uint64_t dx0 = tc::desc_sw128_mn(sbase, 1024u, 2048u);
       const uint64_t dy0 = tc::desc_sw128_mn(sbase + 2 * XH, 1024u, YKG);
@@ -214,7 +235,7 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
       for (int t = 0; t < total; ++t) {
         if (abort_flag) break;
         if (!tc::mbar_wait(&full[s], (uint32_t)ph, VM_SPINS) ||
-            (t >= NB && !tc::mbar_wait(&tfree[t % NB], (uint32_t)((t / NB - 1) & 1), VM_SPINS))) {
+            (t >= NBF && !tc::mbar_wait(&tfree[t % NBF], (uint32_t)((t / NBF - 1) & 1), VM_SPINS))) {
           atomicExch(V.status, 1);
           abort_flag = 1;
           break;
@@ -222,20 +243,29 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
         tc::tc_fence_after();
         const uint64_t so = (uint64_t)(((uint32_t)s * STAGE) >> 4);
         const uint64_t dx = dx0 + so, dy = dy0 + so;
-        const uint32_t d = taddr + (uint32_t)((t % NB) * N2);
+        const uint32_t d = taddr + (uint32_t)((t % NBF) * N2);
 #pragma unroll
         for (int ks = 0; ks < 4; ++ks) {
           const uint64_t xh = dx + (uint64_t)(ks * 256), xl = xh + (XH >> 4);
-          const uint64_t yh = dy + (uint64_t)(ks * 2 * (YKG >> 4)), yl = yh + (YLO >> 4);
-          tc::mma_bf16(d, xl, yh, id, ks > 0 ? 1u : 0u);  // Xl . Yh
-          tc::mma_bf16(d, xh, yl, id, 1u);                // + Xh . Yl
-          tc::mma_bf16(d, xh, yh, id, 1u);                // + Xh . Yh
+          const uint64_t yh = dy + (uint64_t)ks * YG2, yl = yh + (YLO >> 4);
+          const uint32_t acc = ks > 0 ? 1u : 0u;
+          tc::mma_bf16(d, xl, yh, id, acc);  // Xl . Yh
+          tc::mma_bf16(d, xh, yl, id, 1u);   // + Xh . Yl
+          tc::mma_bf16(d, xh, yh, id, 1u);   // + Xh . Yh
+          if constexpr (!IMG) {
+            // Im D: K rows of X against the other half of Y's K rows
+            const uint64_t ih = dy + (uint64_t)(ks ^ 2) * YG2, il = ih + (YLO >> 4);
+            const uint32_t ii = ks < 2 ? idn : id;
+            tc::mma_bf16(d + (uint32_t)NYN, xl, ih, ii, acc);
+            tc::mma_bf16(d + (uint32_t)NYN, xh, il, ii, 1u);
+            tc::mma_bf16(d + (uint32_t)NYN, xh, ih, ii, 1u);
+          }
         }
-        tc::mma_commit(&done[t % NB]);
+        tc::mma_commit(&done[t % NBF]);
         last = t;
         if (++s == S) s = 0, ph ^= 1;
       }
-      if (last >= 0) tc::mbar_wait(&done[last % NB], (uint32_t)((last / NB) & 1), VM_SPINS);
+      if (last >= 0) tc::mbar_wait(&done[last % NBF], (uint32_t)((last / NBF) & 1), VM_SPINS);
     }
   } else {
     // ------------------------------------------------------------- worker warps
@@ -249,11 +279,11 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
     const size_t pstride = (size_t)4 * V.nbp;  // halves per plane wave
     const __half* xsrc = V.planes + (size_t)kX * V.npwx * pstride + V.xs + xb0;
     const int16_t* mp = V.map + (size_t)kl * V.nlf * V.nsum_max + xpw;
-    // Y copies: e = tid + VM_WORKERS v over 2 halves x 64 K rows x NYN / 8 chunks of y
+    // Y copies: e = tid + VM_WORKERS v over 2 halves x 64 K rows x NYN / 8 chunks
     constexpr int YCH = NYN / 8, YE = 128 * YCH, YV = (YE + VM_WORKERS - 1) / VM_WORKERS;
     // ysrc: plane * nbp + band (bits 0-15), plane wave of the chunk (bits 16-20),
-    // b(i) c block (bit 21), zero fill (bit 22), imaginary part (bit 23: negated
-    // in y'); -1: no copy
+    // column block (bits 21-22: c, b1 c, b2 c), zero fill (bit 23), imaginary
+    // part (bit 24: negated in y'); -1: no copy
     uint32_t ydst[YV], yidst[YV];  // the chunk in y, its image in y'
     int ysrc[YV];
 #pragma unroll
@@ -265,29 +295,34 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
         const int line = e / YCH, j = e - line * YCH;
         const int half = line >> 6, kk = line & 63, part = kk >> 5, pw = kk & 31;
         const int col = 8 * j, u = 2 * half + part;
-        const bool bblk = CURRENT && col >= NBY;
-        const int band = V.ys + (bblk ? col - NBY : col);
+        const int blk = col / NBY;
+        const int band = V.ys + col - blk * NBY;
         ydst[v] = 2 * XH + (uint32_t)(kk >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(col >> 6) * 1024u +
                   (uint32_t)(kk & 7) * 128u + ((uint32_t)(((col >> 3) & 7) ^ (kk & 7)) << 4);
-        const int ki = kk ^ 32, ci = NYN + col;  // y' row and column of the chunk
-        yidst[v] = 2 * XH + (uint32_t)(ki >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(ci >> 6) * 1024u +
-                   (uint32_t)(ki & 7) * 128u + ((uint32_t)(((ci >> 3) & 7) ^ (ki & 7)) << 4);
-        ysrc[v] = (band < V.nbp ? u * V.nbp + band : (1 << 22)) | (pw << 16) | (bblk ? (1 << 21) : 0) | (part << 23);
+        if constexpr (IMG) {
+          const int ki = kk ^ 32, ci = NYN + col;  // y' row and column of the chunk
+          yidst[v] = 2 * XH + (uint32_t)(ki >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(ci >> 6) * 1024u +
+                     (uint32_t)(ki & 7) * 128u + ((uint32_t)(((ci >> 3) & 7) ^ (ki & 7)) << 4);
+        }
+        ysrc[v] = (band < V.nbp ? u * V.nbp + band : (1 << 23)) | (pw << 16) | (blk << 21) | (part << 24);
       }
     }
     const __half* ysrc_c = V.planes + (size_t)kY * V.npwx * pstride;
-    const __half* ysrc_b = CURRENT ? V.ybt + (size_t)kl * V.nsum_max * pstride : nullptr;
+    const __half* ysrc_b1 = CURRENT ? V.ybt + (size_t)kl * V.nsum_max * pstride : nullptr;
+    const __half* ysrc_b2 = NB == 3 ? V.ybt2 + (size_t)kl * V.nsum_max * pstride : nullptr;
 
     // y' images of the chunks this thread copied into a stage
     constexpr uint32_t NEG = 0x80008000u;
     auto form = [&](int stage) {
-      const uint32_t st = sbase + (uint32_t)stage * STAGE;
+      if constexpr (IMG) {
+        const uint32_t st = sbase + (uint32_t)stage * STAGE;
 #pragma unroll
-      for (int v = 0; v < YV; ++v) {
-        if (ysrc[v] < 0) continue;
-        uint4 w = lds16(st + ydst[v]);
-        if (ysrc[v] & (1 << 23)) w = make_uint4(w.x ^ NEG, w.y ^ NEG, w.z ^ NEG, w.w ^ NEG);
-        sts16(st + yidst[v], w);
+        for (int v = 0; v < YV; ++v) {
+          if (ysrc[v] < 0) continue;
+          uint4 w = lds16(st + ydst[v]);
+          if (ysrc[v] & (1 << 24)) w = make_uint4(w.x ^ NEG, w.y ^ NEG, w.z ^ NEG, w.w ^ NEG);
+          sts16(st + yidst[v], w);
+        }
       }
     };
 
@@ -317,9 +352,10 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
         for (int v = 0; v < YV; ++v) {
           if (ysrc[v] < 0) continue;
           const int i = i0 + ((ysrc[v] >> 16) & 31);
-          const bool ok = !(ysrc[v] & (1 << 22)) && i < nsum;
+          const bool ok = !(ysrc[v] & (1 << 23)) && i < nsum;
           const int so = ysrc[v] & 0xffff;
-          const __half* b = (CURRENT && (ysrc[v] & (1 << 21))) ? ysrc_b : ysrc_c;
+          const int blk = (ysrc[v] >> 21) & 3;
+          const __half* b = blk == 0 ? ysrc_c : (blk == 1 ? ysrc_b1 : ysrc_b2);
           cp16z(st + ydst[v], ok ? b + (size_t)i * pstride + so : ysrc_c, ok ? 16u : 0u);
         }
       }
@@ -330,53 +366,63 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
     const int wq = warp & 3, cg = warp >> 2;
     const int row_t = wq * 32 + lane;
     const int eg = row_t / XB, ea = row_t - eg * XB;
-    float accR[CW], accI[CW];
+    float accR[NP][CW], accI[NP][CW];
 #pragma unroll
-    for (int j = 0; j < CW; ++j) accR[j] = accI[j] = 0.f;
-    float fa = 0.f;
+    for (int p = 0; p < NP; ++p)
+#pragma unroll
+      for (int j = 0; j < CW; ++j) accR[p][j] = accI[p][j] = 0.f;
+    float fa[NP];
     auto set_afac = [&](int gt) {
       const int G = gt * GPT + eg;
-      fa = 0.f;
-      if (CURRENT && eg < GPT && G < V.nlf) {
-        const double* kv = V.ktot + 3 * ik;
-        const double* gl = V.Glf + 3 * G;
-        const int mu = V.comp;
-        const double qmu = mu == 0 ? V.q0 : (mu == 1 ? V.q1 : V.q2);
-        fa = (float)(0.5 * V.Gcar * (qmu + 2.0 * kv[mu] + gl[mu])) * V.a_scale;
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        fa[p] = 0.f;
+        if (CURRENT && eg < GPT && G < V.nlf) {
+          const double* kv = V.ktot + 3 * ik;
+          const double* gl = V.Glf + 3 * G;
+          const int mu = p == 0 ? V.comp : V.comp2;
+          const double qmu = mu == 0 ? V.q0 : (mu == 1 ? V.q1 : V.q2);
+          fa[p] = (float)(0.5 * V.Gcar * (qmu + 2.0 * kv[mu] + gl[mu])) * V.a_scale;
+        }
       }
     };
     auto consume = [&](int t) -> bool {
-      constexpr int NB = Cfg::NBUF;
-      if (!tc::mbar_wait(&done[t % NB], (uint32_t)((t / NB) & 1), VM_SPINS)) {
+      constexpr int NBF = Cfg::NBUF;
+      if (!tc::mbar_wait(&done[t % NBF], (uint32_t)((t / NBF) & 1), VM_SPINS)) {
         atomicExch(V.status, 1);
         abort_flag = 1;
         return false;
       }
       tc::tc_fence_after();
-      const uint32_t ad = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)((t % NB) * Cfg::N2 + cg * CW);
-      float v[2][CW], w[2][CW];
+      const uint32_t ad = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)((t % NBF) * Cfg::N2 + cg * CW);
+      float vr[NB][CW], vi[NB][CW];  // Re D, Im D of each column block
 #pragma unroll
-      for (int part = 0; part < 2; ++part) {
-        tmem_ld_n<CW>(ad + part * NYN, v[part]);
-        if constexpr (CURRENT) tmem_ld_n<CW>(ad + part * NYN + NBY, w[part]);
+      for (int b = 0; b < NB; ++b) {
+        tmem_ld_n<CW>(ad + b * NBY, vr[b]);
+        tmem_ld_n<CW>(ad + NYN + b * NBY, vi[b]);
       }
       tc::tmem_ld_wait();
       tc::tc_fence_before();
       __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&tfree[t % NB]);
+      if (lane == 0) tc::mbar_arrive(&tfree[t % NBF]);
 #pragma unroll
       for (int j = 0; j < CW; ++j) {
         if constexpr (CURRENT) {
-          accR[j] += fa * v[0][j] + w[0][j];
-          accI[j] += fa * v[1][j] + w[1][j];
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            accR[p][j] += fa[p] * vr[0][j] + vr[p + 1][j];
+            accI[p][j] += fa[p] * vi[0][j] + vi[p + 1][j];
+          }
         } else {
-          accR[j] += v[0][j];
-          accI[j] += v[1][j];
+          accR[0][j] += vr[0][j];
+          accI[0][j] += vi[0][j];
         }
       }
       return true;
     };
-    float amx = 0.f;
+    float amx[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) amx[p] = 0.f;
     const float isign = V.swap ? -V.out_scale : V.out_scale;
     auto write_out = [&](int gt) {
       const int G = gt * GPT + eg;
@@ -385,14 +431,19 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
         for (int j = 0; j < CW; ++j) {
           const int r = ptab[ea * NBY + cg * CW + j];
           if (r >= 0) {
-            const float re = accR[j] * V.out_scale, im = accI[j] * isign;
-            V.M[(size_t)r * V.nlf + G] = make_float2(re, im);
-            amx = fmaxf(amx, fmaxf(fabsf(re), fabsf(im)));
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+              const float re = accR[p][j] * V.out_scale, im = accI[p][j] * isign;
+              (p == 0 ? V.M : V.M2)[(size_t)r * V.nlf + G] = make_float2(re, im);
+              amx[p] = fmaxf(amx[p], fmaxf(fabsf(re), fabsf(im)));
+            }
           }
         }
       }
 #pragma unroll
-      for (int j = 0; j < CW; ++j) accR[j] = accI[j] = 0.f;
+      for (int p = 0; p < NP; ++p)
+#pragma unroll
+        for (int j = 0; j < CW; ++j) accR[p][j] = accI[p][j] = 0.f;
     };
 
     // prologue: chunks 0 .. S-2 in flight.  The Gfast positions of a chunk are
@@ -453,8 +504,12 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
     }
     if (!fail && consume(total - 1)) write_out(ngt - 1);
     cp_wait<0>();
-    for (int o = 16; o > 0; o >>= 1) amx = fmaxf(amx, __shfl_xor_sync(0xffffffffu, amx, o));
-    if (lane == 0) atomicMax(V.amax, __float_as_uint(amx));
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      float a = amx[p];
+      for (int o = 16; o > 0; o >>= 1) a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+      if (lane == 0) atomicMax(V.amax + p, __float_as_uint(a));
+    }
   }
   tc::tc_fence_before();
   __syncthreads();
@@ -463,7 +518,8 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
 
 // b(i) c of every FBZ k-point of the launch, split like the coefficient planes:
 // ybt[k_local][i][plane][band], b(i) = Gcar (R1 G1_i)_mu sB / 2^14 (zero beyond
-// nsum), c the planes of K1; (h + l) b is split again into fp16 hi + lo.
+// nsum), c the planes of K1; (h + l) b is split again into fp16 hi + lo.  With
+// comp2 >= 0 the same for the second component into ybt2, from the same loads.
 struct YbtCtx {
   const int* kmap;
   const double* G;
@@ -472,13 +528,39 @@ struct YbtCtx {
   const int* npw;
   const __half* planes;
   __half* ybt;
-  int k0, nk, npwx, nbp, nsum_max, legacy, nsum_legacy, comp;
+  __half* ybt2;
+  int k0, nk, npwx, nbp, nsum_max, legacy, nsum_legacy, comp, comp2;
   double Gcar;
   float sB;
 };
 
+// (h + l) b for the eight bands of p[], split into fp16 hi + lo planes
+__device__ __forceinline__ void ybt_split(const uint4* p, float b, __half* out, int nbp) {
+  uint4 o[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    // bands 2q, 2q + 1 of the group: re = re_hi + re_lo, im = im_hi + im_lo
+    const float2 rh = __half22float2(reinterpret_cast<const __half2*>(&p[0])[q]);
+    const float2 ih = __half22float2(reinterpret_cast<const __half2*>(&p[1])[q]);
+    const float2 rl = __half22float2(reinterpret_cast<const __half2*>(&p[2])[q]);
+    const float2 il = __half22float2(reinterpret_cast<const __half2*>(&p[3])[q]);
+    const float2 re = make_float2((rh.x + rl.x) * b, (rh.y + rl.y) * b);
+    const float2 im = make_float2((ih.x + il.x) * b, (ih.y + il.y) * b);
+    const __half2 reh = __floats2half2_rn(re.x, re.y), imh = __floats2half2_rn(im.x, im.y);
+    const float2 rehf = __half22float2(reh), imhf = __half22float2(imh);
+    const __half2 rel = __floats2half2_rn(re.x - rehf.x, re.y - rehf.y);
+    const __half2 iml = __floats2half2_rn(im.x - imhf.x, im.y - imhf.y);
+    reinterpret_cast<__half2*>(&o[0])[q] = reh;
+    reinterpret_cast<__half2*>(&o[1])[q] = imh;
+    reinterpret_cast<__half2*>(&o[2])[q] = rel;
+    reinterpret_cast<__half2*>(&o[3])[q] = iml;
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) *reinterpret_cast<uint4*>(out + u * nbp) = o[u];
+}
+
 // One thread per (k-point, plane wave, 8-band group): 16-byte loads of the four
-// coefficient planes and 16-byte stores of the four b(i) c planes.
+// coefficient planes and 16-byte stores of the four b(i) c planes (per component).
 __global__ void k_vtx_ybt(YbtCtx Y) {
   const int ng = Y.nbp / 8;
   const size_t n = (size_t)Y.nk * Y.nsum_max * ng;
@@ -489,45 +571,29 @@ __global__ void k_vtx_ybt(YbtCtx Y) {
     const int* km = Y.kmap + 5 * (Y.k0 + kl);
     const int K1 = km[0];
     const int nsum = Y.legacy ? Y.nsum_legacy : Y.npw[K1];
-    float b = 0.f;
+    float b = 0.f, b2 = 0.f;
     if (i < nsum) {
-      const double* R = Y.Rcart + 9 * km[1] + 3 * Y.comp;
       const double* g1 = Y.G + 3 * Y.gidx[(size_t)K1 * Y.npwx + i];
+      const double* R = Y.Rcart + 9 * km[1] + 3 * Y.comp;
       b = (float)(Y.Gcar * (R[0] * g1[0] + R[1] * g1[1] + R[2] * g1[2])) * Y.sB * (1.0f / 16384.0f);
+      if (Y.comp2 >= 0) {
+        const double* R2 = Y.Rcart + 9 * km[1] + 3 * Y.comp2;
+        b2 = (float)(Y.Gcar * (R2[0] * g1[0] + R2[1] * g1[1] + R2[2] * g1[2])) * Y.sB * (1.0f / 16384.0f);
+      }
     }
     const __half* c = Y.planes + ((size_t)K1 * Y.npwx + (i < nsum ? i : 0)) * 4 * Y.nbp + 8 * g;
     uint4 p[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) p[u] = __ldg(reinterpret_cast<const uint4*>(c + u * Y.nbp));
-    uint4 o[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      // bands 2q, 2q + 1 of the group: re = re_hi + re_lo, im = im_hi + im_lo
-      const float2 rh = __half22float2(reinterpret_cast<const __half2*>(&p[0])[q]);
-      const float2 ih = __half22float2(reinterpret_cast<const __half2*>(&p[1])[q]);
-      const float2 rl = __half22float2(reinterpret_cast<const __half2*>(&p[2])[q]);
-      const float2 il = __half22float2(reinterpret_cast<const __half2*>(&p[3])[q]);
-      const float2 re = make_float2((rh.x + rl.x) * b, (rh.y + rl.y) * b);
-      const float2 im = make_float2((ih.x + il.x) * b, (ih.y + il.y) * b);
-      const __half2 reh = __floats2half2_rn(re.x, re.y), imh = __floats2half2_rn(im.x, im.y);
-      const float2 rehf = __half22float2(reh), imhf = __half22float2(imh);
-      const __half2 rel = __floats2half2_rn(re.x - rehf.x, re.y - rehf.y);
-      const __half2 iml = __floats2half2_rn(im.x - imhf.x, im.y - imhf.y);
-      reinterpret_cast<__half2*>(&o[0])[q] = reh;
-      reinterpret_cast<__half2*>(&o[1])[q] = imh;
-      reinterpret_cast<__half2*>(&o[2])[q] = rel;
-      reinterpret_cast<__half2*>(&o[3])[q] = iml;
-    }
-    __half* out = Y.ybt + r * 4 * Y.nbp + 8 * g;
-#pragma unroll
-    for (int u = 0; u < 4; ++u) *reinterpret_cast<uint4*>(out + u * Y.nbp) = o[u];
+    ybt_split(p, b, Y.ybt + r * 4 * Y.nbp + 8 * g, Y.nbp);
+    if (Y.comp2 >= 0) ybt_split(p, b2, Y.ybt2 + r * 4 * Y.nbp + 8 * g, Y.nbp);
   }
 }
 
-template <int NBY, bool CURRENT>
+template <int NBY, int NB>
 static int launch_vmn(rpa_ctx* c, const VtxMnCtx& V, int nk) {
-  using Cfg = VmCfg<NBY, CURRENT>;
-  auto kern = k_vertex_mn<NBY, CURRENT>;
+  using Cfg = VmCfg<NBY, NB>;
+  auto kern = k_vertex_mn<NBY, NB>;
   RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
   kern<<<nk, VM_THREADS, Cfg::SMEM, c->stream>>>(V);
   RPA_CUDA(c, cudaGetLastError());
@@ -535,23 +601,28 @@ static int launch_vmn(rpa_ctx* c, const VtxMnCtx& V, int nk) {
   return RPA_OK;
 }
 
-template <bool CURRENT>
-static int launch_vmn_nby(rpa_ctx* c, const VtxMnCtx& V, int nk, int nby) {
-  if (nby == 16) return launch_vmn<16, CURRENT>(c, V, nk);
-  if (nby == 32) return launch_vmn<32, CURRENT>(c, V, nk);
-  if constexpr (!CURRENT) {
-    if (nby == 48) return launch_vmn<48, false>(c, V, nk);
-    if (nby == 64) return launch_vmn<64, false>(c, V, nk);
+// nb: column blocks of Y (1 charge, 2 current, 3 current with two components)
+static int launch_vmn_nby(rpa_ctx* c, const VtxMnCtx& V, int nk, int nby, int nb) {
+  if (nb == 1) {
+    if (nby == 16) return launch_vmn<16, 1>(c, V, nk);
+    if (nby == 32) return launch_vmn<32, 1>(c, V, nk);
+    if (nby == 48) return launch_vmn<48, 1>(c, V, nk);
+    if (nby == 64) return launch_vmn<64, 1>(c, V, nk);
+  } else if (nb == 2) {
+    if (nby == 16) return launch_vmn<16, 2>(c, V, nk);
+    if (nby == 32) return launch_vmn<32, 2>(c, V, nk);
+  } else if (nb == 3) {
+    if (nby == 16) return launch_vmn<16, 3>(c, V, nk);
+    if (nby == 32) return launch_vmn<32, 3>(c, V, nk);
   }
-  return fail(c, RPA_EINVAL, "vertices: no kernel for a %d-band window", nby);
+  return fail(c, RPA_EINVAL, "vertices: no kernel for a %d-band window with %d column blocks", nby, nb);
 }
 
 // One launch per pair of band windows: gathered bands [x0, x1) in windows of
 // 32 starting on multiples of 8, sequential bands [y0, y1) in windows of at most
-// ymax (multiples of 16 wide, starting on a multiple of 8; the Y tile, y and y'
-// of every column block, spans at most 128 columns so that three stages fit).
-template <bool CURRENT>
-static int launch_windows_mn(rpa_ctx* c, VtxMnCtx V, int nk, int x0, int x1, int y0, int y1, int ymax) {
+// ymax (multiples of 16 wide, starting on a multiple of 8; the Y tile spans at
+// most 128 columns so that three stages fit).
+static int launch_windows_mn(rpa_ctx* c, VtxMnCtx V, int nk, int x0, int x1, int y0, int y1, int ymax, int nb) {
   const int ys0 = y0 & ~7, span = y1 - ys0;
   const int nyw = (span + ymax - 1) / ymax;
   const int W = ((span + nyw - 1) / nyw + 15) / 16 * 16;
@@ -566,7 +637,7 @@ static int launch_windows_mn(rpa_ctx* c, VtxMnCtx V, int nk, int x0, int x1, int
       V.yo0 = std::max(y0, V.ys);
       V.yo1 = std::min(y1, V.ys + W);
       if (V.yo1 <= V.yo0) continue;
-      RPA_TRY(launch_vmn_nby<CURRENT>(c, V, nk, W));
+      RPA_TRY(launch_vmn_nby(c, V, nk, W, nb));
     }
   }
   return RPA_OK;
@@ -576,10 +647,12 @@ static double pow2_floor_m(double x) { return std::ldexp(1.0, (int)std::floor(st
 
 // Mixed-path vertices of the FBZ k-points [k0, k0+nk) with MN-major operands.
 // Leaves *used false when the plane-wave count does not fit the int16 map
-// positions or the band count the int16 pair table (the caller then uses the
-// CUDA-core kernel).
+// positions or the band count the int16 pair table.  Current vertices of the
+// yz / zy pair go to Mf and Mf2 in one pass; with extra_pol (RPA_POL_XX / YY /
+// ZZ, not the call's own) a single-component polarisation also gets the
+// vertices of extra_pol into Mf2, from the same pass.
 int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans, const int* pos_of, float2* Mf,
-                float2* Mf2, unsigned* amax, bool* used) {
+                float2* Mf2, unsigned* amax, bool* used, int extra_pol) {
   *used = false;
   if (n_trans == 0) return RPA_OK;
   if (c->npwx > 32767 || c->nbnd > 181 || c->d_cpl.p == nullptr) return RPA_OK;
@@ -638,7 +711,9 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
   V.Glf = c->d_Glf.as<double>();
   V.npw = c->d_npw.as<int>();
   V.planes = c->d_cpl.as<__half>();
-  V.ybt = nullptr;
+  V.ybt = V.ybt2 = nullptr;
+  V.M2 = nullptr;
+  V.comp2 = 0;
   V.map = map;
   V.trans = c->d_trans.as<Trans>();
   V.offsets = c->d_offsets.as<long long>();
@@ -657,13 +732,14 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
   V.q2 = c->q[2];
   V.Gcar = P.Gcar;
   if (!current) {
-    V.comp = 0;
+    V.comp = V.comp2 = 0;
     V.a_scale = 0.0f;
     V.out_scale = (float)(1.0 / (16384.0 * 16384.0));
-    V.M = Mf;
+    V.M = V.M2 = Mf;
+    V.ybt2 = nullptr;
     V.amax = amax;
     *used = true;
-    return launch_windows_mn<false>(c, V, nk, x0, x1, y0, y1, ymax_chg);
+    return launch_windows_mn(c, V, nk, x0, x1, y0, y1, ymax_chg, 1);
   }
   // current vertices: |C| <= 1 (orthonormal bands), |b(i)| <= Gcar max|G|
   double gmax = 0.0;
@@ -683,8 +759,15 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
     case RPA_POL_YZ: comps[0] = 1; comps[1] = 2; break;
     default: comps[0] = 2; comps[1] = 1; break;
   }
-  RPA_TRY(ensure(c, c->d_ybt, sizeof(__half) * (size_t)nk * nsum_max * 4 * c->nbp));
+  bool pair = two;
+  if (!two && extra_pol >= 0) {
+    comps[1] = extra_pol == RPA_POL_XX ? 0 : (extra_pol == RPA_POL_YY ? 1 : 2);
+    pair = true;
+  }
+  const size_t ybt_n = (size_t)nk * nsum_max * 4 * c->nbp;
+  RPA_TRY(ensure(c, c->d_ybt, sizeof(__half) * ybt_n * (pair ? 2 : 1)));
   V.ybt = c->d_ybt.as<__half>();
+  V.ybt2 = pair ? V.ybt + ybt_n : nullptr;
   YbtCtx Y;
   Y.kmap = V.kmap;
   Y.G = c->d_G.as<double>();
@@ -702,16 +785,17 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
   Y.nsum_legacy = P.nsum_legacy;
   Y.Gcar = P.Gcar;
   Y.sB = sB;
-  // the yz / zy pair: one pass per Cartesian component
-  for (int a = 0; a < (two ? 2 : 1); ++a) {
-    V.comp = Y.comp = comps[a];
-    V.M = a == 0 ? Mf : Mf2;
-    V.amax = amax + a;
-    k_vtx_ybt<<<2 * 152 * 8, 256, 0, c->stream>>>(Y);
-    RPA_CUDA(c, cudaGetLastError());
-    ++c->launches;
-    RPA_TRY(launch_windows_mn<true>(c, V, nk, x0, x1, y0, y1, ymax_cur));
-  }
+  Y.ybt2 = const_cast<__half*>(V.ybt2);
+  V.comp = Y.comp = comps[0];
+  V.comp2 = comps[1];
+  Y.comp2 = pair ? comps[1] : -1;
+  V.M = Mf;
+  V.M2 = pair ? Mf2 : Mf;
+  V.amax = amax;
+  k_vtx_ybt<<<2 * 152 * 8, 256, 0, c->stream>>>(Y);
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  RPA_TRY(launch_windows_mn(c, V, nk, x0, x1, y0, y1, ymax_cur, pair ? 3 : 2));
   *used = true;
   return RPA_OK;
 }

@@ -32,7 +32,7 @@ int cmax_of(rpa_ctx* c, int n_inter, double* cmax);
 int vertices_f32(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, int maxpairs, long long n_trans, const int* pos_of,
                  float2* Mf, float2* Mf2, unsigned* amax);
 int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans, const int* pos_of, float2* Mf,
-                float2* Mf2, unsigned* amax, bool* used);
+                float2* Mf2, unsigned* amax, bool* used, int extra_pol);
 int qeff_fp64(rpa_ctx* c, const Chi0Plan& P, int n_inter, int n_trans);
 int kk_run(rpa_ctx* c, int variant, int no, double domega);
 int dyson_fp64(rpa_ctx* c, const double* V_host, bool want_epsinv, int* n_singular, int* n_zero,
@@ -408,7 +408,7 @@ int rpa_destroy(rpa_ctx* c) {
 const char* rpa_last_error(const rpa_ctx* c) { return c ? c->err.c_str() : g_create_err.c_str(); }
 
 int rpa_set_gvectors(rpa_ctx* c, int ng, const int* miller, const double* G, const double* KC) {
-  if (c) c->gmap_valid = c->ginv_valid = false;
+  if (c) c->gmap_valid = c->ginv_valid = c->vstash.valid = false;
   if (c && (c->parent || c->children > 0))
     return fail(c, RPA_ESTATE, "rpa_set_gvectors: the G list and basis are shared between contexts");
   if (!c || ng <= 0 || !miller || !G || !KC) return fail(c, RPA_EINVAL, "rpa_set_gvectors: bad arguments");
@@ -449,7 +449,7 @@ int rpa_set_gvectors(rpa_ctx* c, int ng, const int* miller, const double* G, con
 }
 
 int rpa_set_symmetry(rpa_ctx* c, int nsym, const double* R, const double* RI) {
-  if (c) c->gmap_valid = c->ginv_valid = false;
+  if (c) c->gmap_valid = c->ginv_valid = c->vstash.valid = false;
   if (c && (c->parent || c->children > 0))
     return fail(c, RPA_ESTATE, "rpa_set_symmetry: the G list and basis are shared between contexts");
   if (!c || nsym < 1 || nsym > 48 || !R || !RI) return fail(c, RPA_EINVAL, "rpa_set_symmetry: bad arguments");
@@ -465,7 +465,7 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
                    const double* E) {
   if (c && (c->parent || c->children > 0))
     return fail(c, RPA_ESTATE, "rpa_load_basis: the G list and basis are shared between contexts");
-  if (c) c->gmap_valid = c->ginv_valid = false;
+  if (c) c->gmap_valid = c->ginv_valid = c->vstash.valid = false;
   if (!c || nks <= 0 || nbnd <= 0 || npwx <= 0 || !npw || !coeff || !E)
     return fail(c, RPA_EINVAL, "rpa_load_basis: bad arguments");
   if (c->ng == 0) return fail(c, RPA_ESTATE, "rpa_load_basis: call rpa_set_gvectors first");
@@ -551,7 +551,7 @@ int rpa_load_basis(rpa_ctx* c, int nks, int nbnd, int npwx, const int* npw, cons
 
 int rpa_kmap(rpa_ctx* c, int ntot, const double* ktot, const int* K1, const int* R1, const int* K2, const int* R2,
              const int* iG0) {
-  if (c) c->gmap_valid = c->ginv_valid = false;
+  if (c) c->gmap_valid = c->ginv_valid = c->vstash.valid = false;
   if (!c || ntot <= 0 || !ktot || !K1 || !R1 || !K2 || !R2 || !iG0)
     return fail(c, RPA_EINVAL, "rpa_kmap: bad arguments");
   if (c->nks == 0) return fail(c, RPA_ESTATE, "rpa_kmap: call rpa_load_basis first");
@@ -578,7 +578,7 @@ int rpa_kmap(rpa_ctx* c, int ntot, const double* ktot, const int* K1, const int*
 }
 
 int rpa_set_q(rpa_ctx* c, const double* q, int nlf, const int* ilf, const int* parG) {
-  if (c) c->gmap_valid = c->ginv_valid = false;
+  if (c) c->gmap_valid = c->ginv_valid = c->vstash.valid = false;
   if (!c || !q || nlf <= 0 || !ilf) return fail(c, RPA_EINVAL, "rpa_set_q: bad arguments");
   if (nlf > 1000) return fail(c, RPA_EINVAL, "Nlf = %d exceeds the gjel limit NMAX = 1000", nlf);
   if (c->ng == 0) return fail(c, RPA_ESTATE, "rpa_set_q: call rpa_set_gvectors first");
@@ -608,6 +608,22 @@ int rpa_set_q(rpa_ctx* c, const double* q, int nlf, const int* ilf, const int* p
   RPA_CUDA(c, cudaMemcpy(c->d_Glf.p, gl.data(), sizeof(double) * gl.size(), cudaMemcpyHostToDevice));
   c->have_q = true;
   c->have_S = c->have_chi0 = c->have_W = false;
+  return RPA_OK;
+}
+
+// every argument but the polarisation equal (the transitions and their order
+// depend on these alone)
+static bool same_chi0_args(const rpa_chi0_args& x, const rpa_chi0_args& y) {
+  return x.mode == y.mode && x.ngd == y.ngd && x.nocc == y.nocc && x.no == y.no && x.ntot_norm == y.ntot_norm &&
+         x.domega == y.domega && x.eta == y.eta && x.lor_cut == y.lor_cut && x.df_cut == y.df_cut && x.T == y.T &&
+         x.Efermi == y.Efermi && x.Vcell == y.Vcell && x.Gcar == y.Gcar;
+}
+
+int rpa_chi0_prefetch(rpa_ctx* c, int pol) {
+  if (!c) return fail(c, RPA_EINVAL, "rpa_chi0_prefetch: bad arguments");
+  if (pol != -1 && pol != RPA_POL_XX && pol != RPA_POL_YY && pol != RPA_POL_ZZ)
+    return fail(c, RPA_EINVAL, "rpa_chi0_prefetch: pol must be RPA_POL_XX, YY, ZZ or -1");
+  c->prefetch_pol = pol;
   return RPA_OK;
 }
 
@@ -711,11 +727,20 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
   RPA_TRY(count_pairs(c, P, 0, c->ntot, counts, &maxp));
   // k chunks bounded by the vertex buffer budget
   const bool two = cplx && (a->pol == RPA_POL_YZ || a->pol == RPA_POL_ZY);
+  // vertices of this polarisation computed beside the previous call (rpa_chi0_prefetch)
+  const bool from_stash = c->vstash.valid && c->precision == RPA_PREC_MIXED && cplx && !two &&
+                          c->vstash.pol == a->pol && same_chi0_args(c->vstash.args, *a);
+  c->vstash.valid = false;
+  const int extra_pol = c->precision == RPA_PREC_MIXED && cplx && !two && c->vertex_kind != 1 &&
+                                c->prefetch_pol >= 0 && c->prefetch_pol != a->pol
+                            ? c->prefetch_pol
+                            : -1;
+  c->prefetch_pol = -1;
   // per-transition device memory: FP64 vertices (FP64 path) or FP32 vertex rows
   // plus pre-split tiles (mixed path), records, keys and sort buffers
   const size_t per_trans =
       (c->precision == RPA_PREC_MIXED
-           ? (size_t)c->nlf * sizeof(float2) * (two ? 2 : 1) + (cplx ? 4 : 2) * 96 * 128 / 32 *
+           ? (size_t)c->nlf * sizeof(float2) * (two || extra_pol >= 0 ? 2 : 1) + (cplx ? 4 : 2) * 96 * 128 / 32 *
                                                                     (size_t)((c->nlf + 95) / 96)
            : (size_t)c->nlf * sizeof(double2) * (two ? 2 : 1)) +
       2 * sizeof(Trans) + 24;
@@ -725,6 +750,7 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
   size_t max_trans = std::max<size_t>(budget / per_trans, (size_t)maxp + 1);
   max_trans = std::min<size_t>(max_trans, (size_t)1 << 30);
   int k0 = 0;
+  bool stashed = false;
   while (k0 < c->ntot) {
     long long tot = 0;
     int k1 = k0;
@@ -741,27 +767,37 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
     RPA_TRY(emit_pairs(c, P, k0, nk, off, tot, &wmax, &n_inter, &winsum));
     RPA_TRY(sort_trans(c, (int)tot, P.nw));
     if (c->precision == RPA_PREC_MIXED) {
-      // FP32 vertices written straight into the window-sorted rows
+      // FP32 vertices written straight into the window-sorted rows (the
+      // transitions and their sorted order are those of the previous call when
+      // its stashed rows are used: same arguments, k map, q and basis)
+      const bool whole = k0 == 0 && k1 == c->ntot;
+      const bool use_stash = from_stash && whole && tot == c->vstash.tot;
+      const int xpol = whole ? extra_pol : -1;
       const size_t mrows = ((size_t)tot + 31) / 32 * 32 + 32;
+      if (use_stash) std::swap(c->d_Mf, c->d_Mf2);
       RPA_TRY(ensure(c, c->d_Mf, sizeof(float2) * mrows * c->nlf));
-      if (two) RPA_TRY(ensure(c, c->d_Mf2, sizeof(float2) * mrows * c->nlf));
+      if (two || xpol >= 0) RPA_TRY(ensure(c, c->d_Mf2, sizeof(float2) * mrows * c->nlf));
       RPA_TRY(ensure(c, c->d_counts, sizeof(int) * ((size_t)tot + 1 > (size_t)c->ntot + 1 ? (size_t)tot + 1
                                                                                             : (size_t)c->ntot + 1)));
       float2* Mf = c->d_Mf.as<float2>();
       float2* Mf2 = two ? c->d_Mf2.as<float2>() : Mf;
+      float2* Mx = xpol >= 0 ? c->d_Mf2.as<float2>() : Mf2;  // second vertex set of the pass
       const size_t pad0 = (size_t)tot * c->nlf, pad1 = mrows * c->nlf;
       RPA_CUDA(c, cudaMemsetAsync(Mf + pad0, 0, sizeof(float2) * (pad1 - pad0), c->stream));
-      if (two) RPA_CUDA(c, cudaMemsetAsync(Mf2 + pad0, 0, sizeof(float2) * (pad1 - pad0), c->stream));
+      if (two || xpol >= 0) RPA_CUDA(c, cudaMemsetAsync(Mx + pad0, 0, sizeof(float2) * (pad1 - pad0), c->stream));
       int* pos_of = c->d_counts.as<int>();
       RPA_TRY(inverse_perm(c, (int)tot, pos_of));
       RPA_TRY(ensure(c, c->d_ntrans, 32));
       RPA_CUDA(c, cudaMemsetAsync(c->d_ntrans.p, 0, 32, c->stream));
       cudaEventRecord(c->ev[2], c->stream);
-      if (c->vertex_kind == 1) {
+      if (use_stash) {
+        // nothing to compute: the rows are in d_Mf
+      } else if (c->vertex_kind == 1) {
         RPA_TRY(vertices_f32(c, P, k0, nk, maxp, tot, pos_of, Mf, Mf2, c->d_ntrans.as<unsigned>()));
       } else {
         bool used_tc = false;
-        RPA_TRY(vertices_mn(c, P, k0, nk, tot, pos_of, Mf, Mf2, c->d_ntrans.as<unsigned>(), &used_tc));
+        RPA_TRY(vertices_mn(c, P, k0, nk, tot, pos_of, Mf, two ? Mf2 : Mx, c->d_ntrans.as<unsigned>(), &used_tc,
+                            xpol));
         if (!used_tc && tot > 0) return fail(c, RPA_ESTATE, "rpa_chi0: the tensor-core vertex kernel did not run");
       }
       cudaEventRecord(c->ev[3], c->stream);
@@ -772,6 +808,15 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
       float amM, amM2;
       std::memcpy(&amM, &am[0], 4);
       std::memcpy(&amM2, &am[1], 4);
+      if (use_stash) amM = c->vstash.amax;
+      if (xpol >= 0) {
+        c->vstash.pol = xpol;
+        c->vstash.args = *a;
+        c->vstash.args.pol = xpol;
+        c->vstash.tot = tot;
+        c->vstash.amax = amM2;
+        stashed = true;
+      }
       if (!two) amM2 = amM;
       RPA_TRY(accumulate_tc(c, P, n_inter, wmax, Mf, Mf2, amM, amM2, cmax));
       if (cplx) RPA_TRY(qeff_f32(c, n_inter, (int)tot, Mf, Mf2));
@@ -804,6 +849,7 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
     RPA_CUDA(c, cudaMemcpy(fl, c->d_flags.p, sizeof(int) * 4, cudaMemcpyDeviceToHost));
     if (fl[2]) return fail(c, RPA_ETIMEOUT, "rpa_chi0: a tensor-core completion wait timed out");
   }
+  c->vstash.valid = stashed;
   c->stage_ms[0] = t_pairs;
   c->stage_ms[1] = t_vert;
   c->stage_ms[2] = t_acc;

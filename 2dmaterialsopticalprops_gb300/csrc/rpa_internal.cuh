@@ -110,6 +110,17 @@ struct rpa_ctx {
   // cached inverse map (gathered K1 plane wave of each K2 plane wave), same validity
   bool ginv_valid = false;
   int ginv_k0 = 0, ginv_nk = 0, ginv_nsum = 0;
+  // rpa_chi0_prefetch: the polarisation whose vertices the next current-mode
+  // chi0 computes beside its own (-1 none), and those vertex rows, kept in d_Mf2
+  // for the chi0 call that directly follows with the same arguments
+  int prefetch_pol = -1;
+  struct VStash {
+    bool valid = false;
+    int pol = -1;
+    rpa_chi0_args args{};
+    long long tot = 0;
+    float amax = 0.f;
+  } vstash;
   // results
   int last_mode = -1, last_no = 0, last_nw = 0;
   double last_domega = 0.0, last_Gcar = 0.0;

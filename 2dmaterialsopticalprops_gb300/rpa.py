@@ -23,7 +23,7 @@ POL = {"xx": 0, "yy": 1, "zz": 2, "yz": 3, "zy": 4}
 KK_OPTABS_COMPLEX, KK_SLOSS_REAL = 1, 2
 
 EXPORTS = ["rpa_create", "rpa_destroy", "rpa_last_error", "rpa_set_gvectors", "rpa_set_symmetry",
-           "rpa_load_basis", "rpa_kmap", "rpa_set_q", "rpa_chi0", "rpa_kk", "rpa_dyson", "rpa_gfast",
+           "rpa_load_basis", "rpa_kmap", "rpa_set_q", "rpa_chi0", "rpa_chi0_prefetch", "rpa_kk", "rpa_dyson", "rpa_gfast",
            "rpa_init_igk", "rpa_kk_matrix", "rpa_stage_times", "rpa_chi0_stats", "rpa_accum_tile", "rpa_dyson_noalloc", "rpa_selftest", "rpa_launch_count", "rpa_get_stream", "rpa_synchronize",
            "rpa_basis_info", "rpa_create_shared", "rpa_server_create", "rpa_server_submit", "rpa_server_wait",
            "rpa_server_last_error", "rpa_server_destroy", "rpa_pi", "rpa_kk_w", "rpa_gen_fbz",
@@ -86,6 +86,7 @@ def load_library(path: str = LIB_PATH):
     L.rpa_kmap.argtypes = [vp, ip, vp, vp, vp, vp, vp, vp]
     L.rpa_set_q.argtypes = [vp, vp, ip, vp, vp]
     L.rpa_chi0.argtypes = [vp, C.POINTER(RpaChi0Args), vp, vp]
+    L.rpa_chi0_prefetch.argtypes = [vp, ip]
     L.rpa_kk.argtypes = [vp, ip, vp]
     L.rpa_dyson.argtypes = [vp, dp, dp, vp, vp, vp]
     L.rpa_gfast.argtypes = [vp, ip, ip, vp]
@@ -387,6 +388,12 @@ class Context:
         self.no = no
         self.mode = mode
         return S0, Q
+
+    def chi0_prefetch(self, pol: str | None):
+        """The next current-mode chi0 (xx, yy or zz) also computes the vertices
+        of `pol` and keeps them for a chi0 of `pol` that directly follows with
+        the same arguments (rpa_chi0_prefetch); None cancels."""
+        self._chk(self.L.rpa_chi0_prefetch(self.h, -1 if pol is None else POL[pol]))
 
     def kk(self, variant: int, want: bool = True, out: np.ndarray | None = None):
         """chi0 after the KK transform, (nlf, nlf, no-1) complex; `out` may be a

@@ -40,9 +40,10 @@ PKG = "2dmaterialsopticalprops_gb300"
 
 ACC_DRAM_BYTES_PER_PAIR = 30.4e9 / 54.6e6
 # DRAM bytes per FBZ k-point of the vertex launches (k_vertex_mn): ncu measured
-# 16.0 + 0.55 GB (current, xx) and 1.30 + 0.18 GB (charge) for the 1600
-# k-points of the 40x40 case
+# 16.0 + 0.55 GB (current, xx), 34.4 + 1.19 GB (current, xx and zz in one pass)
+# and 1.30 + 0.18 GB (charge) for the 1600 k-points of the 40x40 case
 VTX_DRAM_BYTES_PER_K_CURRENT = 16.56e9 / 1600
+VTX_DRAM_BYTES_PER_K_PAIR = 35.59e9 / 1600
 VTX_DRAM_BYTES_PER_K_CHARGE = 1.48e9 / 1600
 
 
@@ -142,6 +143,11 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
+# Optabs xx computes the zz vertices in the same pass (rpa_chi0_prefetch);
+# --no-prefetch runs the two polarisations' vertex passes separately
+PREFETCH = True
+
+
 def run_step(ctx, s, rpa, host=None):
     """One q-point: Optabs xx, Optabs zz, Sloss + Dyson.  host: None (outputs
     stay on the device), {} (new host arrays) or the dict alloc_outputs()
@@ -151,6 +157,8 @@ def run_step(ctx, s, rpa, host=None):
     bufs = host if host else None
     out = {}
     for pol in ("xx", "zz"):
+        if pol == "xx" and PREFETCH:
+            ctx.chi0_prefetch("zz")
         b = bufs[pol] if bufs else None
         S0, Q = ctx.chi0(rpa.MODE_CURRENT, want=want, out=b[:2] if b else None, **rpa.optabs_args(s, pol))
         chi = ctx.kk(rpa.KK_OPTABS_COMPLEX, want=want, out=b[2] if b else None)
@@ -196,11 +204,18 @@ def step_work(ctx, s, rpa):
     t = {"accumulate": 0.0, "vertices": 0.0, "pairs": 0.0, "kk": 0.0, "dyson": 0.0}
     n2 = float(s.nlf) ** 2
     for pol in ("xx", "zz"):
+        if pol == "xx" and PREFETCH:
+            ctx.chi0_prefetch("zz")
         ctx.chi0(rpa.MODE_CURRENT, want=False, **rpa.optabs_args(s, pol))
         st, tm = ctx.chi0_stats(), ctx.stage_times()
         tot_acc += 8.0 * n2 * st["sum_nwin"]
         tot_vert += 8.0 * st["vertex_macs"]
-        vbytes += vertex_bytes(st, 2 * s.nbnd)
+        if not PREFETCH:
+            vbytes += vertex_bytes(st, 2 * s.nbnd)
+        elif pol == "xx":
+            # one pass for both polarisations: the coefficients and the map read
+            # once, two sets of vertex rows written
+            vbytes += vertex_bytes(st, 2 * s.nbnd) + 8.0 * s.nlf * st["transitions"]
         for k in ("accumulate", "vertices", "pairs"):
             t[k] += tm[k]
         ctx.kk(rpa.KK_OPTABS_COMPLEX, want=False)
@@ -696,7 +711,11 @@ def main():
                     help="skip the 64-q loss-function dispersion (mixed path batched, FP64 GPU path on 8 q-points)")
     ap.add_argument("--dispersion", action="store_true",
                     help="run the dispersion on --config's basis too (it runs on grid120 by default)")
+    ap.add_argument("--no-prefetch", action="store_true",
+                    help="separate vertex passes for Optabs xx and zz (default: one pass, rpa_chi0_prefetch)")
     args = ap.parse_args()
+    global PREFETCH
+    PREFETCH = not args.no_prefetch
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -872,8 +891,9 @@ def main():
     roof_vtx = {"bound": "hbm", "achieved": vtx_gbs, "peak": hbm, "unit": "GB/s",
                 "frac": (vtx_gbs / hbm) if vtx_gbs else None, "peak_source": hbm_src,
                 "bytes_per_step": work["vertex_bytes"],
-                "byte_count": "sum over vertex passes of 8*Nb*sum_k NGd + 2*NG*sum_k NGd + 8*NG*T "
-                              "(Nb: bands read on both k-points; int16 Gfast map; FP32 rows out)",
+                "byte_count": "sum over vertex passes of 8*Nb*sum_k NGd + 2*NG*sum_k NGd + 8*NG*T per row set "
+                              "(Nb: bands read on both k-points; int16 Gfast map; FP32 rows out; the xx + zz "
+                              "pass writes two row sets)",
                 "vertex_tflops": (work["vertex_flops"] / vtx_s / 1e12) if vtx_s > 0 else None}
     if args.precision == "fp64":
         roof_vtx.update({"kernel": "k_vertex_fp64", "traffic": None})
@@ -883,11 +903,19 @@ def main():
                     "kernel": "k_accum_fp64 (+ per-chunk calls)",
                     "flops_per_step": work["acc_flops"], "flop_count": "8*NGloc^2*sum_t N_win(t)"}
     else:
-        roof_vtx.update({"kernel": "k_vertex_mn (Optabs xx, zz: current; Sloss: charge), 3 launches per step",
-                         "traffic": (2 * VTX_DRAM_BYTES_PER_K_CURRENT + VTX_DRAM_BYTES_PER_K_CHARGE) * s.ntot,
-                         "traffic_basis": "DRAM bytes of the step's three vertex launches (xx, zz current; charge), "
-                                          "per k-point from an ncu capture of the 40x40 case, times this "
-                                          "workload's FBZ k-points (the passes bytes_per_step counts)"})
+        if PREFETCH:
+            roof_vtx.update({"kernel": "k_vertex_mn (Optabs xx and zz: one current pass; Sloss: charge), "
+                                       "2 launches per step",
+                             "traffic": (VTX_DRAM_BYTES_PER_K_PAIR + VTX_DRAM_BYTES_PER_K_CHARGE) * s.ntot,
+                             "traffic_basis": "DRAM bytes of the step's two vertex launches (xx + zz current; "
+                                              "charge), per k-point from an ncu capture of the 40x40 case, times "
+                                              "this workload's FBZ k-points (the passes bytes_per_step counts)"})
+        else:
+            roof_vtx.update({"kernel": "k_vertex_mn (Optabs xx, zz: current; Sloss: charge), 3 launches per step",
+                             "traffic": (2 * VTX_DRAM_BYTES_PER_K_CURRENT + VTX_DRAM_BYTES_PER_K_CHARGE) * s.ntot,
+                             "traffic_basis": "DRAM bytes of the step's three vertex launches (xx, zz current; "
+                                              "charge), per k-point from an ncu capture of the 40x40 case, times "
+                                              "this workload's FBZ k-points (the passes bytes_per_step counts)"})
         pk = peaks.get("bf16_tflops_sustained", 1700.0)
         # DRAM bytes of one complex (Optabs) accumulation launch: ncu measured
         # 30.4 GB for 54.6 M (transition, frequency) pairs on the 60x60 case,
@@ -934,7 +962,9 @@ def main():
         cfgd = workload_desc(s, args.config)
         cfgd.update({"l2": "inputs larger than L2 (basis %.1f GB resident)" % (s.coeff.nbytes / 1e9),
                      "parallelism": f"q-sharded x{world}" if world > 1 else "single GPU",
-                     "precision_path": args.precision, "setup_s": round(t_gen, 1)})
+                     "precision_path": args.precision, "setup_s": round(t_gen, 1),
+                     "vertex_passes": ("Optabs xx and zz share one vertex pass (rpa_chi0_prefetch)" if PREFETCH
+                                       else "one vertex pass per polarisation")})
         line = {"metric": "q-point chi/W spectra/sec", "value": value, "unit": "q-spectra/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f16x3->f32 (vertices, S0), f32 (KK), f64 (Dyson)",

@@ -220,6 +220,21 @@ int rpa_set_q(rpa_ctx* ctx, const double* q, int nlf, const int* ilf, const int*
  * case the result only stays on the device for rpa_kk. */
 int rpa_chi0(rpa_ctx* ctx, const rpa_chi0_args* args, double* S0_out, double* Qeff_out);
 
+/* No counterpart in the reference (each Optabs run computes one polarisation,
+ * Optabs.f90:291-471).  RPA_PREC_MIXED, current mode: the next rpa_chi0 on ctx
+ * for a single-component polarisation (xx, yy, zz) also computes the vertices
+ * of pol (another of RPA_POL_XX, YY, ZZ) in the same vertex pass -- the two
+ * share the gathered coefficients and the c . c block -- and keeps them on the
+ * device.  An rpa_chi0 for pol that directly follows that call on ctx with the
+ * same arguments (rpa_kk and rpa_dyson in between are fine; rpa_set_q,
+ * rpa_kmap, rpa_load_basis, rpa_set_gvectors, rpa_set_symmetry or another
+ * rpa_chi0 drop them) uses them instead of computing its vertices.  Without
+ * effect on the FP64 path, charge mode, the yz / zy pair, the CUDA-core vertex
+ * kernel and transitions that need more than one k chunk.  One-shot: applies
+ * to the next rpa_chi0 only; pol = -1 cancels.  Results equal those of the
+ * two calls without it up to FP32 rounding order. */
+int rpa_chi0_prefetch(rpa_ctx* ctx, int pol);
+
 /* Replaces: genReChi0/genImChi0 (Optabs.f90:1112-1318, variant
  * RPA_KK_OPTABS_COMPLEX) or genChi0 (Sloss.f90:954-1059, RPA_KK_SLOSS_REAL)
  * for io = 1..no-1 over the S0 left on the device by rpa_chi0.

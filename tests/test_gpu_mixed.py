@@ -235,3 +235,42 @@ def test_mixed_point_group_system(synth, rpa, orc):
         Sco, _ = orc.optabs_s0(orc.Bound(s, pol=pol))
         assert rel(Sc, Sco) < TOL, pol
     ctx.close()
+
+
+@pytest.mark.parametrize("first,second,ymax", [("xx", "zz", 32), ("zz", "yy", 16)])
+def test_prefetched_polarisation(synth, rpa, orc, first, second, ymax):
+    """rpa_chi0_prefetch: the first chi0 computes the second polarisation's
+    vertices in the same pass (three column blocks c | b1 c | b2 c); the second
+    chi0 uses them.  Both S0 / Qeff against the oracle (Optabs.f90:291-471) at
+    the mixed-path tolerance and against the same calls without the prefetch
+    (equal up to FP32 rounding order); rpa_kk in between keeps the stash,
+    rpa_set_q drops it."""
+    import json
+    s = synth.build(synth.config_small(nbnd=24, npw=150, nlf=40, lf="xyz", no=31))
+    ctx = rpa.Context(precision=rpa.PREC_MIXED)
+    ctx.load_system(s)
+    ctx.tune_import(json.dumps({"vertex": [{"mode": rpa.MODE_CURRENT, "nbnd": 24, "nocc": 0, "nlf32": s.nlf // 32,
+                                            "ymax": ymax, "swap": -1}]}))
+    ref = {}
+    for pol in (first, second):
+        ref[pol] = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, pol))
+    ctx.chi0_prefetch(second)
+    S1, Q1 = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, first))
+    ctx.kk(rpa.KK_OPTABS_COMPLEX, want=False)
+    S2, Q2 = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, second))
+    assert ctx.stage_times()["vertices"] < 0.05  # the stashed rows were used
+    for pol, (S, Q) in ((first, (S1, Q1)), (second, (S2, Q2))):
+        So, Qo = orc.optabs_s0(orc.Bound(s, pol=pol))
+        assert rel(S, So) < TOL and rel(Q, Qo) < TOL, pol
+        assert rel(S, ref[pol][0]) < 1e-6 and rel(Q, ref[pol][1]) < 1e-6, pol
+    # a set_q between the two calls drops the stash: the second call recomputes
+    ctx.chi0_prefetch(second)
+    ctx.chi0(rpa.MODE_CURRENT, want=False, **rpa.optabs_args(s, first))
+    ctx.set_q(s.q, s.ilf, s.parG)
+    S3, _ = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, second))
+    assert ctx.stage_times()["vertices"] > 0
+    assert rel(S3, ref[second][0]) < 1e-6
+    with pytest.raises(rpa.RpaError) as e:
+        ctx.chi0_prefetch("yz")
+    assert e.value.code == rpa.RPA_EINVAL
+    ctx.close()

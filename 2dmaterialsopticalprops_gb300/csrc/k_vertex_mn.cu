@@ -281,15 +281,22 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
     const int16_t* mp = V.map + (size_t)kl * V.nlf * V.nsum_max + xpw;
     // Y copies: e = tid + VM_WORKERS v over 2 halves x 64 K rows x NYN / 8 chunks
     constexpr int YCH = NYN / 8, YE = 128 * YCH, YV = (YE + VM_WORKERS - 1) / VM_WORKERS;
-    // ysrc: plane * nbp + band (bits 0-15), plane wave of the chunk (bits 16-20),
-    // column block (bits 21-22: c, b1 c, b2 c), zero fill (bit 23), imaginary
-    // part (bit 24: negated in y'); -1: no copy
+    const __half* ysrc_c = V.planes + (size_t)kY * V.npwx * pstride;
+    const __half* ysrc_b1 = CURRENT ? V.ybt + (size_t)kl * V.nsum_max * pstride : nullptr;
+    const __half* ysrc_b2 = NB == 3 ? V.ybt2 + (size_t)kl * V.nsum_max * pstride : nullptr;
+    // per copy: its place in y (and y'), its source for chunk 0 (a chunk adds
+    // its plane-wave offset), the chunk start from which it is a zero fill
+    // (beyond nsum, or a band beyond the window), the imaginary-part flag
     uint32_t ydst[YV], yidst[YV];  // the chunk in y, its image in y'
-    int ysrc[YV];
+    const __half* ysb[YV];
+    int ylim[YV];
+    bool ycp[YV], yneg[YV];
 #pragma unroll
     for (int v = 0; v < YV; ++v) {
       const int e = tid + VM_WORKERS * v;
-      ysrc[v] = -1;
+      ycp[v] = yneg[v] = false;
+      ysb[v] = ysrc_c;
+      ylim[v] = 0;
       ydst[v] = yidst[v] = 0;
       if (e < YE) {
         const int line = e / YCH, j = e - line * YCH;
@@ -304,12 +311,13 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
           yidst[v] = 2 * XH + (uint32_t)(ki >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(ci >> 6) * 1024u +
                      (uint32_t)(ki & 7) * 128u + ((uint32_t)(((ci >> 3) & 7) ^ (ki & 7)) << 4);
         }
-        ysrc[v] = (band < V.nbp ? u * V.nbp + band : (1 << 23)) | (pw << 16) | (blk << 21) | (part << 24);
+        const __half* bp = blk == 0 ? ysrc_c : (blk == 1 ? ysrc_b1 : ysrc_b2);
+        ycp[v] = true;
+        yneg[v] = part != 0;
+        ysb[v] = bp + (size_t)pw * pstride + (band < V.nbp ? u * V.nbp + band : 0);
+        ylim[v] = band < V.nbp ? nsum - pw : 0;
       }
     }
-    const __half* ysrc_c = V.planes + (size_t)kY * V.npwx * pstride;
-    const __half* ysrc_b1 = CURRENT ? V.ybt + (size_t)kl * V.nsum_max * pstride : nullptr;
-    const __half* ysrc_b2 = NB == 3 ? V.ybt2 + (size_t)kl * V.nsum_max * pstride : nullptr;
 
     // y' images of the chunks this thread copied into a stage
     constexpr uint32_t NEG = 0x80008000u;
@@ -318,9 +326,9 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
         const uint32_t st = sbase + (uint32_t)stage * STAGE;
 #pragma unroll
         for (int v = 0; v < YV; ++v) {
-          if (ysrc[v] < 0) continue;
+          if (!ycp[v]) continue;
           uint4 w = lds16(st + ydst[v]);
-          if (ysrc[v] & (1 << 24)) w = make_uint4(w.x ^ NEG, w.y ^ NEG, w.z ^ NEG, w.w ^ NEG);
+          if (yneg[v]) w = make_uint4(w.x ^ NEG, w.y ^ NEG, w.z ^ NEG, w.w ^ NEG);
           sts16(st + yidst[v], w);
         }
       }
@@ -348,15 +356,12 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
         for (int u4 = 0; u4 < 4; ++u4)
           cp16z(st + xoff + (uint32_t)(u4 >> 1) * XH + (uint32_t)(u4 & 1) * 8192u, src + u4 * V.nbp, sz);
         const int i0 = chunk_of(u) * VM_I;
+        const size_t off = (size_t)i0 * pstride;
 #pragma unroll
         for (int v = 0; v < YV; ++v) {
-          if (ysrc[v] < 0) continue;
-          const int i = i0 + ((ysrc[v] >> 16) & 31);
-          const bool ok = !(ysrc[v] & (1 << 23)) && i < nsum;
-          const int so = ysrc[v] & 0xffff;
-          const int blk = (ysrc[v] >> 21) & 3;
-          const __half* b = blk == 0 ? ysrc_c : (blk == 1 ? ysrc_b1 : ysrc_b2);
-          cp16z(st + ydst[v], ok ? b + (size_t)i * pstride + so : ysrc_c, ok ? 16u : 0u);
+          if (!ycp[v]) continue;
+          const bool ok = i0 < ylim[v];
+          cp16z(st + ydst[v], ok ? ysb[v] + off : ysrc_c, ok ? 16u : 0u);
         }
       }
       cp_commit();
@@ -366,11 +371,13 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
     const int wq = warp & 3, cg = warp >> 2;
     const int row_t = wq * 32 + lane;
     const int eg = row_t / XB, ea = row_t - eg * XB;
-    float accR[NP][CW], accI[NP][CW];
+    // FP32 sums over the chunks, pairs of columns (packed f32x2 arithmetic)
+    constexpr int CH = CW / 2;
+    float2 accR[NP][CH], accI[NP][CH];
 #pragma unroll
     for (int p = 0; p < NP; ++p)
 #pragma unroll
-      for (int j = 0; j < CW; ++j) accR[p][j] = accI[p][j] = 0.f;
+      for (int j = 0; j < CH; ++j) accR[p][j] = accI[p][j] = make_float2(0.f, 0.f);
     float fa[NP];
     auto set_afac = [&](int gt) {
       const int G = gt * GPT + eg;
@@ -406,16 +413,21 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&tfree[t % NBF]);
 #pragma unroll
-      for (int j = 0; j < CW; ++j) {
+      for (int j = 0; j < CH; ++j) {
+        const float2 r0 = make_float2(vr[0][2 * j], vr[0][2 * j + 1]);
+        const float2 i0 = make_float2(vi[0][2 * j], vi[0][2 * j + 1]);
         if constexpr (CURRENT) {
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
-            accR[p][j] += fa[p] * vr[0][j] + vr[p + 1][j];
-            accI[p][j] += fa[p] * vi[0][j] + vi[p + 1][j];
+            const float2 f2 = make_float2(fa[p], fa[p]);
+            const float2 rp = make_float2(vr[p + 1][2 * j], vr[p + 1][2 * j + 1]);
+            const float2 ip = make_float2(vi[p + 1][2 * j], vi[p + 1][2 * j + 1]);
+            accR[p][j] = __fadd2_rn(accR[p][j], __ffma2_rn(f2, r0, rp));
+            accI[p][j] = __fadd2_rn(accI[p][j], __ffma2_rn(f2, i0, ip));
           }
         } else {
-          accR[0][j] += vr[0][j];
-          accI[0][j] += vi[0][j];
+          accR[0][j] = __fadd2_rn(accR[0][j], r0);
+          accI[0][j] = __fadd2_rn(accI[0][j], i0);
         }
       }
       return true;
@@ -433,7 +445,9 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
           if (r >= 0) {
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
-              const float re = accR[p][j] * V.out_scale, im = accI[p][j] * isign;
+              const float ar = (j & 1) ? accR[p][j >> 1].y : accR[p][j >> 1].x;
+              const float ai = (j & 1) ? accI[p][j >> 1].y : accI[p][j >> 1].x;
+              const float re = ar * V.out_scale, im = ai * isign;
               (p == 0 ? V.M : V.M2)[(size_t)r * V.nlf + G] = make_float2(re, im);
               amx[p] = fmaxf(amx[p], fmaxf(fabsf(re), fabsf(im)));
             }
@@ -443,7 +457,7 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
 #pragma unroll
       for (int p = 0; p < NP; ++p)
 #pragma unroll
-        for (int j = 0; j < CW; ++j) accR[p][j] = accI[p][j] = 0.f;
+        for (int j = 0; j < CH; ++j) accR[p][j] = accI[p][j] = make_float2(0.f, 0.f);
     };
 
     // prologue: chunks 0 .. S-2 in flight.  The Gfast positions of a chunk are

@@ -74,6 +74,7 @@ struct VtxMnCtx {
   const int* pos_of;
   float2* M;
   float2* M2;             // vertex rows of the second component (three column blocks)
+  int* ptab_g;            // [k_local][32][NBY]: pair table of the three-block pass (global memory)
   unsigned* amax;         // [2]: max |M|, max |M2| (float bits)
   int* status;
   int k0, nlf, npwx, nbp, nsum_max, legacy, nsum_legacy;
@@ -98,14 +99,20 @@ constexpr int VM_SMAX = 6;
 template <int NBY, int NB>
 struct VmCfg {
   static constexpr bool IMG = NB <= 2;                   // y' images in the Y tile
+  // three blocks: the Y tile in the 64-byte swizzle (32-wide atoms, no padding
+  // to 64 columns) and the pair table in global memory, so that four stages fit
+  static constexpr bool SW64 = !IMG;
   static constexpr int NYN = NB * NBY;                   // columns of Re D (and of Im D)
   static constexpr int NYT = IMG ? 2 * NYN : NYN;        // columns of the Y tile
-  static constexpr int NTA = (NYT + 63) / 64;            // 64-wide atoms along N of one half (lo or hi) of Y
+  static constexpr int AW = SW64 ? 32 : 64;              // atom width along N (elements)
+  static constexpr uint32_t AB = SW64 ? 512 : 1024;      // bytes of one atom (8 K rows)
+  static constexpr int NTA = (NYT + AW - 1) / AW;        // atoms along N of one half (lo or hi) of Y
   static constexpr uint32_t XH = 64 * 128 * 2;           // one half (hi or lo) of X
-  static constexpr uint32_t YKG = (uint32_t)NTA * 2048;  // Y bytes per group of 8 K rows: hi atoms, then lo atoms
-  static constexpr uint32_t YLO = (uint32_t)NTA * 1024;  // offset of the lo atoms in a K group
+  static constexpr uint32_t YKG = 2u * NTA * AB;         // Y bytes per group of 8 K rows: hi atoms, then lo atoms
+  static constexpr uint32_t YLO = (uint32_t)NTA * AB;    // offset of the lo atoms in a K group
   static constexpr uint32_t STAGE = 2 * XH + 8 * YKG;
-  static constexpr uint32_t PTAB = 32 * NBY * 4;         // int32 [32][NBY]
+  static constexpr bool PTAB_SMEM = IMG;
+  static constexpr uint32_t PTAB = PTAB_SMEM ? 32 * NBY * 4 : 0;  // int32 [32][NBY]
   static constexpr int S0 = (int)((VM_SMEM_MAX - 1024 - (int)PTAB) / (int)STAGE);
   static constexpr int S = S0 > VM_SMAX ? VM_SMAX : S0;
   // accumulator columns: Re D then Im D (with images: one MMA of N = 64 NTA over both)
@@ -114,9 +121,13 @@ struct VmCfg {
   static constexpr uint32_t NCOL = NBUF * N2 <= 256 ? 256 : 512;
   static constexpr int CW = NBY / 4;                     // columns per thread per block
   static constexpr size_t SMEM = (size_t)S * STAGE + PTAB + 1024;
-  static_assert(NBY % 16 == 0 && NTA <= 2 && NYN <= 256, "window too wide");
+  static_assert(NBY % 16 == 0 && (SW64 || NTA <= 2) && NYN <= 256, "window too wide");
   static_assert(NBUF * N2 <= 512, "accumulator ring beyond TMEM");
   static_assert(S >= 3, "shared-memory ring too shallow");
+  // four stages or more: a step signals the chunk issued S - 2 steps before
+  // it waits for the read-back of the chunk before last (see the worker loop)
+  static constexpr bool EARLY = S >= 4;
+  static_assert(IMG || EARLY, "three blocks need four stages");
 };
 
 __device__ __forceinline__ void cp16z(uint32_t dst, const void* src, uint32_t src_bytes) {
@@ -172,7 +183,9 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
   extern __shared__ unsigned char smraw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
   const uint32_t sbase = tc::smem_u32(base);
-  int* ptab = reinterpret_cast<int*>(base + (size_t)S * STAGE);  // [a][b]: vertex row of the pair, -1 none
+  // [a][b]: vertex row of the pair, -1 none
+  int* ptab = Cfg::PTAB_SMEM ? reinterpret_cast<int*>(base + (size_t)S * STAGE)
+                             : V.ptab_g + (size_t)blockIdx.x * 32 * NBY;
   __shared__ uint64_t full[VM_SMAX], done[Cfg::NBUF], tfree[Cfg::NBUF];
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
@@ -229,7 +242,8 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
       const uint32_t idn = tc::idesc_f16_mn(128, IMG ? N2 : (uint32_t)NYN, true);
       // descriptors of stage 0; a chunk adds its byte offsets / 16 to the start-address field
       const uint64_t dx0 = tc::desc_sw128_mn(sbase, 1024u, 2048u);
-      const uint64_t dy0 = tc::desc_sw128_mn(sbase + 2 * XH, 1024u, YKG);
+      const uint64_t dy0 = Cfg::SW64 ? tc::desc_sw64_mn(sbase + 2 * XH, Cfg::AB, YKG)
+                                     : tc::desc_sw128_mn(sbase + 2 * XH, 1024u, YKG);
       int last = -1;
       int s = 0, ph = 0;
       for (int t = 0; t < total; ++t) {
@@ -304,8 +318,12 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
         const int col = 8 * j, u = 2 * half + part;
         const int blk = col / NBY;
         const int band = V.ys + col - blk * NBY;
-        ydst[v] = 2 * XH + (uint32_t)(kk >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(col >> 6) * 1024u +
-                  (uint32_t)(kk & 7) * 128u + ((uint32_t)(((col >> 3) & 7) ^ (kk & 7)) << 4);
+        if constexpr (Cfg::SW64)
+          ydst[v] = 2 * XH + (uint32_t)(kk >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(col >> 5) * 512u +
+                    (uint32_t)(kk & 7) * 64u + ((uint32_t)(((col >> 3) & 3) ^ ((kk & 7) >> 1)) << 4);
+        else
+          ydst[v] = 2 * XH + (uint32_t)(kk >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(col >> 6) * 1024u +
+                    (uint32_t)(kk & 7) * 128u + ((uint32_t)(((col >> 3) & 7) ^ (kk & 7)) << 4);
         if constexpr (IMG) {
           const int ki = kk ^ 32, ci = NYN + col;  // y' row and column of the chunk
           yidst[v] = 2 * XH + (uint32_t)(ki >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(ci >> 6) * 1024u +
@@ -487,23 +505,42 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
     int si = S - 1;    // stage of the next chunk to issue
     int sf = 1 % S;    // stage of chunk j + 1
     bool fail = false;
-    auto body = [&](int j, int& R) -> bool {
-      if (j >= 1) {
-        if (!consume(j - 1)) return false;
-        if (uc.c == nchunk - 1) {
-          write_out(uc.gt);
-          set_afac(uc.gt + 1);
-        }
-        advance(uc);
+    auto read_back = [&](int j) -> bool {
+      if (!consume(j)) return false;
+      if (uc.c == nchunk - 1) {
+        write_out(uc.gt);
+        set_afac(uc.gt + 1);
       }
-      issue_with(si, R);
-      si = si + 1 == S ? 0 : si + 1;
-      cp_wait<S - 2>();
+      advance(uc);
+      return true;
+    };
+    auto signal = [&](int j) {
       if (j + 1 < total) form(sf);
       tc::fence_async_smem();
       __syncwarp();
       if (lane == 0 && j + 1 < total) tc::mbar_arrive(&full[sf]);
       sf = sf + 1 == S ? 0 : sf + 1;
+    };
+    // Step j: chunk j + 1 to the MMA warp, chunk j - 1 read back, chunk
+    // j + S - 1 issued into the stage of chunk j - 1.
+    auto body = [&](int j, int& R) -> bool {
+      if constexpr (Cfg::EARLY) {
+        // chunk j + 1 (issued S - 2 steps ago) is signalled before this step
+        // waits for the MMAs of chunk j - 1, so the MMA warp learns that its
+        // operands are in without waiting for that read-back round trip
+        cp_wait<S - 3>();
+        signal(j);
+        if (j >= 1 && !read_back(j - 1)) return false;
+        issue_with(si, R);
+        si = si + 1 == S ? 0 : si + 1;
+      } else {
+        // three stages: chunk j + 1 was issued one step ago
+        if (j >= 1 && !read_back(j - 1)) return false;
+        issue_with(si, R);
+        si = si + 1 == S ? 0 : si + 1;
+        cp_wait<S - 2>();
+        signal(j);
+      }
       return !abort_flag;
     };
     // chunk j + S - 1 is issued at step j: its positions are in pA for even
@@ -727,6 +764,7 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
   V.planes = c->d_cpl.as<__half>();
   V.ybt = V.ybt2 = nullptr;
   V.M2 = nullptr;
+  V.ptab_g = nullptr;
   V.comp2 = 0;
   V.map = map;
   V.trans = c->d_trans.as<Trans>();
@@ -777,6 +815,10 @@ int vertices_mn(rpa_ctx* c, const Chi0Plan& P, int k0, int nk, long long n_trans
   if (!two && extra_pol >= 0) {
     comps[1] = extra_pol == RPA_POL_XX ? 0 : (extra_pol == RPA_POL_YY ? 1 : 2);
     pair = true;
+  }
+  if (pair) {
+    RPA_TRY(ensure(c, c->d_ptab, sizeof(int) * (size_t)nk * 32 * 32));
+    V.ptab_g = c->d_ptab.as<int>();
   }
   const size_t ybt_n = (size_t)nk * nsum_max * 4 * c->nbp;
   RPA_TRY(ensure(c, c->d_ybt, sizeof(__half) * ybt_n * (pair ? 2 : 1)));

@@ -175,6 +175,19 @@ __device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t smem_addr, uint32_t l
   return d;
 }
 
+// The same in the 64-byte swizzle layout (layout type 4): atoms of 8 K rows x
+// 64 bytes (32 elements along M or N), the 16-byte chunk c of K row k at
+// chunk position c ^ ((k % 8) / 2); atoms 512-byte aligned.
+__device__ __forceinline__ uint64_t desc_sw64_mn(uint32_t smem_addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((smem_addr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)4 << 61;
+  return d;
+}
+
 // Instruction descriptor, kind::f16: D f32, A and B f16, both MN-major; negb
 // negates B.
 __host__ __device__ constexpr uint32_t idesc_f16_mn(int M, int N, bool negb) {

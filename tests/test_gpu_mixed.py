@@ -274,3 +274,28 @@ def test_prefetched_polarisation(synth, rpa, orc, first, second, ymax):
         ctx.chi0_prefetch("yz")
     assert e.value.code == rpa.RPA_EINVAL
     ctx.close()
+
+
+def test_prefetch_dropped_by_another_call(synth, rpa, orc):
+    """The stash of a prefetched polarisation is dropped by any chi0 in
+    between (a charge-mode call here): the later zz call computes its own
+    vertices and still matches the oracle; a prefetch on an FP64 context is
+    accepted and has no effect."""
+    s = synth.build(synth.config_small(nbnd=16, npw=120, nlf=19, lf="xyz", no=21))
+    ctx = rpa.Context(precision=rpa.PREC_MIXED)
+    ctx.load_system(s)
+    ctx.chi0_prefetch("zz")
+    ctx.chi0(rpa.MODE_CURRENT, want=False, **rpa.optabs_args(s, "xx"))
+    Sl, _ = ctx.chi0(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+    S, Q = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, "zz"))
+    assert ctx.stage_times()["vertices"] > 0
+    So, Qo = orc.optabs_s0(orc.Bound(s, pol="zz"))
+    assert rel(S, So) < TOL and rel(Q, Qo) < TOL
+    assert rel(Sl, orc.sloss_s0(orc.Bound(s))) < TOL
+    ctx.close()
+    f = rpa.Context(precision=rpa.PREC_FP64)
+    f.load_system(s)
+    f.chi0_prefetch("zz")
+    S64, _ = f.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, "xx"))
+    assert rel(S64, orc.optabs_s0(orc.Bound(s, pol="xx"))[0]) < 1e-11
+    f.close()

@@ -99,8 +99,43 @@ __global__ void k_basis_transpose(const double2* __restrict__ src, double2* __re
   }
 }
 
+// The same through shared memory, for nbnd <= 64: a block moves a tile of
+// BT_I plane waves x all bands of one k-point, reading rows of plane waves and
+// writing the tile's contiguous [i][b] run, both coalesced.  The tile row is
+// padded by one element so that eight threads reading one column of 16-byte
+// elements fall in eight different 16-byte bank groups.
+constexpr int BT_I = 64;
+__global__ void k_basis_transpose_tiled(const double2* __restrict__ src, double2* __restrict__ dst, int nkc,
+                                        int nbnd, int npwx) {
+  extern __shared__ double2 bt_tile[];  // [nbnd][BT_I + 1]
+  const int nic = (npwx + BT_I - 1) / BT_I;
+  for (long long blk = blockIdx.x; blk < (long long)nkc * nic; blk += gridDim.x) {
+    const int k = (int)(blk / nic), i0 = (int)(blk % nic) * BT_I;
+    const int ni = min(BT_I, npwx - i0);
+    const double2* s = src + (size_t)k * nbnd * npwx + i0;
+    for (int e = threadIdx.x; e < nbnd * BT_I; e += blockDim.x) {
+      const int b = e / BT_I, ii = e - b * BT_I;
+      if (ii < ni) bt_tile[b * (BT_I + 1) + ii] = s[(size_t)b * npwx + ii];
+    }
+    __syncthreads();
+    double2* d = dst + ((size_t)k * npwx + i0) * nbnd;
+    for (int e = threadIdx.x; e < ni * nbnd; e += blockDim.x) {
+      const int ii = e / nbnd, b = e - ii * nbnd;
+      d[e] = bt_tile[b * (BT_I + 1) + ii];
+    }
+    __syncthreads();
+  }
+}
+
 void launch_basis_transpose(const double2* src, double2* dst, int nkc, int nbnd, int npwx, cudaStream_t s) {
-  k_basis_transpose<<<2048, 256, 0, s>>>(src, dst, nkc, nbnd, npwx);
+  if (nbnd <= 64) {
+    const size_t smem = sizeof(double2) * (size_t)nbnd * (BT_I + 1);
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_basis_transpose_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_basis_transpose_tiled<<<4 * 152, 256, smem, s>>>(src, dst, nkc, nbnd, npwx);
+  } else {
+    k_basis_transpose<<<2048, 256, 0, s>>>(src, dst, nkc, nbnd, npwx);
+  }
 }
 
 // gidx[k][i] = igk(i, k) - 1 (0-based G index), or i for the legacy basis

@@ -759,13 +759,20 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
   std::vector<int> counts;
   int maxp = 0;
   cudaEventRecord(c->ev[0], c->stream);
-  RPA_TRY(count_pairs(c, P, 0, c->ntot, counts, &maxp));
-  // k chunks bounded by the vertex buffer budget
   const bool two = cplx && (a->pol == RPA_POL_YZ || a->pol == RPA_POL_ZY);
-  // vertices of this polarisation computed beside the previous call (rpa_chi0_prefetch)
-  const bool from_stash = c->vstash.valid && c->precision == RPA_PREC_MIXED && cplx && !two &&
-                          c->vstash.pol == a->pol && same_chi0_args(c->vstash.args, *a);
+  // vertices of this polarisation computed beside the previous call
+  // (rpa_chi0_prefetch): that call's transitions, their window-sorted records
+  // and its vertex rows for this polarisation are still on the device (the
+  // same arguments, k map, q and basis give the same transitions)
+  bool from_stash = c->vstash.valid && c->precision == RPA_PREC_MIXED && cplx && !two &&
+                    c->vstash.pol == a->pol && same_chi0_args(c->vstash.args, *a);
   c->vstash.valid = false;
+  if (from_stash) {
+    counts = c->vstash.counts;
+    maxp = c->vstash.maxp;
+  } else {
+    RPA_TRY(count_pairs(c, P, 0, c->ntot, counts, &maxp));
+  }
   const int extra_pol = c->precision == RPA_PREC_MIXED && cplx && !two && c->vertex_kind != 1 &&
                                 c->prefetch_pol >= 0 && c->prefetch_pol != a->pol
                             ? c->prefetch_pol
@@ -784,6 +791,15 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
   const size_t budget = std::max<size_t>((size_t)1 << 30, std::min<size_t>(free_b / 2, (size_t)96 << 30));
   size_t max_trans = std::max<size_t>(budget / per_trans, (size_t)maxp + 1);
   max_trans = std::min<size_t>(max_trans, (size_t)1 << 30);
+  if (from_stash) {
+    long long all = 0;
+    for (int k = 0; k < c->ntot; ++k) all += counts[k];
+    if (all != c->vstash.tot || (size_t)all > max_trans) {
+      // not one chunk any more: count again (the pair scratch is rebuilt too)
+      from_stash = false;
+      RPA_TRY(count_pairs(c, P, 0, c->ntot, counts, &maxp));
+    }
+  }
   int k0 = 0;
   bool stashed = false;
   while (k0 < c->ntot) {
@@ -799,14 +815,20 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
     int wmax = 0, n_inter = 0;
     double winsum = 0;
     cudaEventRecord(c->ev[1], c->stream);
-    RPA_TRY(emit_pairs(c, P, k0, nk, off, tot, &wmax, &n_inter, &winsum));
-    RPA_TRY(sort_trans(c, (int)tot, P.nw));
+    if (from_stash) {
+      n_inter = c->vstash.n_inter;
+      wmax = c->vstash.wmax;
+      winsum = c->vstash.winsum;
+    } else {
+      RPA_TRY(emit_pairs(c, P, k0, nk, off, tot, &wmax, &n_inter, &winsum));
+      RPA_TRY(sort_trans(c, (int)tot, P.nw));
+    }
     if (c->precision == RPA_PREC_MIXED) {
       // FP32 vertices written straight into the window-sorted rows (the
       // transitions and their sorted order are those of the previous call when
       // its stashed rows are used: same arguments, k map, q and basis)
       const bool whole = k0 == 0 && k1 == c->ntot;
-      const bool use_stash = from_stash && whole && tot == c->vstash.tot;
+      const bool use_stash = from_stash && whole;
       const int xpol = whole ? extra_pol : -1;
       const size_t mrows = ((size_t)tot + 31) / 32 * 32 + 32;
       if (use_stash) std::swap(c->d_Mf, c->d_Mf2);
@@ -821,7 +843,7 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
       RPA_CUDA(c, cudaMemsetAsync(Mf + pad0, 0, sizeof(float2) * (pad1 - pad0), c->stream));
       if (two || xpol >= 0) RPA_CUDA(c, cudaMemsetAsync(Mx + pad0, 0, sizeof(float2) * (pad1 - pad0), c->stream));
       int* pos_of = c->d_counts.as<int>();
-      RPA_TRY(inverse_perm(c, (int)tot, pos_of));
+      if (!use_stash) RPA_TRY(inverse_perm(c, (int)tot, pos_of));
       RPA_TRY(ensure(c, c->d_ntrans, 32));
       RPA_CUDA(c, cudaMemsetAsync(c->d_ntrans.p, 0, 32, c->stream));
       cudaEventRecord(c->ev[2], c->stream);
@@ -850,6 +872,11 @@ int rpa_chi0(rpa_ctx* c, const rpa_chi0_args* a, double* S0_out, double* Qeff_ou
         c->vstash.args.pol = xpol;
         c->vstash.tot = tot;
         c->vstash.amax = amM2;
+        c->vstash.counts = counts;
+        c->vstash.maxp = maxp;
+        c->vstash.n_inter = n_inter;
+        c->vstash.wmax = wmax;
+        c->vstash.winsum = winsum;
         stashed = true;
       }
       if (!two) amM2 = amM;

@@ -120,6 +120,9 @@ struct rpa_ctx {
     rpa_chi0_args args{};
     long long tot = 0;
     float amax = 0.f;
+    std::vector<int> counts;  // transitions per FBZ k-point
+    int maxp = 0, n_inter = 0, wmax = 0;
+    double winsum = 0.0;
   } vstash;
   // results
   int last_mode = -1, last_no = 0, last_nw = 0;

@@ -128,6 +128,7 @@ struct VmCfg {
   // it waits for the read-back of the chunk before last (see the worker loop)
   static constexpr bool EARLY = S >= 4;
   static_assert(IMG || EARLY, "three blocks need four stages");
+  static_assert(PTAB_SMEM || NBY <= 32, "the global pair table holds 32 x 32 entries per k-point");
 };
 
 __device__ __forceinline__ void cp16z(uint32_t dst, const void* src, uint32_t src_bytes) {

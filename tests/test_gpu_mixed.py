@@ -157,15 +157,22 @@ def test_current_vertices_32_band_windows(synth, rpa, orc, nbnd, nocc, nlf):
     """Current vertices in 32-band windows (one window, and two windows on
     each side), odd NGloc, plane-wave counts that are not a multiple of the
     32-plane-wave chunk: S0 and Qeff of xx, zz and the yz pair against the
-    oracle."""
+    oracle, then xx with zz prefetched (the two-component pass in every pair
+    of band windows)."""
     s = synth.build(synth.config_small(nbnd=nbnd, nocc=nocc, npw=150, nlf=nlf, no=31))
     ctx = rpa.Context(precision=rpa.PREC_MIXED)
     ctx.load_system(s)
+    ref = {}
     for pol in ("xx", "zz", "yz"):
         So, Qo = orc.optabs_s0(orc.Bound(s, pol=pol))
+        ref[pol] = (So, Qo)
         a, qa = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, pol))
         assert rel(a, So) < TOL
         assert rel(qa, Qo) < TOL
+    ctx.chi0_prefetch("zz")
+    for pol in ("xx", "zz"):
+        a, qa = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, pol))
+        assert rel(a, ref[pol][0]) < TOL and rel(qa, ref[pol][1]) < TOL, pol
     ctx.close()
 
 

@@ -30,10 +30,10 @@
 // One or two column blocks (charge; current, one component): the Y tile holds
 // [y | y'] with y' = (-Im y rows 0-31, Re y rows 32-63), written by the threads
 // that copy the y chunk, and three MMAs of N = 2 NYN per K step give
-// Re D = X . y and Im D = X . y'.  Three blocks: [y | y'] would not leave room
-// for three stages, so the Y tile holds y alone; per K step (16 rows) three
-// MMAs of N = NYN give Re D from the same K rows of X and Y, and three more
-// give Im D from X's rows and the other half of Y's K rows, negated
+// Re D = X . y and Im D = X . y'.  Three blocks (k_vertex_mn_split): [y | y']
+// would not leave room for enough stages, so the Y tile holds y alone; per K
+// step (16 rows) three MMAs of N = NYN give Re D from the same K rows of X and
+// Y, and three more give Im D from X's rows and the other half of Y's K rows, negated
 // (instruction-descriptor bit) where X holds real parts.
 // Small products first: Xl . Yh, Xh . Yl, Xh . Yh.  (The tensor core reads its
 // operands from shared memory at 128 bytes per cycle: an N = 128 MMA just
@@ -176,7 +176,8 @@ __device__ __forceinline__ void tmem_ld_n(uint32_t addr, float* v) {
 template <int NBY, int NB>
 __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
   using Cfg = VmCfg<NBY, NB>;
-  constexpr bool CURRENT = NB > 1, IMG = Cfg::IMG;
+  constexpr bool CURRENT = NB > 1;
+  static_assert(Cfg::IMG && Cfg::PTAB_SMEM, "three column blocks run in k_vertex_mn_split");
   constexpr int NP = CURRENT ? NB - 1 : 1;  // vertex sets written
   constexpr int S = Cfg::S, NYN = Cfg::NYN, CW = Cfg::CW;
   constexpr uint32_t XH = Cfg::XH, YKG = Cfg::YKG, YLO = Cfg::YLO, STAGE = Cfg::STAGE;
@@ -184,9 +185,7 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
   extern __shared__ unsigned char smraw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
   const uint32_t sbase = tc::smem_u32(base);
-  // [a][b]: vertex row of the pair, -1 none
-  int* ptab = Cfg::PTAB_SMEM ? reinterpret_cast<int*>(base + (size_t)S * STAGE)
-                             : V.ptab_g + (size_t)blockIdx.x * 32 * NBY;
+  int* ptab = reinterpret_cast<int*>(base + (size_t)S * STAGE);  // [a][b]: vertex row of the pair, -1 none
   __shared__ uint64_t full[VM_SMAX], done[Cfg::NBUF], tfree[Cfg::NBUF];
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
@@ -237,14 +236,11 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
       constexpr uint32_t N2 = Cfg::N2;
       constexpr int NBF = Cfg::NBUF;
       constexpr uint64_t YG2 = 2 * (YKG >> 4);  // descriptor step of 16 K rows of Y
-      // with images: one MMA over [y | y'];  three blocks: N = NYN for Re D, the
-      // same with B negated for the -X[Re] . Im y part of Im D
-      const uint32_t id = tc::idesc_f16_mn(128, IMG ? N2 : (uint32_t)NYN, false);
-      const uint32_t idn = tc::idesc_f16_mn(128, IMG ? N2 : (uint32_t)NYN, true);
+      // one MMA of N = 64 NTA over [y | y']
+      const uint32_t id = tc::idesc_f16_mn(128, N2, false);
       // descriptors of stage 0; a chunk adds its byte offsets / 16 to the start-address field
       const uint64_t dx0 = tc::desc_sw128_mn(sbase, 1024u, 2048u);
-      const uint64_t dy0 = Cfg::SW64 ? tc::desc_sw64_mn(sbase + 2 * XH, Cfg::AB, YKG)
-                                     : tc::desc_sw128_mn(sbase + 2 * XH, 1024u, YKG);
+      const uint64_t dy0 = tc::desc_sw128_mn(sbase + 2 * XH, 1024u, YKG);
       int last = -1;
       int s = 0, ph = 0;
       for (int t = 0; t < total; ++t) {
@@ -267,14 +263,6 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
           tc::mma_bf16(d, xl, yh, id, acc);  // Xl . Yh
           tc::mma_bf16(d, xh, yl, id, 1u);   // + Xh . Yl
           tc::mma_bf16(d, xh, yh, id, 1u);   // + Xh . Yh
-          if constexpr (!IMG) {
-            // Im D: K rows of X against the other half of Y's K rows
-            const uint64_t ih = dy + (uint64_t)(ks ^ 2) * YG2, il = ih + (YLO >> 4);
-            const uint32_t ii = ks < 2 ? idn : id;
-            tc::mma_bf16(d + (uint32_t)NYN, xl, ih, ii, acc);
-            tc::mma_bf16(d + (uint32_t)NYN, xh, il, ii, 1u);
-            tc::mma_bf16(d + (uint32_t)NYN, xh, ih, ii, 1u);
-          }
         }
         tc::mma_commit(&done[t % NBF]);
         last = t;
@@ -298,7 +286,6 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
     constexpr int YCH = NYN / 8, YE = 128 * YCH, YV = (YE + VM_WORKERS - 1) / VM_WORKERS;
     const __half* ysrc_c = V.planes + (size_t)kY * V.npwx * pstride;
     const __half* ysrc_b1 = CURRENT ? V.ybt + (size_t)kl * V.nsum_max * pstride : nullptr;
-    const __half* ysrc_b2 = NB == 3 ? V.ybt2 + (size_t)kl * V.nsum_max * pstride : nullptr;
     // per copy: its place in y (and y'), its source for chunk 0 (a chunk adds
     // its plane-wave offset), the chunk start from which it is a zero fill
     // (beyond nsum, or a band beyond the window), the imaginary-part flag
@@ -319,18 +306,12 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
         const int col = 8 * j, u = 2 * half + part;
         const int blk = col / NBY;
         const int band = V.ys + col - blk * NBY;
-        if constexpr (Cfg::SW64)
-          ydst[v] = 2 * XH + (uint32_t)(kk >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(col >> 5) * 512u +
-                    (uint32_t)(kk & 7) * 64u + ((uint32_t)(((col >> 3) & 3) ^ ((kk & 7) >> 1)) << 4);
-        else
-          ydst[v] = 2 * XH + (uint32_t)(kk >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(col >> 6) * 1024u +
-                    (uint32_t)(kk & 7) * 128u + ((uint32_t)(((col >> 3) & 7) ^ (kk & 7)) << 4);
-        if constexpr (IMG) {
-          const int ki = kk ^ 32, ci = NYN + col;  // y' row and column of the chunk
-          yidst[v] = 2 * XH + (uint32_t)(ki >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(ci >> 6) * 1024u +
-                     (uint32_t)(ki & 7) * 128u + ((uint32_t)(((ci >> 3) & 7) ^ (ki & 7)) << 4);
-        }
-        const __half* bp = blk == 0 ? ysrc_c : (blk == 1 ? ysrc_b1 : ysrc_b2);
+        ydst[v] = 2 * XH + (uint32_t)(kk >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(col >> 6) * 1024u +
+                  (uint32_t)(kk & 7) * 128u + ((uint32_t)(((col >> 3) & 7) ^ (kk & 7)) << 4);
+        const int ki = kk ^ 32, ci = NYN + col;  // y' row and column of the chunk
+        yidst[v] = 2 * XH + (uint32_t)(ki >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(ci >> 6) * 1024u +
+                   (uint32_t)(ki & 7) * 128u + ((uint32_t)(((ci >> 3) & 7) ^ (ki & 7)) << 4);
+        const __half* bp = blk == 0 ? ysrc_c : ysrc_b1;
         ycp[v] = true;
         yneg[v] = part != 0;
         ysb[v] = bp + (size_t)pw * pstride + (band < V.nbp ? u * V.nbp + band : 0);
@@ -341,15 +322,13 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
     // y' images of the chunks this thread copied into a stage
     constexpr uint32_t NEG = 0x80008000u;
     auto form = [&](int stage) {
-      if constexpr (IMG) {
-        const uint32_t st = sbase + (uint32_t)stage * STAGE;
+      const uint32_t st = sbase + (uint32_t)stage * STAGE;
 #pragma unroll
-        for (int v = 0; v < YV; ++v) {
-          if (!ycp[v]) continue;
-          uint4 w = lds16(st + ydst[v]);
-          if (yneg[v]) w = make_uint4(w.x ^ NEG, w.y ^ NEG, w.z ^ NEG, w.w ^ NEG);
-          sts16(st + yidst[v], w);
-        }
+      for (int v = 0; v < YV; ++v) {
+        if (!ycp[v]) continue;
+        uint4 w = lds16(st + ydst[v]);
+        if (yneg[v]) w = make_uint4(w.x ^ NEG, w.y ^ NEG, w.z ^ NEG, w.w ^ NEG);
+        sts16(st + yidst[v], w);
       }
     };
 
@@ -568,6 +547,354 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
   if (warp == 0) tc::tmem_dealloc(taddr, Cfg::NCOL);
 }
 
+// The three-block pass (two Cartesian components) with the worker roles split:
+// warps 0-7 read the TMEM accumulators back (two per lane quadrant, 16 of the
+// window's columns of each block), warps 8-15 gather and copy the stages and
+// signal them, warp 16 issues the MMAs and commits, besides each chunk's
+// accumulator, the release of its stage.  The roles advance independently: a
+// chunk is signalled as soon as its copies land, a stage is refilled as soon
+// as its MMAs are done, an accumulator is freed as soon as it is read back.
+// Registers (setmaxnreg): 256 x 128 (read-back) + 256 x 64 (copies) + 32 x 96
+// (MMA warp) = 544 x 96, the launch's allocation.
+constexpr int VS_CONS = 8, VS_PROD = 8;  // warps
+constexpr int VS_REG_CONS = 128, VS_REG_PROD = 64;
+static_assert(32 * (VS_CONS * VS_REG_CONS + VS_PROD * VS_REG_PROD + 96) == VM_THREADS * 96, "register split");
+
+template <int NBY>
+__global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn_split(VtxMnCtx V) {
+  using Cfg = VmCfg<NBY, 3>;
+  constexpr int NP = 2;  // vertex sets written
+  constexpr int S = Cfg::S, NYN = Cfg::NYN, NBF = Cfg::NBUF;
+  constexpr uint32_t XH = Cfg::XH, YKG = Cfg::YKG, YLO = Cfg::YLO, STAGE = Cfg::STAGE, N2 = Cfg::N2;
+  constexpr int CW = NBY / 2;  // columns of each block per read-back thread
+  constexpr int CH = CW / 2;
+  static_assert(!Cfg::IMG && Cfg::SW64 && !Cfg::PTAB_SMEM && S >= 4, "three-block layout");
+
+  extern __shared__ unsigned char smraw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+  const uint32_t sbase = tc::smem_u32(base);
+  int* ptab = V.ptab_g + (size_t)blockIdx.x * 32 * NBY;  // [a][b]: vertex row of the pair, -1 none
+  __shared__ uint64_t full[VM_SMAX], sfree[VM_SMAX], done[NBF], tfree[NBF];
+  __shared__ uint32_t tslot;
+  __shared__ volatile int abort_flag;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int kl = blockIdx.x, ik = V.k0 + kl;
+  const long long t0 = V.offsets[kl], t1 = V.offsets[kl + 1];
+  if (t1 == t0) return;
+  const int* km = V.kmap + 5 * ik;
+  const int K1 = km[0], K2 = km[2];
+  const int kX = V.swap ? K1 : K2, kY = V.swap ? K2 : K1;
+  const int nsum = V.legacy ? V.nsum_legacy : V.npw[kY];
+  const int nchunk = (nsum + VM_I - 1) / VM_I;
+  const int GPT = V.gpt, XB = V.xb;
+  const int ngt = (V.nlf + GPT - 1) / GPT;
+  const int total = ngt * nchunk;
+
+  if (warp == 0) {
+    tc::tmem_alloc(&tslot, Cfg::NCOL);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) {
+      tc::mbar_init(&full[s], VS_PROD);
+      tc::mbar_init(&sfree[s], 1);
+    }
+    for (int b = 0; b < NBF; ++b) {
+      tc::mbar_init(&done[b], 1);
+      tc::mbar_init(&tfree[b], VS_CONS);
+    }
+    abort_flag = 0;
+    tc::fence_mbar_init();
+  }
+  for (int e = tid; e < XB * NBY; e += VM_THREADS) ptab[e] = -1;
+  __syncthreads();
+  for (long long t = t0 + tid; t < t1; t += VM_THREADS) {
+    const int nm = V.trans[t].nm;
+    const int n = nm & 0xffff, m = nm >> 16;
+    const int xa = V.swap ? n : m, yb = V.swap ? m : n;
+    if (xa >= V.xo0 && xa < V.xo1 && yb >= V.yo0 && yb < V.yo1)
+      ptab[(xa - V.xs) * NBY + (yb - V.ys)] = V.pos_of[t];
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t taddr = tslot;
+  auto fail_status = [&]() {
+    atomicExch(V.status, 1);
+    abort_flag = 1;
+  };
+  struct Cur {
+    int gt, c;
+  };
+  auto advance = [&](Cur& u) {
+    if (++u.c == nchunk) u.c = 0, ++u.gt;
+  };
+  // plane-wave chunk swept at position c of tile gt (alternating direction)
+  auto chunk_of = [&](Cur u) { return (u.gt & 1) ? nchunk - 1 - u.c : u.c; };
+
+  if (warp == VM_WORKERS / 32) {
+    // ---------------------------------------------------------------- MMA warp
+    if (lane == 0) {
+      constexpr uint64_t YG2 = 2 * (YKG >> 4);
+      const uint32_t id = tc::idesc_f16_mn(128, (uint32_t)NYN, false);
+      const uint32_t idn = tc::idesc_f16_mn(128, (uint32_t)NYN, true);
+      const uint64_t dx0 = tc::desc_sw128_mn(sbase, 1024u, 2048u);
+      const uint64_t dy0 = tc::desc_sw64_mn(sbase + 2 * XH, Cfg::AB, YKG);
+      int last = -1, s = 0, ph = 0;
+      for (int t = 0; t < total; ++t) {
+        if (abort_flag) break;
+        if (!tc::mbar_wait(&full[s], (uint32_t)ph, VM_SPINS) ||
+            (t >= NBF && !tc::mbar_wait(&tfree[t % NBF], (uint32_t)((t / NBF - 1) & 1), VM_SPINS))) {
+          fail_status();
+          break;
+        }
+        tc::tc_fence_after();
+        const uint64_t so = (uint64_t)(((uint32_t)s * STAGE) >> 4);
+        const uint64_t dx = dx0 + so, dy = dy0 + so;
+        const uint32_t d = taddr + (uint32_t)((t % NBF) * N2);
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+          const uint64_t xh = dx + (uint64_t)(ks * 256), xl = xh + (XH >> 4);
+          const uint64_t yh = dy + (uint64_t)ks * YG2, yl = yh + (YLO >> 4);
+          const uint32_t acc = ks > 0 ? 1u : 0u;
+          tc::mma_bf16(d, xl, yh, id, acc);  // Xl . Yh
+          tc::mma_bf16(d, xh, yl, id, 1u);   // + Xh . Yl
+          tc::mma_bf16(d, xh, yh, id, 1u);   // + Xh . Yh
+          // Im D: K rows of X against the other half of Y's K rows
+          const uint64_t ih = dy + (uint64_t)(ks ^ 2) * YG2, il = ih + (YLO >> 4);
+          const uint32_t ii = ks < 2 ? idn : id;
+          tc::mma_bf16(d + (uint32_t)NYN, xl, ih, ii, acc);
+          tc::mma_bf16(d + (uint32_t)NYN, xh, il, ii, 1u);
+          tc::mma_bf16(d + (uint32_t)NYN, xh, ih, ii, 1u);
+        }
+        tc::mma_commit(&done[t % NBF]);
+        tc::mma_commit(&sfree[s]);
+        last = t;
+        if (++s == S) s = 0, ph ^= 1;
+      }
+      if (last >= 0) tc::mbar_wait(&done[last % NBF], (uint32_t)((last / NBF) & 1), VM_SPINS);
+    }
+  } else if (warp < VS_CONS) {
+    // ------------------------------------------------------------ read-back warps
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(VS_REG_CONS));
+    const int wq = warp & 3, hc = warp >> 2;  // lane quadrant, column half of each block
+    const int row_t = wq * 32 + lane;
+    const int eg = row_t / XB, ea = row_t - eg * XB;
+    float2 accR[NP][CH], accI[NP][CH];
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+#pragma unroll
+      for (int j = 0; j < CH; ++j) accR[p][j] = accI[p][j] = make_float2(0.f, 0.f);
+    float fa[NP];
+    auto set_afac = [&](int gt) {
+      const int G = gt * GPT + eg;
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        fa[p] = 0.f;
+        if (eg < GPT && G < V.nlf) {
+          const double* kv = V.ktot + 3 * ik;
+          const double* gl = V.Glf + 3 * G;
+          const int mu = p == 0 ? V.comp : V.comp2;
+          const double qmu = mu == 0 ? V.q0 : (mu == 1 ? V.q1 : V.q2);
+          fa[p] = (float)(0.5 * V.Gcar * (qmu + 2.0 * kv[mu] + gl[mu])) * V.a_scale;
+        }
+      }
+    };
+    // acc[p] += fa[p] * D[c] + D[b_p c] over this thread's columns of one part
+    auto add_block = [&](const float (&vc)[CW], const float (&vb)[CW], int p, float2 (&acc)[NP][CH]) {
+      const float2 f2 = make_float2(fa[p], fa[p]);
+#pragma unroll
+      for (int j = 0; j < CH; ++j)
+        acc[p][j] = __fadd2_rn(acc[p][j], __ffma2_rn(f2, make_float2(vc[2 * j], vc[2 * j + 1]),
+                                                     make_float2(vb[2 * j], vb[2 * j + 1])));
+    };
+    float amx[NP] = {0.f, 0.f};
+    auto write_out = [&](int gt) {
+      const int G = gt * GPT + eg;
+      if (eg < GPT && G < V.nlf) {
+#pragma unroll
+        for (int j = 0; j < CW; ++j) {
+          const int r = ptab[ea * NBY + hc * CW + j];
+          if (r >= 0) {
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+              const float ar = (j & 1) ? accR[p][j >> 1].y : accR[p][j >> 1].x;
+              const float ai = (j & 1) ? accI[p][j >> 1].y : accI[p][j >> 1].x;
+              const float re = ar * V.out_scale, im = ai * V.out_scale;
+              (p == 0 ? V.M : V.M2)[(size_t)r * V.nlf + G] = make_float2(re, im);
+              amx[p] = fmaxf(amx[p], fmaxf(fabsf(re), fabsf(im)));
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int p = 0; p < NP; ++p)
+#pragma unroll
+        for (int j = 0; j < CH; ++j) accR[p][j] = accI[p][j] = make_float2(0.f, 0.f);
+    };
+    set_afac(0);
+    Cur uc = {0, 0};
+    bool fail = false;
+    for (int t = 0; t < total; ++t) {
+      if (!tc::mbar_wait(&done[t % NBF], (uint32_t)((t / NBF) & 1), VM_SPINS)) {
+        fail_status();
+        fail = true;
+        break;
+      }
+      tc::tc_fence_after();
+      const uint32_t ad = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)((t % NBF) * N2 + hc * CW);
+      float vc[CW], vb[CW];
+#pragma unroll
+      for (int part = 0; part < 2; ++part) {
+        const uint32_t a = ad + (uint32_t)(part * NYN);
+        tmem_ld_n<CW>(a, vc);
+        tmem_ld_n<CW>(a + NBY, vb);
+        tc::tmem_ld_wait();
+        add_block(vc, vb, 0, part == 0 ? accR : accI);
+        tmem_ld_n<CW>(a + 2 * NBY, vb);
+        tc::tmem_ld_wait();
+        add_block(vc, vb, 1, part == 0 ? accR : accI);
+      }
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&tfree[t % NBF]);
+      if (uc.c == nchunk - 1) {
+        write_out(uc.gt);
+        set_afac(uc.gt + 1);
+      }
+      advance(uc);
+      if (abort_flag) {
+        fail = true;
+        break;
+      }
+    }
+    (void)fail;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      float a = amx[p];
+      for (int o = 16; o > 0; o >>= 1) a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+      if (lane == 0) atomicMax(V.amax + p, __float_as_uint(a));
+    }
+  } else {
+    // ------------------------------------------------------------- copy warps
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(VS_REG_PROD));
+    const int ptid = tid - 32 * VS_CONS;  // 0 .. 255
+    // X copies: plane waves xpw and xpw + 16 of the chunk, rows 8 xj .. 8 xj + 7,
+    // the four planes each
+    const int xpw = ptid >> 4, xj = ptid & 15;
+    const int xrow = 8 * xj, xg = xrow / XB, xb0 = xrow - xg * XB;
+    const bool xok = xg < GPT && V.xs + xb0 < V.nbp;
+    auto xoff_of = [&](int pw) {
+      return (uint32_t)(pw >> 3) * 2048u + (uint32_t)(xj >> 3) * 1024u + (uint32_t)(pw & 7) * 128u +
+             ((uint32_t)((xj & 7) ^ (pw & 7)) << 4);
+    };
+    const uint32_t xoffA = xoff_of(xpw), xoffB = xoff_of(xpw + 16);
+    const size_t pstride = (size_t)4 * V.nbp;
+    const __half* xsrc = V.planes + (size_t)kX * V.npwx * pstride + V.xs + xb0;
+    const int16_t* mp = V.map + (size_t)kl * V.nlf * V.nsum_max + xpw;
+    // Y copies: e = ptid + 256 v over 2 halves x 64 K rows x NYN / 8 chunks
+    constexpr int YCH = NYN / 8, YE = 128 * YCH, YV = YE / (32 * VS_PROD);
+    static_assert(YE % (32 * VS_PROD) == 0, "Y copies per thread");
+    const __half* ysrc_c = V.planes + (size_t)kY * V.npwx * pstride;
+    const __half* ysrc_b1 = V.ybt + (size_t)kl * V.nsum_max * pstride;
+    const __half* ysrc_b2 = V.ybt2 + (size_t)kl * V.nsum_max * pstride;
+    uint32_t ydst[YV];
+    const __half* ysb[YV];
+    int ylim[YV];
+#pragma unroll
+    for (int v = 0; v < YV; ++v) {
+      const int e = ptid + 32 * VS_PROD * v;
+      const int line = e / YCH, j = e - line * YCH;
+      const int half = line >> 6, kk = line & 63, part = kk >> 5, pw = kk & 31;
+      const int col = 8 * j, u = 2 * half + part;
+      const int blk = col / NBY;
+      const int band = V.ys + col - blk * NBY;
+      ydst[v] = 2 * XH + (uint32_t)(kk >> 3) * YKG + (uint32_t)half * YLO + (uint32_t)(col >> 5) * 512u +
+                (uint32_t)(kk & 7) * 64u + ((uint32_t)(((col >> 3) & 3) ^ ((kk & 7) >> 1)) << 4);
+      const __half* bp = blk == 0 ? ysrc_c : (blk == 1 ? ysrc_b1 : ysrc_b2);
+      ysb[v] = bp + (size_t)pw * pstride + (band < V.nbp ? u * V.nbp + band : 0);
+      ylim[v] = band < V.nbp ? nsum - pw : 0;
+    }
+    // Gfast positions of the chunk's two plane waves, -1: none
+    auto load_pos = [&](Cur u, int& pa, int& pb) {
+      const int G = u.gt * GPT + xg;
+      if (u.gt >= ngt || !xok || G >= V.nlf) {
+        pa = pb = -1;
+        return;
+      }
+      const int16_t* q = mp + (size_t)G * V.nsum_max + chunk_of(u) * VM_I;
+      pa = (int)q[0];
+      pb = (int)q[16];
+    };
+    auto issue = [&](Cur u, int stage, int pa, int pb) {
+      if (u.gt < ngt) {
+        const uint32_t st = sbase + (uint32_t)stage * STAGE;
+        const __half* sa = xsrc + (size_t)(pa >= 0 ? pa : 0) * pstride;
+        const __half* sb = xsrc + (size_t)(pb >= 0 ? pb : 0) * pstride;
+        const uint32_t za = pa >= 0 ? 16u : 0u, zb = pb >= 0 ? 16u : 0u;
+#pragma unroll
+        for (int u4 = 0; u4 < 4; ++u4) {
+          const uint32_t o = (uint32_t)(u4 >> 1) * XH + (uint32_t)(u4 & 1) * 8192u;
+          cp16z(st + xoffA + o, sa + u4 * V.nbp, za);
+          cp16z(st + xoffB + o, sb + u4 * V.nbp, zb);
+        }
+        const int i0 = chunk_of(u) * VM_I;
+        const size_t off = (size_t)i0 * pstride;
+#pragma unroll
+        for (int v = 0; v < YV; ++v) {
+          const bool ok = i0 < ylim[v];
+          cp16z(st + ydst[v], ok ? ysb[v] + off : ysrc_c, ok ? 16u : 0u);
+        }
+      }
+      cp_commit();
+    };
+    auto signal = [&](int s) {
+      tc::fence_async_smem();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&full[s]);
+    };
+    // chunks 0 .. S - 2 in flight, positions one chunk ahead
+    Cur ui = {0, 0};
+    int pa = 0, pb = 0, na = 0, nb = 0;
+    load_pos(ui, pa, pb);
+#pragma unroll 1
+    for (int s = 0; s < S - 1; ++s) {
+      Cur un = ui;
+      advance(un);
+      load_pos(un, na, nb);
+      issue(ui, s, pa, pb);
+      ui = un;
+      pa = na;
+      pb = nb;
+    }
+    cp_wait<S - 2>();
+    signal(0);
+    // step j: chunk j + 1 (issued S - 2 steps ago) signalled, then chunk
+    // j + S - 1 issued into the stage of chunk j - 1 once its MMAs are done
+    for (int j = 0; j < total; ++j) {
+      cp_wait<S - 3>();
+      if (j + 1 < total) signal((j + 1) % S);
+      if (j >= 1 && !tc::mbar_wait(&sfree[(j - 1) % S], (uint32_t)(((j - 1) / S) & 1), VM_SPINS)) {
+        fail_status();
+        break;
+      }
+      Cur un = ui;
+      advance(un);
+      load_pos(un, na, nb);
+      issue(ui, (j + S - 1) % S, pa, pb);
+      ui = un;
+      pa = na;
+      pb = nb;
+      if (abort_flag) break;
+    }
+    cp_wait<0>();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, Cfg::NCOL);
+}
+
 // b(i) c of every FBZ k-point of the launch, split like the coefficient planes:
 // ybt[k_local][i][plane][band], b(i) = Gcar (R1 G1_i)_mu sB / 2^14 (zero beyond
 // nsum), c the planes of K1; (h + l) b is split again into fp16 hi + lo.  With
@@ -653,6 +980,17 @@ static int launch_vmn(rpa_ctx* c, const VtxMnCtx& V, int nk) {
   return RPA_OK;
 }
 
+template <int NBY>
+static int launch_vmn_split(rpa_ctx* c, const VtxMnCtx& V, int nk) {
+  using Cfg = VmCfg<NBY, 3>;
+  auto kern = k_vertex_mn_split<NBY>;
+  RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
+  kern<<<nk, VM_THREADS, Cfg::SMEM, c->stream>>>(V);
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  return RPA_OK;
+}
+
 // nb: column blocks of Y (1 charge, 2 current, 3 current with two components)
 static int launch_vmn_nby(rpa_ctx* c, const VtxMnCtx& V, int nk, int nby, int nb) {
   if (nb == 1) {
@@ -664,8 +1002,8 @@ static int launch_vmn_nby(rpa_ctx* c, const VtxMnCtx& V, int nk, int nby, int nb
     if (nby == 16) return launch_vmn<16, 2>(c, V, nk);
     if (nby == 32) return launch_vmn<32, 2>(c, V, nk);
   } else if (nb == 3) {
-    if (nby == 16) return launch_vmn<16, 3>(c, V, nk);
-    if (nby == 32) return launch_vmn<32, 3>(c, V, nk);
+    if (nby == 16) return launch_vmn_split<16>(c, V, nk);
+    if (nby == 32) return launch_vmn_split<32>(c, V, nk);
   }
   return fail(c, RPA_EINVAL, "vertices: no kernel for a %d-band window with %d column blocks", nby, nb);
 }

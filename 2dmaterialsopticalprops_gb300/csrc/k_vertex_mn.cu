@@ -172,6 +172,21 @@ __device__ __forceinline__ void tmem_ld_n(uint32_t addr, float* v) {
   }
 }
 
+// the vertex rows of CW consecutive columns of band row a of the pair table
+template <int CW>
+__device__ __forceinline__ void load_rows(const int* ptab, int (&rr)[CW]) {
+  static_assert(CW % 4 == 0, "pair-table row slice");
+  const int4* pt = reinterpret_cast<const int4*>(ptab);
+#pragma unroll
+  for (int q = 0; q < CW / 4; ++q) {
+    const int4 w = pt[q];
+    rr[4 * q] = w.x;
+    rr[4 * q + 1] = w.y;
+    rr[4 * q + 2] = w.z;
+    rr[4 * q + 3] = w.w;
+  }
+}
+
 // One CTA per FBZ k-point of the launch.
 template <int NBY, int NB>
 __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
@@ -438,16 +453,21 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
       const int G = gt * GPT + eg;
       if (eg < GPT && G < V.nlf) {
 #pragma unroll
-        for (int j = 0; j < CW; ++j) {
-          const int r = ptab[ea * NBY + cg * CW + j];
-          if (r >= 0) {
+        for (int q = 0; q < CW / 4; ++q) {
+          int rr[4];  // vertex rows of columns 4 q .. 4 q + 3
+          load_rows<4>(ptab + ea * NBY + cg * CW + 4 * q, rr);
 #pragma unroll
-            for (int p = 0; p < NP; ++p) {
-              const float ar = (j & 1) ? accR[p][j >> 1].y : accR[p][j >> 1].x;
-              const float ai = (j & 1) ? accI[p][j >> 1].y : accI[p][j >> 1].x;
-              const float re = ar * V.out_scale, im = ai * isign;
-              (p == 0 ? V.M : V.M2)[(size_t)r * V.nlf + G] = make_float2(re, im);
-              amx[p] = fmaxf(amx[p], fmaxf(fabsf(re), fabsf(im)));
+          for (int i = 0; i < 4; ++i) {
+            const int j = 4 * q + i, r = rr[i];
+            if (r >= 0) {
+#pragma unroll
+              for (int p = 0; p < NP; ++p) {
+                const float ar = (j & 1) ? accR[p][j >> 1].y : accR[p][j >> 1].x;
+                const float ai = (j & 1) ? accI[p][j >> 1].y : accI[p][j >> 1].x;
+                const float re = ar * V.out_scale, im = ai * isign;
+                (p == 0 ? V.M : V.M2)[(size_t)r * V.nlf + G] = make_float2(re, im);
+                amx[p] = fmaxf(amx[p], fmaxf(fabsf(re), fabsf(im)));
+              }
             }
           }
         }
@@ -554,10 +574,10 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
 // accumulator, the release of its stage.  The roles advance independently: a
 // chunk is signalled as soon as its copies land, a stage is refilled as soon
 // as its MMAs are done, an accumulator is freed as soon as it is read back.
-// Registers (setmaxnreg): 256 x 128 (read-back) + 256 x 64 (copies) + 32 x 96
+// Registers (setmaxnreg): 256 x 136 (read-back) + 256 x 56 (copies) + 32 x 96
 // (MMA warp) = 544 x 96, the launch's allocation.
 constexpr int VS_CONS = 8, VS_PROD = 8;  // warps
-constexpr int VS_REG_CONS = 128, VS_REG_PROD = 64;
+constexpr int VS_REG_CONS = 136, VS_REG_PROD = 56;
 static_assert(32 * (VS_CONS * VS_REG_CONS + VS_PROD * VS_REG_PROD + 96) == VM_THREADS * 96, "register split");
 
 template <int NBY>
@@ -686,21 +706,23 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn_split(VtxMnCtx V) {
     for (int p = 0; p < NP; ++p)
 #pragma unroll
       for (int j = 0; j < CH; ++j) accR[p][j] = accI[p][j] = make_float2(0.f, 0.f);
-    float fa[NP];
-    auto set_afac = [&](int gt) {
+    // a(G) of each vertex set for this thread's local field of tile gt
+    auto afac = [&](int gt, float (&f)[NP]) {
       const int G = gt * GPT + eg;
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
-        fa[p] = 0.f;
+        f[p] = 0.f;
         if (eg < GPT && G < V.nlf) {
           const double* kv = V.ktot + 3 * ik;
           const double* gl = V.Glf + 3 * G;
           const int mu = p == 0 ? V.comp : V.comp2;
           const double qmu = mu == 0 ? V.q0 : (mu == 1 ? V.q1 : V.q2);
-          fa[p] = (float)(0.5 * V.Gcar * (qmu + 2.0 * kv[mu] + gl[mu])) * V.a_scale;
+          f[p] = (float)(0.5 * V.Gcar * (qmu + 2.0 * kv[mu] + gl[mu])) * V.a_scale;
         }
       }
     };
+    float fa[NP], fn[NP];
+    afac(0, fa);
     // acc[p] += fa[p] * D[c] + D[b_p c] over this thread's columns of one part
     auto add_block = [&](const float (&vc)[CW], const float (&vb)[CW], int p, float2 (&acc)[NP][CH]) {
       const float2 f2 = make_float2(fa[p], fa[p]);
@@ -710,33 +732,63 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn_split(VtxMnCtx V) {
                                                      make_float2(vb[2 * j], vb[2 * j + 1])));
     };
     float amx[NP] = {0.f, 0.f};
-    auto write_out = [&](int gt) {
-      const int G = gt * GPT + eg;
-      if (eg < GPT && G < V.nlf) {
+    // A finished tile's sums wait in TMEM, in the columns past the accumulator
+    // ring ([column][p][Re, Im] per thread), and go out a few columns per chunk
+    // of the next tile while the read-back warps wait for the MMAs: written
+    // all at once they held up the read-back, and with it the MMA warp, for
+    // the time of the tile's scattered row stores.
+    constexpr uint32_t STASH = (uint32_t)(NBF * N2);
+    static_assert(STASH + 8 * CW <= Cfg::NCOL, "stash beyond the TMEM allocation");
+    const uint32_t stash = taddr + ((uint32_t)(wq * 32) << 16) + STASH + (uint32_t)(hc * 4 * CW);
+    const int* prow = ptab + ea * NBY + hc * CW;  // vertex rows of this thread's columns
+    const int dper = nchunk > 1 ? (CW + nchunk - 2) / (nchunk - 1) : CW;  // columns written per chunk
+    int sj = CW;     // next stashed column to write (CW: none left)
+    int sG = -1;     // local field of the stashed tile (-1: padding row)
+    int srow = -1;   // vertex row of column sj
+    auto drain = [&](int n) {
+#pragma unroll 1
+      for (int i = 0; i < n && sj < CW; ++i, ++sj) {
+        float v[4];
+        tc::tmem_ld4(stash + (uint32_t)(4 * sj), v);
+        tc::tmem_ld_wait();
+        const int r = srow;
+        if (sj + 1 < CW) srow = prow[sj + 1];
+        if (sG >= 0 && r >= 0) {
 #pragma unroll
-        for (int j = 0; j < CW; ++j) {
-          const int r = ptab[ea * NBY + hc * CW + j];
-          if (r >= 0) {
-#pragma unroll
-            for (int p = 0; p < NP; ++p) {
-              const float ar = (j & 1) ? accR[p][j >> 1].y : accR[p][j >> 1].x;
-              const float ai = (j & 1) ? accI[p][j >> 1].y : accI[p][j >> 1].x;
-              const float re = ar * V.out_scale, im = ai * V.out_scale;
-              (p == 0 ? V.M : V.M2)[(size_t)r * V.nlf + G] = make_float2(re, im);
-              amx[p] = fmaxf(amx[p], fmaxf(fabsf(re), fabsf(im)));
-            }
+          for (int p = 0; p < NP; ++p) {
+            const float re = v[2 * p] * V.out_scale, im = v[2 * p + 1] * V.out_scale;
+            (p == 0 ? V.M : V.M2)[(size_t)r * V.nlf + sG] = make_float2(re, im);
+            amx[p] = fmaxf(amx[p], fmaxf(fabsf(re), fabsf(im)));
           }
         }
       }
+    };
+    auto stash_tile = [&](int gt) {
+      drain(CW);
+#pragma unroll
+      for (int j = 0; j < CW; ++j) {
+        const int h = j >> 1;
+        const bool od = j & 1;
+        tc::tmem_st4(stash + (uint32_t)(4 * j), __float_as_uint(od ? accR[0][h].y : accR[0][h].x),
+                     __float_as_uint(od ? accI[0][h].y : accI[0][h].x),
+                     __float_as_uint(od ? accR[1][h].y : accR[1][h].x),
+                     __float_as_uint(od ? accI[1][h].y : accI[1][h].x));
+      }
+      tc::tmem_st_wait();
 #pragma unroll
       for (int p = 0; p < NP; ++p)
 #pragma unroll
         for (int j = 0; j < CH; ++j) accR[p][j] = accI[p][j] = make_float2(0.f, 0.f);
+      const int G = gt * GPT + eg;
+      sG = eg < GPT && G < V.nlf ? G : -1;
+      sj = 0;
+      srow = prow[0];
     };
-    set_afac(0);
     Cur uc = {0, 0};
     bool fail = false;
     for (int t = 0; t < total; ++t) {
+      const bool tile_end = uc.c == nchunk - 1;
+      if (tile_end) afac(uc.gt + 1, fn);  // loads in flight across the wait
       if (!tc::mbar_wait(&done[t % NBF], (uint32_t)((t / NBF) & 1), VM_SPINS)) {
         fail_status();
         fail = true;
@@ -759,9 +811,12 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn_split(VtxMnCtx V) {
       tc::tc_fence_before();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&tfree[t % NBF]);
-      if (uc.c == nchunk - 1) {
-        write_out(uc.gt);
-        set_afac(uc.gt + 1);
+      if (tile_end) {
+        stash_tile(uc.gt);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) fa[p] = fn[p];
+      } else {
+        drain(dper);
       }
       advance(uc);
       if (abort_flag) {
@@ -769,6 +824,7 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn_split(VtxMnCtx V) {
         break;
       }
     }
+    drain(CW);
     (void)fail;
 #pragma unroll
     for (int p = 0; p < NP; ++p) {

@@ -256,17 +256,23 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
       // descriptors of stage 0; a chunk adds its byte offsets / 16 to the start-address field
       const uint64_t dx0 = tc::desc_sw128_mn(sbase, 1024u, 2048u);
       const uint64_t dy0 = tc::desc_sw128_mn(sbase + 2 * XH, 1024u, YKG);
+      // the next chunk's barriers are tested while this chunk's MMAs are
+      // queued (a test costs ~150-200 cycles under the kernel's shared-memory
+      // load); only one not yet seen complete is waited for between chunks
       int last = -1;
       int s = 0, ph = 0;
+      bool fnext = false, tnext = false;
       for (int t = 0; t < total; ++t) {
-        if (abort_flag) break;
-        if (!tc::mbar_wait(&full[s], (uint32_t)ph, VM_SPINS) ||
-            (t >= NBF && !tc::mbar_wait(&tfree[t % NBF], (uint32_t)((t / NBF - 1) & 1), VM_SPINS))) {
+        if ((t & 15) == 0 && abort_flag) break;
+        if ((!fnext && !tc::mbar_wait(&full[s], (uint32_t)ph, VM_SPINS)) ||
+            (!tnext && t >= NBF && !tc::mbar_wait(&tfree[t % NBF], (uint32_t)((t / NBF - 1) & 1), VM_SPINS))) {
           atomicExch(V.status, 1);
           abort_flag = 1;
           break;
         }
         tc::tc_fence_after();
+        const int sn = s + 1 == S ? 0 : s + 1;
+        const int phn = sn == 0 ? ph ^ 1 : ph;
         const uint64_t so = (uint64_t)(((uint32_t)s * STAGE) >> 4);
         const uint64_t dx = dx0 + so, dy = dy0 + so;
         const uint32_t d = taddr + (uint32_t)((t % NBF) * N2);
@@ -278,10 +284,14 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
           tc::mma_bf16(d, xl, yh, id, acc);  // Xl . Yh
           tc::mma_bf16(d, xh, yl, id, 1u);   // + Xh . Yl
           tc::mma_bf16(d, xh, yh, id, 1u);   // + Xh . Yh
+          if (ks == 1) fnext = t + 1 >= total || tc::mbar_test_wait(&full[sn], (uint32_t)phn);
+          if (ks == 2)
+            tnext = t + 1 < NBF || tc::mbar_test_wait(&tfree[(t + 1) % NBF], (uint32_t)(((t + 1) / NBF - 1) & 1));
         }
         tc::mma_commit(&done[t % NBF]);
         last = t;
-        if (++s == S) s = 0, ph ^= 1;
+        s = sn;
+        ph = phn;
       }
       if (last >= 0) tc::mbar_wait(&done[last % NBF], (uint32_t)((last / NBF) & 1), VM_SPINS);
     }
@@ -661,15 +671,24 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn_split(VtxMnCtx V) {
       const uint32_t idn = tc::idesc_f16_mn(128, (uint32_t)NYN, true);
       const uint64_t dx0 = tc::desc_sw128_mn(sbase, 1024u, 2048u);
       const uint64_t dy0 = tc::desc_sw64_mn(sbase + 2 * XH, Cfg::AB, YKG);
+      // Under this kernel's shared-memory load an mbarrier test takes
+      // ~150-200 cycles even when the phase is long complete, and the MMAs
+      // of a chunk stop issuing when the tensor core's queue is full: so the
+      // barriers of chunk t + 1 are tested while the MMAs of chunk t are
+      // queued, and only a barrier not yet seen complete is waited for
+      // between chunks (the abort flag is read every 16 chunks).
       int last = -1, s = 0, ph = 0;
+      bool fnext = false, tnext = false;  // barriers of the next chunk seen complete
       for (int t = 0; t < total; ++t) {
-        if (abort_flag) break;
-        if (!tc::mbar_wait(&full[s], (uint32_t)ph, VM_SPINS) ||
-            (t >= NBF && !tc::mbar_wait(&tfree[t % NBF], (uint32_t)((t / NBF - 1) & 1), VM_SPINS))) {
+        if ((t & 15) == 0 && abort_flag) break;
+        if ((!fnext && !tc::mbar_wait(&full[s], (uint32_t)ph, VM_SPINS)) ||
+            (!tnext && t >= NBF && !tc::mbar_wait(&tfree[t % NBF], (uint32_t)((t / NBF - 1) & 1), VM_SPINS))) {
           fail_status();
           break;
         }
         tc::tc_fence_after();
+        const int sn = s + 1 == S ? 0 : s + 1;
+        const int phn = sn == 0 ? ph ^ 1 : ph;
         const uint64_t so = (uint64_t)(((uint32_t)s * STAGE) >> 4);
         const uint64_t dx = dx0 + so, dy = dy0 + so;
         const uint32_t d = taddr + (uint32_t)((t % NBF) * N2);
@@ -687,11 +706,15 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn_split(VtxMnCtx V) {
           tc::mma_bf16(d + (uint32_t)NYN, xl, ih, ii, acc);
           tc::mma_bf16(d + (uint32_t)NYN, xh, il, ii, 1u);
           tc::mma_bf16(d + (uint32_t)NYN, xh, ih, ii, 1u);
+          if (ks == 0) fnext = t + 1 >= total || tc::mbar_test_wait(&full[sn], (uint32_t)phn);
+          if (ks == 2)
+            tnext = t + 1 < NBF || tc::mbar_test_wait(&tfree[(t + 1) % NBF], (uint32_t)(((t + 1) / NBF - 1) & 1));
         }
         tc::mma_commit(&done[t % NBF]);
         tc::mma_commit(&sfree[s]);
         last = t;
-        if (++s == S) s = 0, ph ^= 1;
+        s = sn;
+        ph = phn;
       }
       if (last >= 0) tc::mbar_wait(&done[last % NBF], (uint32_t)((last / NBF) & 1), VM_SPINS);
     }

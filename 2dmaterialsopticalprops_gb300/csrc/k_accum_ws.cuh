@@ -360,7 +360,9 @@ __device__ __forceinline__ void accum_ws_cta(const AccTcCtx& A, const unsigned c
       for (int j = 0; j < CW; ++j) acc[j] = 0.f;
     };
     for (int c = 0; c < nchunks; ++c) {
-      ok = ws_wait(&dfull[c % S], (c / S) & 1, &abort_flag);
+      // the weights of chunk c are written after their warp saw the stage
+      // land (its arrive releases what it observed), so one wait covers both
+      ok = ws_wait(&wready[c & 1], (c >> 1) & 1, &abort_flag);
       if (ok && c >= 2) ok = ws_wait(&mdone[c & 1], ((c - 2) >> 1) & 1, &abort_flag);
       ok = __all_sync(0xffffffffu, ok);
       unsigned char* st = stage(c);
@@ -376,7 +378,6 @@ __device__ __forceinline__ void accum_ws_cta(const AccTcCtx& A, const unsigned c
         if (lane == 0) tc::mbar_arrive(&tfree[sg & 1]);
         if (++consumed % TC_FLUSH == 0) flush();
       }
-      if (ok) ok = __all_sync(0xffffffffu, ws_wait(&wready[c & 1], (c >> 1) & 1, &abort_flag));
       if (!ok) break;
       // A tiles: A = w * (hi + lo) of the staged vertex tile (B1 rows, or the
       // separate A-side tile), re-split

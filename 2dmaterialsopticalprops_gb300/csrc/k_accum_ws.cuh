@@ -367,17 +367,6 @@ __device__ __forceinline__ void accum_ws_cta(const AccTcCtx& A, const unsigned c
       ok = __all_sync(0xffffffffu, ok);
       unsigned char* st = stage(c);
       unsigned char* fs = slot(c);
-      // chunk c-2 done: its slot is free, and for odd c it closed segment
-      // (c - 3) / 2, which is read back now
-      if (ok && c >= 3 && (c & 1)) {
-        const int sg = (c - 3) >> 1;
-        tc::tc_fence_after();
-        consume(sg & 1);
-        tc::tc_fence_before();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&tfree[sg & 1]);
-        if (++consumed % TC_FLUSH == 0) flush();
-      }
       if (!ok) break;
       // A tiles: A = w * (hi + lo) of the staged vertex tile (B1 rows, or the
       // separate A-side tile), re-split
@@ -462,6 +451,18 @@ __device__ __forceinline__ void accum_ws_cta(const AccTcCtx& A, const unsigned c
       if (lane == 0) {
         tc::mbar_arrive(&formed[c & 1]);
         tc::mbar_arrive(&dfree[c % S]);
+      }
+      // chunk c - 2 done: for odd c it closed segment (c - 3) / 2, read back
+      // once chunk c is handed over (the MMA warp needs that TMEM buffer only
+      // for chunk c + 1)
+      if (c >= 3 && (c & 1)) {
+        const int sg = (c - 3) >> 1;
+        tc::tc_fence_after();
+        consume(sg & 1);
+        tc::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&tfree[sg & 1]);
+        if (++consumed % TC_FLUSH == 0) flush();
       }
     }
     // drain: read back the segments the loop did not reach

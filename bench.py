@@ -40,10 +40,10 @@ PKG = "2dmaterialsopticalprops_gb300"
 
 ACC_DRAM_BYTES_PER_PAIR = 30.4e9 / 54.6e6
 # DRAM bytes per FBZ k-point of the vertex launches (k_vertex_mn): ncu measured
-# 16.0 + 0.55 GB (current, xx), 35.97 + 1.21 GB (current, xx and zz in one pass)
-# and 1.30 + 0.18 GB (charge) for the 1600 k-points of the 40x40 case
+# 16.0 + 0.55 GB (current, xx), 34.47 + 1.20 GB (current, xx and zz in one pass)
+# and 1.31 + 0.18 GB (charge) for the 1600 k-points of the 40x40 case
 VTX_DRAM_BYTES_PER_K_CURRENT = 16.56e9 / 1600
-VTX_DRAM_BYTES_PER_K_PAIR = 37.18e9 / 1600
+VTX_DRAM_BYTES_PER_K_PAIR = 35.67e9 / 1600
 VTX_DRAM_BYTES_PER_K_CHARGE = 1.48e9 / 1600
 
 

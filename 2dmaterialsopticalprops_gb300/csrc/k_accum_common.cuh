@@ -36,6 +36,8 @@ struct AccTcCtx {
   int a_lo;             // A-side source: offset of the lo rows
   int n_rows;           // rows of M / M2 (n_inter rounded up to a multiple of 32, zero padded)
   int seg;              // chunks accumulated in one TMEM segment before it is read back
+  const int* order;     // k_accum_ws: frequency-row blocks in launch order (costliest window
+                        // first), null: in index order
 };
 
 constexpr int TC_TT = 32;       // transitions per chunk (K = 64 16-bit values)

@@ -461,6 +461,7 @@ int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const fl
   if (n_inter == 0) return RPA_OK;
   AccTcCtx A;
   A.sym = 0;
+  A.order = nullptr;
   A.rec = c->d_sorted.as<Trans>();
   A.M = Mf;
   A.M2 = Mf2;

@@ -491,7 +491,49 @@ __device__ __forceinline__ void accum_ws_cta(const AccTcCtx& A, const unsigned c
 template <int NIO, bool CPLX, bool SEPA, int GB>
 __global__ void __launch_bounds__(WS_THREADS, 1)
     k_accum_ws(AccTcCtx A, const unsigned char* __restrict__ tiles, const unsigned char* __restrict__ tilesA) {
-  accum_ws_cta<NIO, CPLX, SEPA, GB>(A, tiles, tilesA, blockIdx.x, blockIdx.y, blockIdx.z);
+  accum_ws_cta<NIO, CPLX, SEPA, GB>(A, tiles, tilesA, A.order ? A.order[blockIdx.x] : (int)blockIdx.x, blockIdx.y,
+                                    blockIdx.z);
+}
+
+// Launch order of the frequency-row blocks: costliest window first (chunks
+// of records it sweeps, the same range the CTA computes), so that the last
+// CTAs to start are short ones.  A row's cost varies ~30-fold along the
+// spectrum (few transitions near zero frequency and beyond the band
+// widths), and in index order the last wave held full-cost rows.
+constexpr int WS_ORDER_MAX = 4096;
+static __global__ void __launch_bounds__(1024) k_row_order(const Trans* __restrict__ rec, int n_inter, int wmax, int nrb,
+                                                    int nio, int* __restrict__ order) {
+  __shared__ unsigned long long key[WS_ORDER_MAX];
+  int n = 1;
+  while (n < nrb) n <<= 1;
+  for (int b = threadIdx.x; b < n; b += blockDim.x) {
+    unsigned long long k = ~0ull;  // padding sorts last
+    if (b < nrb) {
+      const int r0 = b * nio;
+      const int ta = lb_lo(rec, n_inter, r0 - wmax + 1) & ~(TC_TT - 1);
+      const int tb = lb_lo(rec, n_inter, r0 + nio);
+      const unsigned cost = (unsigned)max(0, (tb - ta + TC_TT - 1) / TC_TT);
+      k = ((unsigned long long)(~cost) << 32) | (unsigned)b;  // ascending: costliest first, then by index
+    }
+    key[b] = k;
+  }
+  __syncthreads();
+  // bitonic sort, ascending
+  for (int size = 2; size <= n; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const unsigned long long a = key[i], b2 = key[j];
+          if ((a > b2) == ((i & size) == 0)) {
+            key[i] = b2;
+            key[j] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  for (int i = threadIdx.x; i < nrb; i += blockDim.x) order[i] = (int)(key[i] & 0xffffffffu);
 }
 
 // One item of a grouped launch: the accumulation of one q-point (its launch
@@ -587,7 +629,16 @@ static int launch_ws(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char*
   auto kern = k_accum_ws<NIO, CPLX, SEPA, GB>;
   RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
   dim3 grid((nw + NIO - 1) / NIO, A.sym ? A.nht * (A.nht + 1) / 2 : A.nht, A.sym ? 1 : A.nht);
-  kern<<<grid, WS_THREADS, Cfg::SMEM, c->stream>>>(A, tiles, tilesA);
+  AccTcCtx Ao = A;
+  Ao.order = nullptr;
+  if ((int)grid.x <= WS_ORDER_MAX) {
+    RPA_TRY(ensure(c, c->d_order, WS_ORDER_MAX * sizeof(int)));
+    Ao.order = c->d_order.as<int>();
+    k_row_order<<<1, 1024, 0, c->stream>>>(A.rec, A.n_inter, A.wmax, (int)grid.x, NIO, c->d_order.as<int>());
+    RPA_CUDA(c, cudaGetLastError());
+    ++c->launches;
+  }
+  kern<<<grid, WS_THREADS, Cfg::SMEM, c->stream>>>(Ao, tiles, tilesA);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;
   return RPA_OK;

@@ -428,7 +428,7 @@ int rpa_destroy(rpa_ctx* c) {
   DevBuf* bufs[] = {&c->d_miller, &c->d_G, &c->d_box, &c->d_Rc, &c->d_RIc, &c->d_Rcart, &c->d_npw, &c->d_gidx,
                     &c->d_inv, &c->d_coeff, &c->d_coeff32, &c->d_cpl, &c->d_E, &c->d_kmap, &c->d_ktot, &c->d_lf_miller,
                     &c->d_Glf, &c->d_occ, &c->d_counts, &c->d_offsets, &c->d_trans, &c->d_keys, &c->d_keys_alt,
-                    &c->d_vals, &c->d_vals_alt, &c->d_sorted, &c->d_M, &c->d_M2, &c->d_Mf, &c->d_Mf2, &c->d_tiles, &c->d_tilesA, &c->d_gmap, &c->d_ginv, &c->d_vbt, &c->d_ybt, &c->d_ptab, &c->d_cub, &c->d_wmax, &c->d_pairscr,
+                    &c->d_vals, &c->d_vals_alt, &c->d_sorted, &c->d_M, &c->d_M2, &c->d_Mf, &c->d_Mf2, &c->d_tiles, &c->d_tilesA, &c->d_gmap, &c->d_ginv, &c->d_vbt, &c->d_ybt, &c->d_ptab, &c->d_order, &c->d_cub, &c->d_wmax, &c->d_pairscr,
                     &c->d_ntrans, &c->d_S, &c->d_Sdf, &c->d_Q, &c->d_chi0, &c->d_kk[0], &c->d_kk[1], &c->d_kkf[0], &c->d_kkf[1], &c->d_kkw, &c->d_V, &c->d_eps, &c->d_WT,
                     &c->d_flags, &c->d_tmp};
   for (DevBuf* b : bufs) release(*b);

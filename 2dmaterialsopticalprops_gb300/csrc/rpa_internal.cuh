@@ -102,7 +102,7 @@ struct rpa_ctx {
 
   // per-call scratch
   rpa::DevBuf d_occ, d_counts, d_offsets, d_trans, d_keys, d_keys_alt, d_vals, d_vals_alt, d_sorted,
-      d_M, d_M2, d_Mf, d_Mf2, d_tiles, d_tilesA, d_gmap, d_ginv, d_vbt, d_ybt, d_ptab, d_cub, d_wmax, d_ntrans,
+      d_M, d_M2, d_Mf, d_Mf2, d_tiles, d_tilesA, d_gmap, d_ginv, d_vbt, d_ybt, d_ptab, d_order, d_cub, d_wmax, d_ntrans,
       d_pairscr;
   // cached Gfast map (int16) of the last k-chunk, valid until the basis, k map or q change
   bool gmap_valid = false;

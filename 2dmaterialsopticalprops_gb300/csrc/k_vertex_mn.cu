@@ -584,8 +584,9 @@ __global__ void __launch_bounds__(VM_THREADS, 1) k_vertex_mn(VtxMnCtx V) {
 // accumulator, the release of its stage.  The roles advance independently: a
 // chunk is signalled as soon as its copies land, a stage is refilled as soon
 // as its MMAs are done, an accumulator is freed as soon as it is read back.
-// Registers (setmaxnreg): 256 x 136 (read-back) + 256 x 56 (copies) + 32 x 96
-// (MMA warp) = 544 x 96, the launch's allocation.
+// Registers (setmaxnreg, which acts per warpgroup): 256 x 136 (read-back) +
+// 256 x 56 (copies) + 32 x 96 (the MMA warp, alone in its warpgroup, keeps
+// the launch's count) = 544 x 96, the launch's allocation.
 constexpr int VS_CONS = 8, VS_PROD = 8;  // warps
 constexpr int VS_REG_CONS = 136, VS_REG_PROD = 56;
 static_assert(32 * (VS_CONS * VS_REG_CONS + VS_PROD * VS_REG_PROD + 96) == VM_THREADS * 96, "register split");

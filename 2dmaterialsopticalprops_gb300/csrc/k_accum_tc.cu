@@ -531,6 +531,10 @@ int accumulate_tc(rpa_ctx* c, const Chi0Plan& P, int n_inter, int wmax, const fl
       it.nrb = (P.nw + c->acc_last_nio - 1) / c->acc_last_nio;
       it.npy = A.sym ? nhv * (nhv + 1) / 2 : nhv;
       it.npz = A.sym ? 1 : nhv;
+      // its row blocks costliest first, computed now on this context's stream
+      // (its own order buffer; the batch synchronises the stream before the
+      // grouped launch)
+      RPA_TRY(row_order(c, A, it.nrb, c->acc_last_nio, &it.A.order));
       static_assert(sizeof(AccGroupItem) <= sizeof(c->deferred_item), "deferred item storage");
       std::memcpy(c->deferred_item, &it, sizeof it);
       c->deferred = true;

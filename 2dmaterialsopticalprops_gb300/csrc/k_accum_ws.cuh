@@ -536,6 +536,20 @@ static __global__ void __launch_bounds__(1024) k_row_order(const Trans* __restri
   for (int i = threadIdx.x; i < nrb; i += blockDim.x) order[i] = (int)(key[i] & 0xffffffffu);
 }
 
+// Enqueues the row-block order of an accumulation over nrb blocks of nio rows
+// into the context's order buffer; *order stays null (index order) when there
+// are more blocks than the sort holds.
+static int row_order(rpa_ctx* c, const AccTcCtx& A, int nrb, int nio, const int** order) {
+  *order = nullptr;
+  if (nrb > WS_ORDER_MAX) return RPA_OK;
+  RPA_TRY(ensure(c, c->d_order, WS_ORDER_MAX * sizeof(int)));
+  k_row_order<<<1, 1024, 0, c->stream>>>(A.rec, A.n_inter, A.wmax, nrb, nio, c->d_order.as<int>());
+  RPA_CUDA(c, cudaGetLastError());
+  ++c->launches;
+  *order = c->d_order.as<int>();
+  return RPA_OK;
+}
+
 // One item of a grouped launch: the accumulation of one q-point (its launch
 // context and pre-split tiles) and the first CTA of the grouped grid that
 // works on it; its CTAs are numbered as k_accum_ws's grid (nrb row blocks x
@@ -574,7 +588,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
   }
   __syncthreads();
   const long long local = (long long)blockIdx.x - it.cta0;
-  const int bx = (int)(local % it.nrb);
+  const int bl = (int)(local % it.nrb);
+  const int bx = it.A.order ? it.A.order[bl] : bl;  // the q-point's row blocks, costliest first
   const long long rest = local / it.nrb;
   accum_ws_cta<NIO, CPLX, SEPA, GB>(it.A, it.tiles, it.tilesA, bx, (int)(rest % it.npy), (int)(rest / it.npy));
 }
@@ -630,14 +645,7 @@ static int launch_ws(rpa_ctx* c, const AccTcCtx& A, int nw, const unsigned char*
   RPA_CUDA(c, allow_dynamic_smem(kern, c->device));
   dim3 grid((nw + NIO - 1) / NIO, A.sym ? A.nht * (A.nht + 1) / 2 : A.nht, A.sym ? 1 : A.nht);
   AccTcCtx Ao = A;
-  Ao.order = nullptr;
-  if ((int)grid.x <= WS_ORDER_MAX) {
-    RPA_TRY(ensure(c, c->d_order, WS_ORDER_MAX * sizeof(int)));
-    Ao.order = c->d_order.as<int>();
-    k_row_order<<<1, 1024, 0, c->stream>>>(A.rec, A.n_inter, A.wmax, (int)grid.x, NIO, c->d_order.as<int>());
-    RPA_CUDA(c, cudaGetLastError());
-    ++c->launches;
-  }
+  RPA_TRY(row_order(c, A, (int)grid.x, NIO, &Ao.order));
   kern<<<grid, WS_THREADS, Cfg::SMEM, c->stream>>>(Ao, tiles, tilesA);
   RPA_CUDA(c, cudaGetLastError());
   ++c->launches;

@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 PKG = "2dmaterialsopticalprops_gb300"
 
 
-ACC_DRAM_BYTES_PER_PAIR = 30.4e9 / 54.6e6
+ACC_DRAM_BYTES_PER_PAIR = 43.0e9 / 54.6e6
 # DRAM bytes per FBZ k-point of the vertex launches (k_vertex_mn): ncu measured
 # 16.0 + 0.55 GB (current, xx), 34.47 + 1.20 GB (current, xx and zz in one pass)
 # and 1.31 + 0.18 GB (charge) for the 1600 k-points of the 40x40 case
@@ -918,8 +918,9 @@ def main():
                                               "this workload's FBZ k-points (the passes bytes_per_step counts)"})
         pk = peaks.get("bf16_tflops_sustained", 1700.0)
         # DRAM bytes of one complex (Optabs) accumulation launch: ncu measured
-        # 30.4 GB for 54.6 M (transition, frequency) pairs on the 60x60 case,
-        # scaled here by this workload's pairs per launch
+        # 39.9 + 3.1 GB for 54.6 M (transition, frequency) pairs on the 60x60
+        # case (rows costliest first), scaled here by this workload's pairs
+        # per launch
         nwin = [work["stats"][p]["sum_nwin"] for p in ("xx", "zz")]
         traffic = ACC_DRAM_BYTES_PER_PAIR * sum(nwin) / len(nwin)
         roof_acc = {"bound": "tensor", "achieved": achieved_tf, "peak": pk, "unit": "TFLOP/s",

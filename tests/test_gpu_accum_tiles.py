@@ -101,3 +101,28 @@ def test_autotune_accumulation_table(synth, rpa, orc):
         other.tune_import('{"vertex": [], "accum": [{"cplx": 0, "nlf": 40, "nw64": 0, "gb": 80, "nio": 2}]}')
     for c in (ctx, other):
         c.close()
+
+
+def test_row_order_and_its_limit(synth, rpa, orc):
+    """The frequency-row blocks of an accumulation launch run costliest window
+    first (k_row_order sorts up to 4096 blocks); a launch with more blocks
+    keeps index order.  no = 2100: the complex S0 on forced one-row (96, 1)
+    tiles has 4201 blocks (index order); with the default tile and for the
+    real S0 the blocks are sorted.  All against the oracle at the mixed-path
+    tolerance."""
+    s = synth.build(synth.config_small(npw=200, nlf=19, no=2100))
+    So, Qo = orc.optabs_s0(orc.Bound(s, pol="xx"))
+    Ro = orc.sloss_s0(orc.Bound(s))
+    ctx = rpa.Context(precision=rpa.PREC_MIXED, acc_tile=(96, 1))
+    ctx.load_system(s)
+    S, Q = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, "xx"))
+    assert ctx.accum_tile() == (96, 1)
+    assert S.shape == So.shape and rel(S, So) < TOL and rel(Q, Qo) < TOL
+    ctx.close()
+    ctx = rpa.Context(precision=rpa.PREC_MIXED)
+    ctx.load_system(s)
+    S, Q = ctx.chi0(rpa.MODE_CURRENT, **rpa.optabs_args(s, "xx"))
+    assert rel(S, So) < TOL and rel(Q, Qo) < TOL
+    R, _ = ctx.chi0(rpa.MODE_CHARGE, **rpa.sloss_args(s))
+    assert rel(R, Ro) < TOL
+    ctx.close()
